@@ -1,0 +1,178 @@
+"""Build libcudimot_<Model>.so for sm_103a, in-tree.
+
+    python -m cudimot_gb300.build                 # every plugin in mymodels/
+    python -m cudimot_gb300.build --model-dir DIR # any CUDIMOT plugin directory
+
+Like CUDIMOT's Makefile (one binary per mymodels/<Model>), each model plugin
+is compiled into its own library: the generic kernels include the plugin's
+unchanged modelparameters.h / modelfunctions.h / modelparameters.cc. The
+plugin's CFP/FixP block sizes are read from modelparameters.cc into a
+generated header so the kernels can size their register arrays at compile
+time. Libraries land in cudimot_gb300/_lib/ (git-ignored).
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import hashlib
+import os
+import re
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+LIBDIR = os.path.join(HERE, "_lib")
+GENDIR = os.path.join(HERE, "_build")
+MODELS = os.path.join(HERE, "mymodels")
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+
+def nvcc_path():
+    for c in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and os.path.exists(c):
+            return c
+    raise FileNotFoundError("nvcc not found")
+
+
+def shipped_models():
+    return sorted(d for d in os.listdir(MODELS)
+                  if os.path.isfile(os.path.join(MODELS, d, "modelfunctions.h")))
+
+
+def block_sizes(model_dir):
+    """CFP_size / FixP_size initialisers of modelparameters.cc."""
+    txt = open(os.path.join(model_dir, "modelparameters.cc")).read()
+    txt = re.sub(r"//[^\n]*", "", txt)
+    out = {}
+    for name in ("CFP_size", "FixP_size"):
+        m = re.search(name + r"\s*\[\s*\]\s*=\s*\{([^}]*)\}", txt)
+        if not m:
+            raise ValueError(f"{model_dir}: cannot find MODEL::{name}[] in modelparameters.cc")
+        vals = [int(x) for x in m.group(1).replace("\n", " ").split(",") if x.strip()]
+        out[name] = vals
+    return out
+
+
+def sources():
+    files = [os.path.join(CSRC, "cdm_model.cu"), os.path.join(CSRC, "host", "cdm_host.cpp"),
+             os.path.join(CSRC, "host", "cdm_host.h"), os.path.join(CSRC, "host", "cdm_flops.cpp"),
+             os.path.join(ROOT, "include", "cudimot_gb300.h")]
+    for sub in ("prelude", "kernels"):
+        d = os.path.join(CSRC, sub)
+        files += [os.path.join(d, f) for f in sorted(os.listdir(d))]
+    return files
+
+
+def digest(model_dir, flags):
+    h = hashlib.sha256()
+    for f in sources() + sorted(os.path.join(model_dir, x) for x in os.listdir(model_dir)
+                               if x.endswith((".h", ".cc", ".cu", ".hpp"))):
+        h.update(f.encode())
+        h.update(open(f, "rb").read())
+    h.update(" ".join(flags).encode())
+    return h.hexdigest()
+
+
+def lib_path(name):
+    return os.path.join(LIBDIR, f"libcudimot_{name}.so")
+
+
+def build_model(model_dir, name=None, extra_flags=(), verbose=False, force=False):
+    model_dir = os.path.abspath(model_dir)
+    name = name or os.path.basename(model_dir.rstrip("/"))
+    flags = ["-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-shared",
+             "-Xcompiler", "-ffp-contract=off"] + list(extra_flags)
+    out = lib_path(name)
+    stamp = out + ".sha256"
+    dig = digest(model_dir, flags)
+    if not force and os.path.exists(out) and os.path.exists(stamp) and open(stamp).read() == dig:
+        return out, None
+    gen = os.path.join(GENDIR, name)
+    os.makedirs(gen, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    sizes = block_sizes(model_dir)
+    with open(os.path.join(gen, "cdm_model_sizes.h"), "w") as f:
+        f.write("// generated from modelparameters.cc by cudimot_gb300/build.py\n#pragma once\n")
+        f.write(f"#define CDM_CFP_TSIZE {sum(sizes['CFP_size'])}\n")
+        f.write(f"#define CDM_FIXP_TSIZE {sum(sizes['FixP_size'])}\n")
+    # modelparameters.cc defines the MODEL:: size arrays the ABI reports.
+    with open(os.path.join(gen, "cdm_model_params.cpp"), "w") as f:
+        f.write('#include "modelparameters.cc"\n')
+    cmd = [nvcc_path()] + flags + [
+        f'-DCDM_MODEL_NAME="{name}"',
+        "-I", os.path.join(CSRC, "prelude"), "-I", os.path.join(CSRC, "kernels"),
+        "-I", os.path.join(CSRC, "host"), "-I", os.path.join(ROOT, "include"), "-I", gen,
+        "-I", model_dir,
+        os.path.join(CSRC, "cdm_model.cu"), os.path.join(CSRC, "host", "cdm_host.cpp"),
+        os.path.join(gen, "cdm_model_params.cpp"),
+        "-o", out + ".tmp"]
+    if verbose:
+        cmd[1:1] = ["-Xptxas", "-v"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return out, (r.stdout + r.stderr)[-6000:]
+    os.replace(out + ".tmp", out)
+    if verbose:
+        sys.stderr.write(r.stdout + r.stderr)
+    # operation-count build of the same plugin (host, for the roofline)
+    fl = os.path.join(LIBDIR, f"libcdm_flops_{name}.so")
+    cmd = ["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-w",
+           "-I", os.path.join(CSRC, "prelude"), "-I", os.path.join(CSRC, "host"), "-I", gen,
+           "-I", model_dir, os.path.join(CSRC, "host", "cdm_flops.cpp"), "-o", fl + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return fl, (r.stdout + r.stderr)[-6000:]
+    os.replace(fl + ".tmp", fl)
+    with open(stamp, "w") as f:
+        f.write(dig)
+    return out, None
+
+
+def build_peak(force=False):
+    """FP32 FMA probe library (roofline peak)."""
+    src = os.path.join(CSRC, "cdm_peak.cu")
+    out = os.path.join(LIBDIR, "libcdm_peak.so")
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
+        return out, None
+    os.makedirs(LIBDIR, exist_ok=True)
+    cmd = [nvcc_path(), "-O3", ARCH, "-Xcompiler", "-fPIC", "-shared", src, "-o", out + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return out, (r.stdout + r.stderr)[-4000:]
+    os.replace(out + ".tmp", out)
+    return out, None
+
+
+def build_all(models=None, model_dirs=(), jobs=None, verbose=False, force=False):
+    todo = [(os.path.join(MODELS, m), m) for m in (models or shipped_models())]
+    todo += [(d, None) for d in model_dirs]
+    jobs = jobs or max(1, min(len(todo), os.cpu_count() or 1))
+    errors = {}
+    with cf.ThreadPoolExecutor(jobs + 1) as ex:
+        futs = {ex.submit(build_model, d, n, (), verbose, force): (d, n) for d, n in todo}
+        futs[ex.submit(build_peak, force)] = ("peak", None)
+        for f in cf.as_completed(futs):
+            out, err = f.result()
+            if err:
+                errors[out] = err
+    return errors
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--models", nargs="*", default=None)
+    ap.add_argument("--model-dir", action="append", default=[])
+    ap.add_argument("--verbose", action="store_true")
+    ap.add_argument("--force", action="store_true")
+    a = ap.parse_args()
+    errs = build_all(a.models, a.model_dir, verbose=a.verbose, force=a.force)
+    for k, v in errs.items():
+        print(f"FAILED {k}\n{v}", file=sys.stderr)
+    sys.exit(1 if errs else 0)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,725 @@
+// cdm_model.cu - one translation unit per model plugin: the fitting kernels
+// instantiated for the plugin, and the C ABI of include/cudimot_gb300.h.
+//
+// Include order is CUDIMOT's (GridSearch.cu:7-11): math prelude, the
+// plugin's modelparameters.h, macro_numerical.h, the plugin's
+// modelfunctions.h; then this library's plugin tail and kernels.
+#include "functions_gpu.h"
+#include "modelparameters.h"
+#include "macro_numerical.h"
+#include "modelfunctions.h"
+#include "cdm_plugin_tail.h"
+#include "cdm_model_sizes.h"
+
+#include "cdm_common.cuh"
+#include "cdm_gridsearch.cuh"
+#include "cdm_levmar.cuh"
+#include "cdm_mcmc.cuh"
+#include "cdm_postfit.cuh"
+
+#include "cdm_host.h"
+#include "cudimot_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#ifndef CDM_MODEL_NAME
+#define CDM_MODEL_NAME "model"
+#endif
+
+static_assert(NPARAMS <= CDM_MAX_PARAMS, "NPARAMS exceeds CDM_MAX_PARAMS");
+
+namespace {
+
+constexpr float kGsBand = 2e-5f;  // FP32 grid-search near-tie band (relative)
+
+#define CDM_CUDA(call)                                                        \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      cdm_fail(CDM_CUDA_ERROR, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+      return CDM_CUDA_ERROR;                                                  \
+    }                                                                         \
+  } while (0)
+
+#define CDM_TRY(expr)                   \
+  do {                                  \
+    cdm_status s_ = (expr);             \
+    if (s_ != CDM_OK) return s_;        \
+  } while (0)
+
+template <class T>
+cdm_status dev_alloc(T** p, size_t* cap, size_t n) {
+  if (n <= *cap && *p) return CDM_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  if (n == 0) return CDM_OK;
+  CDM_CUDA(cudaMalloc((void**)p, n * sizeof(T)));
+  *cap = n;
+  return CDM_OK;
+}
+
+int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+}  // namespace
+
+struct cdm_ctx {
+  cdm_model_cfg cfg;
+  std::vector<double> grid_host;
+  cdm_limits lim;
+  int gpos[kNP];
+  int device = 0;
+  int num_sms = 0;
+  // scratch (owned)
+  double* grid_dev = nullptr;
+  size_t grid_cap = 0;
+  float* proto32 = nullptr;
+  size_t proto32_cap = 0;
+  double* proto64 = nullptr;
+  size_t proto64_cap = 0;
+  float* sig = nullptr;
+  size_t sig_cap = 0;
+  int* gs_flags = nullptr;
+  size_t gs_flags_cap = 0;
+  int* gs_cand = nullptr;
+  size_t gs_cand_cap = 0;
+  int* gs_best = nullptr;
+  size_t gs_best_cap = 0;
+  int* err = nullptr;
+  unsigned long long* counters = nullptr;  // [0] lm passes [1] lm successes [2] gs rechecks
+  // host-buffer path
+  double* h_meas = nullptr; size_t h_meas_cap = 0;
+  double* h_params = nullptr; size_t h_params_cap = 0;
+  double* h_cfp = nullptr; size_t h_cfp_cap = 0;
+  double* h_fixp = nullptr; size_t h_fixp_cap = 0;
+  double* h_samples = nullptr; size_t h_samples_cap = 0;
+  double* h_tau = nullptr; size_t h_tau_cap = 0;
+  double* h_pred = nullptr; size_t h_pred_cap = 0;
+  double* h_bic = nullptr; size_t h_bic_cap = 0;
+  double* h_aic = nullptr; size_t h_aic_cap = 0;
+  cudaStream_t own_stream = nullptr;
+  // captured fit
+  cudaGraphExec_t graph = nullptr;
+  std::vector<uintptr_t> graph_key;
+  // current protocol / packed signal state
+  int nmeas_pad = 0;
+};
+
+namespace {
+
+cdm_status ensure_base(cdm_ctx* c) {
+  if (!c->err) {
+    CDM_CUDA(cudaMalloc((void**)&c->err, sizeof(int)));
+    CDM_CUDA(cudaMemset(c->err, 0, sizeof(int)));
+    CDM_CUDA(cudaMalloc((void**)&c->counters, 4 * sizeof(unsigned long long)));
+    CDM_CUDA(cudaMemset(c->counters, 0, 4 * sizeof(unsigned long long)));
+  }
+  return CDM_OK;
+}
+
+size_t proto_bytes(int nmeas_pad) { return (size_t)kNCOLS * nmeas_pad * sizeof(float); }
+
+cdm_status check_common(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_size) {
+  if (!c) return cdm_fail(CDM_BAD_ARG, "null context");
+  if (nvox < 0 || nmeas <= 0) return cdm_fail(CDM_BAD_ARG, "nvox must be >= 0 and nmeas > 0");
+  if (CFP_size != CDM_CFP_TSIZE)
+    return cdm_fail(CDM_BAD_ARG, "CFP_size " + std::to_string(CFP_size) + " != model CFP_Tsize " +
+                                     std::to_string(CDM_CFP_TSIZE));
+  if (FixP_size != CDM_FIXP_TSIZE)
+    return cdm_fail(CDM_BAD_ARG, "FixP_size " + std::to_string(FixP_size) +
+                                     " != model FixP_Tsize " + std::to_string(CDM_FIXP_TSIZE));
+  const int pad = round_up(nmeas, 32);
+  if (proto_bytes(pad) > 200 * 1024)
+    return cdm_fail(CDM_BAD_ARG, "protocol too large for shared memory staging");
+  return CDM_OK;
+}
+
+// Protocol tables from CUDIMOT's CFP array (device pointer).
+cdm_status prep_protocol(cdm_ctx* c, int nmeas, const double* CFP, cudaStream_t st) {
+  const int pad = round_up(nmeas, 32);
+  CDM_TRY(dev_alloc(&c->proto32, &c->proto32_cap, (size_t)kNCOLS * pad));
+  CDM_TRY(dev_alloc(&c->proto64, &c->proto64_cap, (size_t)kNCOLS * nmeas));
+  c->nmeas_pad = pad;
+  cdm_prep_protocol_kernel<<<(pad + 127) / 128, 128, 0, st>>>(CFP, nmeas, pad, c->proto32, c->proto64);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+template <int G>
+cdm_status pack_signals_g(cdm_ctx* c, int nvox, int nmeas, const double* meas, cudaStream_t st) {
+  const int nchunk = (nmeas + G - 1) / G;
+  CDM_TRY(dev_alloc(&c->sig, &c->sig_cap, (size_t)nchunk * std::max(nvox, 1) * G));
+  if (nvox == 0) return CDM_OK;
+  const size_t total = (size_t)nchunk * nvox * G;
+  const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)c->num_sms * 32);
+  cdm_pack_signals_kernel<G><<<blocks, 256, 0, st>>>(meas, nvox, nmeas, nchunk, c->sig);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+cdm_status pack_signals(cdm_ctx* c, int G, int nvox, int nmeas, const double* meas, cudaStream_t st) {
+  switch (G) {
+    case 4: return pack_signals_g<4>(c, nvox, nmeas, meas, st);
+    case 8: return pack_signals_g<8>(c, nvox, nmeas, meas, st);
+    case 16: return pack_signals_g<16>(c, nvox, nmeas, meas, st);
+    case 32: return pack_signals_g<32>(c, nvox, nmeas, meas, st);
+  }
+  return cdm_fail(CDM_BAD_ARG, "lanes per voxel must be 4, 8, 16 or 32");
+}
+
+template <class K>
+cdm_status set_smem(K kernel, size_t bytes) {
+  if (bytes > 48 * 1024) CDM_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return CDM_OK;
+}
+
+// Lanes per voxel: explicit choice, else a shape-based default. Every lane
+// of a group redoes the parameter-only work, so fewer lanes are better while
+// there are enough voxels to fill the GPU (>= ~8 resident groups per SM
+// slot); with few voxels, more lanes share each voxel.
+int pick_lanes(const cdm_ctx* c, int requested, int nvox, int nmeas) {
+  if (requested == 4 || requested == 8 || requested == 16 || requested == 32) return requested;
+  const long slots = (long)std::max(c->num_sms, 1) * 1024;  // resident threads of interest
+  int g = 8;
+  while (g < 32 && (long)nvox * g < 2 * slots) g *= 2;
+  if (nmeas < 2 * g && g > 4) g = std::max(4, g / 2);
+  return g;
+}
+
+template <class Args>
+void fill_common(cdm_ctx* c, Args& a, int nvox, int nmeas, int G) {
+  a.nvox = nvox;
+  a.nmeas = nmeas;
+  a.nmeas_pad = c->nmeas_pad;
+  a.nchunk = (nmeas + G - 1) / G;
+  a.fixp_tsize = CDM_FIXP_TSIZE;
+  a.proto_bytes = (uint32_t)proto_bytes(c->nmeas_pad);
+  a.proto = c->proto32;
+  a.sig = c->sig;
+  a.err = c->err;
+  a.lim = c->lim;
+}
+
+int blocks_for(int nvox, int G) { return (nvox + (CDM_NT / G) - 1) / (CDM_NT / G); }
+
+// ------------------------------------------------------------------ stages
+template <int G>
+cdm_status launch_gs(cdm_ctx* c, int nvox, int nmeas, double* params, const double* FixP,
+                     cudaStream_t st) {
+  cdm_gs_args a;
+  fill_common(c, a, nvox, nmeas, G);
+  a.params = params;
+  a.fixp = FixP;
+  a.grid = c->grid_dev;
+  a.ngp = c->cfg.n_grid_params;
+  a.combs = c->cfg.grid_combs;
+  for (int p = 0; p < kNP; p++) a.gpos[p] = c->gpos[p];
+  a.band = kGsBand;
+  a.flags = c->gs_flags;
+  a.cand = c->gs_cand;
+  a.best = c->gs_best;
+  const size_t sm = proto_bytes(c->nmeas_pad);
+  CDM_TRY(set_smem(cdm_gridsearch_kernel<G>, sm));
+  cdm_gridsearch_kernel<G><<<blocks_for(nvox, G), CDM_NT, sm, st>>>(a);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+cdm_status run_gridsearch(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
+                          const double* CFP, const double* FixP, cudaStream_t st) {
+  if (c->cfg.grid_combs <= 0 || c->cfg.n_grid_params <= 0) return CDM_OK;
+  CDM_TRY(prep_protocol(c, nmeas, CFP, st));
+  const int G = pick_lanes(c, c->cfg.lanes_gridsearch, nvox, nmeas);
+  CDM_TRY(pack_signals(c, G, nvox, nmeas, meas, st));
+  const size_t n = (size_t)std::max(nvox, 1);
+  CDM_TRY(dev_alloc(&c->gs_flags, &c->gs_flags_cap, n));
+  CDM_TRY(dev_alloc(&c->gs_cand, &c->gs_cand_cap, n * kGsTop));
+  CDM_TRY(dev_alloc(&c->gs_best, &c->gs_best_cap, n));
+  if (nvox == 0) return CDM_OK;
+  switch (G) {
+    case 4: CDM_TRY(launch_gs<4>(c, nvox, nmeas, params, FixP, st)); break;
+    case 8: CDM_TRY(launch_gs<8>(c, nvox, nmeas, params, FixP, st)); break;
+    case 16: CDM_TRY(launch_gs<16>(c, nvox, nmeas, params, FixP, st)); break;
+    default: CDM_TRY(launch_gs<32>(c, nvox, nmeas, params, FixP, st)); break;
+  }
+  cdm_gs_recheck_args r;
+  r.nvox = nvox;
+  r.nmeas = nmeas;
+  r.fixp_tsize = CDM_FIXP_TSIZE;
+  r.proto64 = c->proto64;
+  r.meas = meas;
+  r.params = params;
+  r.fixp = FixP;
+  r.grid = c->grid_dev;
+  r.ngp = c->cfg.n_grid_params;
+  r.combs = c->cfg.grid_combs;
+  for (int p = 0; p < kNP; p++) r.gpos[p] = c->gpos[p];
+  r.flags = c->gs_flags;
+  r.cand = c->gs_cand;
+  r.best = c->gs_best;
+  r.rechecked = c->counters + 2;
+  r.lim = c->lim;
+  cdm_gs_recheck_kernel<<<blocks_for(nvox, 32), CDM_NT, 0, st>>>(r);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+template <int G>
+cdm_status launch_lm(cdm_ctx* c, int nvox, int nmeas, double* params, const double* FixP,
+                     cudaStream_t st) {
+  cdm_lm_args a;
+  fill_common(c, a, nvox, nmeas, G);
+  a.params = params;
+  a.fixp = FixP;
+  a.max_iters = c->cfg.iter_levmar;
+  a.marquardt = c->cfg.marquardt;
+  a.iter_count = c->counters + 0;
+  a.succ_count = c->counters + 1;
+  const size_t sm = proto_bytes(c->nmeas_pad);
+  CDM_TRY(set_smem(cdm_levmar_kernel<G>, sm));
+  cdm_levmar_kernel<G><<<blocks_for(nvox, G), CDM_NT, sm, st>>>(a);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+cdm_status run_levmar(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
+                      const double* CFP, const double* FixP, cudaStream_t st) {
+  CDM_TRY(prep_protocol(c, nmeas, CFP, st));
+  const int G = pick_lanes(c, c->cfg.lanes_levmar, nvox, nmeas);
+  CDM_TRY(pack_signals(c, G, nvox, nmeas, meas, st));
+  if (nvox == 0) return CDM_OK;
+  switch (G) {
+    case 4: return launch_lm<4>(c, nvox, nmeas, params, FixP, st);
+    case 8: return launch_lm<8>(c, nvox, nmeas, params, FixP, st);
+    case 16: return launch_lm<16>(c, nvox, nmeas, params, FixP, st);
+    default: return launch_lm<32>(c, nvox, nmeas, params, FixP, st);
+  }
+}
+
+template <int G, bool RICIAN>
+cdm_status launch_mcmc(cdm_ctx* c, int nvox, int nmeas, double* params, const double* FixP,
+                       double* samples, double* tau, uint32_t voxel_offset, cudaStream_t st) {
+  cdm_mcmc_args a;
+  fill_common(c, a, nvox, nmeas, G);
+  a.params = params;
+  a.fixp = FixP;
+  a.samples = samples;
+  a.tau_samples = tau;
+  a.nburn = c->cfg.nburn;
+  a.njumps = c->cfg.njumps;
+  a.sampleevery = c->cfg.sampleevery;
+  a.nsamples = c->cfg.njumps / c->cfg.sampleevery;
+  a.update_proposal = c->cfg.update_proposal;
+  a.seed = c->cfg.seed;
+  a.stream = (uint32_t)c->cfg.id_part;
+  a.voxel_offset = voxel_offset;
+  const size_t sm = proto_bytes(c->nmeas_pad);
+  CDM_TRY(set_smem(cdm_mcmc_kernel<G, RICIAN>, sm));
+  cdm_mcmc_kernel<G, RICIAN><<<blocks_for(nvox, G), CDM_NT, sm, st>>>(a);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+cdm_status run_mcmc(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
+                    const double* CFP, const double* FixP, double* samples, double* tau,
+                    uint32_t voxel_offset, cudaStream_t st) {
+  if (c->cfg.sampleevery <= 0 || c->cfg.njumps < c->cfg.sampleevery)
+    return cdm_fail(CDM_BAD_ARG,
+                    "MCMC must record at least one sample: --nj must be >= --se (MCMC.cu:707-710)");
+  if (!samples) return cdm_fail(CDM_BAD_ARG, "samples is null");
+  if (c->cfg.rician && !tau) return cdm_fail(CDM_BAD_ARG, "rician MCMC needs tau_samples");
+  CDM_TRY(prep_protocol(c, nmeas, CFP, st));
+  const int G = pick_lanes(c, c->cfg.lanes_mcmc, nvox, nmeas);
+  CDM_TRY(pack_signals(c, G, nvox, nmeas, meas, st));
+  if (nvox == 0) return CDM_OK;
+  const bool ric = c->cfg.rician != 0;
+#define CDM_MCMC_CASE(GG)                                                                     \
+  case GG:                                                                                    \
+    return ric ? launch_mcmc<GG, true>(c, nvox, nmeas, params, FixP, samples, tau, voxel_offset, st) \
+               : launch_mcmc<GG, false>(c, nvox, nmeas, params, FixP, samples, tau, voxel_offset, st);
+  switch (G) {
+    CDM_MCMC_CASE(4)
+    CDM_MCMC_CASE(8)
+    CDM_MCMC_CASE(16)
+    CDM_MCMC_CASE(32)
+  }
+#undef CDM_MCMC_CASE
+  return cdm_fail(CDM_BAD_ARG, "bad lane count");
+}
+
+cdm_status run_post(cdm_ctx* c, bool bic, int nvox, int nmeas, int nsamples, const double* meas,
+                    const double* samples, const double* CFP, const double* FixP, double* pred,
+                    double* BIC, double* AIC, const double* tau, bool rician, cudaStream_t st) {
+  if (nsamples <= 0) return cdm_fail(CDM_BAD_ARG, "nsamples must be > 0");
+  CDM_TRY(prep_protocol(c, nmeas, CFP, st));
+  if (nvox == 0) return CDM_OK;
+  cdm_post_args a;
+  a.nvox = nvox;
+  a.nmeas = nmeas;
+  a.nmeas_pad = c->nmeas_pad;
+  a.nsamples = nsamples;
+  a.fixp_tsize = CDM_FIXP_TSIZE;
+  a.proto_bytes = (uint32_t)proto_bytes(c->nmeas_pad);
+  a.proto = c->proto32;
+  a.meas = meas;
+  a.samples = samples;
+  a.tau = tau;
+  a.fixp = FixP;
+  a.pred = pred;
+  a.bic = BIC;
+  a.aic = AIC;
+  a.rician = rician ? 1 : 0;
+  a.err = c->err;
+  const size_t sm = proto_bytes(c->nmeas_pad);
+  if (bic) {
+    CDM_TRY(set_smem(cdm_bic_aic_kernel, sm));
+    cdm_bic_aic_kernel<<<blocks_for(nvox, 32), CDM_NT, sm, st>>>(a);
+  } else {
+    CDM_TRY(set_smem(cdm_predicted_kernel, sm));
+    cdm_predicted_kernel<<<blocks_for(nvox, 32), CDM_NT, sm, st>>>(a);
+  }
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+cdm_status fit_sequence(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
+                        const double* CFP, const double* FixP, double* samples, double* tau,
+                        double* pred, double* BIC, double* AIC, uint32_t voxel_offset,
+                        cudaStream_t st) {
+  const cdm_model_cfg& o = c->cfg;
+  if (o.run_gridsearch) CDM_TRY(run_gridsearch(c, nvox, nmeas, meas, params, CFP, FixP, st));
+  if (o.run_levmar) CDM_TRY(run_levmar(c, nvox, nmeas, meas, params, CFP, FixP, st));
+  int nsamples = 1;
+  if (o.run_mcmc) {
+    CDM_TRY(run_mcmc(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau, voxel_offset, st));
+    nsamples = o.njumps / o.sampleevery;
+  } else if (nvox > 0) {
+    cdm_params_to_samples_kernel<<<std::max(1, std::min(c->num_sms * 4, (nvox * kNP + 255) / 256)), 256, 0,
+                                   st>>>(params, nvox, samples);
+    CDM_CUDA(cudaGetLastError());
+  }
+  const bool rician = o.rician && o.run_mcmc;
+  if (o.get_predicted && pred)
+    CDM_TRY(run_post(c, false, nvox, nmeas, nsamples, meas, samples, CFP, FixP, pred, nullptr,
+                     nullptr, tau, rician, st));
+  if (o.bic_aic && BIC && AIC)
+    CDM_TRY(run_post(c, true, nvox, nmeas, nsamples, meas, samples, CFP, FixP, nullptr, BIC, AIC,
+                     tau, rician, st));
+  return CDM_OK;
+}
+
+// Allocate every scratch buffer a fit of this shape needs, so that the
+// captured graph contains no allocation.
+cdm_status reserve_fit(cdm_ctx* c, int nvox, int nmeas) {
+  const int pad = round_up(nmeas, 32);
+  CDM_TRY(dev_alloc(&c->proto32, &c->proto32_cap, (size_t)kNCOLS * pad));
+  CDM_TRY(dev_alloc(&c->proto64, &c->proto64_cap, (size_t)kNCOLS * nmeas));
+  size_t sig = 0;
+  for (int G : {4, 8, 16, 32}) sig = std::max(sig, (size_t)((nmeas + G - 1) / G) * std::max(nvox, 1) * G);
+  CDM_TRY(dev_alloc(&c->sig, &c->sig_cap, sig));
+  const size_t n = (size_t)std::max(nvox, 1);
+  CDM_TRY(dev_alloc(&c->gs_flags, &c->gs_flags_cap, n));
+  CDM_TRY(dev_alloc(&c->gs_cand, &c->gs_cand_cap, n * kGsTop));
+  CDM_TRY(dev_alloc(&c->gs_best, &c->gs_best_cap, n));
+  // kernel attributes are set outside capture too
+  const size_t sm = proto_bytes(pad);
+  CDM_TRY(set_smem(cdm_gridsearch_kernel<4>, sm)); CDM_TRY(set_smem(cdm_gridsearch_kernel<8>, sm));
+  CDM_TRY(set_smem(cdm_gridsearch_kernel<16>, sm)); CDM_TRY(set_smem(cdm_gridsearch_kernel<32>, sm));
+  return CDM_OK;
+}
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+cdm_status cdm_get_model_info(cdm_model_info* info) {
+  if (!info) return cdm_fail(CDM_BAD_ARG, "null info");
+  std::memset(info, 0, sizeof(*info));
+  std::snprintf(info->name, sizeof(info->name), "%s", CDM_MODEL_NAME);
+  info->nparams = NPARAMS;
+  info->ncfp = NCFP;
+  info->nfixp = NFIXP;
+  for (int i = 0; i < NCFP && i < CDM_MAX_BLOCKS; i++) info->cfp_size[i] = MODEL::CFP_size[i];
+  for (int i = 0; i < NFIXP && i < CDM_MAX_BLOCKS; i++) info->fixp_size[i] = MODEL::FixP_size[i];
+  info->cfp_tsize = CDM_CFP_TSIZE;
+  info->fixp_tsize = CDM_FIXP_TSIZE;
+  info->derived_cfp = CDM_NDCFP;
+  info->derived_p = CDM_NDP;
+  return CDM_OK;
+}
+
+cdm_status cdm_default_cfg(cdm_model_cfg* cfg) {
+  if (!cfg) return cdm_fail(CDM_BAD_ARG, "null cfg");
+  cdm_fill_default_cfg(cfg, NPARAMS);
+  return CDM_OK;
+}
+
+cdm_status cdm_parse_priors(const char* path, cdm_model_cfg* cfg, double* p_init, int* p_init_given) {
+  return cdm_parse_priors_impl(path, NPARAMS, cfg, p_init, p_init_given);
+}
+
+cdm_status cdm_parse_grid(const char* path, int* n_grid_params, int* grid_params, int* grid_combs,
+                          double* grid, int64_t grid_capacity) {
+  return cdm_parse_grid_impl(path, NPARAMS, n_grid_params, grid_params, grid_combs, grid,
+                             grid_capacity);
+}
+
+cdm_status cdm_parse_fixed(const char* list, int* fixed) {
+  return cdm_parse_fixed_impl(list, NPARAMS, fixed);
+}
+
+cdm_status cdm_read_cfp_list(const char* path, int nmeas, double* cfp) {
+  std::vector<int> sizes(MODEL::CFP_size, MODEL::CFP_size + NCFP);
+  return cdm_read_cfp_list_impl(path, nmeas, sizes, cfp);
+}
+
+cdm_status cdm_create(const cdm_model_cfg* cfg, cdm_ctx** out) {
+  if (!cfg || !out) return cdm_fail(CDM_BAD_ARG, "null argument");
+  *out = nullptr;
+  if (cfg->nparams != NPARAMS)
+    return cdm_fail(CDM_BAD_ARG, "cfg.nparams " + std::to_string(cfg->nparams) +
+                                     " != model NPARAMS " + std::to_string(NPARAMS));
+  CDM_TRY(cdm_validate_cfg(cfg, NPARAMS));
+  cdm_ctx* c = new cdm_ctx();
+  c->cfg = *cfg;
+  c->cfg.grid = nullptr;
+  for (int p = 0; p < kNP; p++) {
+    c->lim.btype[p] = cfg->bound_types[p];
+    c->lim.bmin[p] = (float)cfg->bounds_min[p];
+    c->lim.bmax[p] = (float)cfg->bounds_max[p];
+    c->lim.ptype[p] = cfg->prior_types[p];
+    c->lim.pa[p] = (float)cfg->priors_a[p];
+    c->lim.pb[p] = (float)cfg->priors_b[p];
+    c->lim.fixed[p] = cfg->fixed[p];
+    c->gpos[p] = -1;
+  }
+  if (cfg->run_gridsearch && cfg->grid_combs > 0 && cfg->n_grid_params > 0) {
+    const size_t n = (size_t)cfg->grid_combs * cfg->n_grid_params;
+    c->grid_host.assign(cfg->grid, cfg->grid + n);
+    for (int i = 0; i < cfg->n_grid_params; i++) c->gpos[cfg->grid_params[i]] = i;
+  } else {
+    c->cfg.run_gridsearch = 0;
+  }
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  if (e != cudaSuccess) {
+    delete c;
+    return cdm_fail(CDM_CUDA_ERROR, std::string("no usable CUDA device: ") + cudaGetErrorString(e));
+  }
+  cdm_status s = ensure_base(c);
+  if (s == CDM_OK && !c->grid_host.empty()) {
+    s = dev_alloc(&c->grid_dev, &c->grid_cap, c->grid_host.size());
+    if (s == CDM_OK) {
+      e = cudaMemcpy(c->grid_dev, c->grid_host.data(), c->grid_host.size() * sizeof(double),
+                     cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) s = cdm_fail(CDM_CUDA_ERROR, cudaGetErrorString(e));
+    }
+  }
+  if (s != CDM_OK) {
+    cdm_destroy(c);
+    return s;
+  }
+  *out = c;
+  return CDM_OK;
+}
+
+cdm_status cdm_destroy(cdm_ctx* c) {
+  if (!c) return CDM_OK;
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  void* bufs[] = {c->grid_dev, c->proto32, c->proto64, c->sig, c->gs_flags, c->gs_cand,
+                  c->gs_best, c->err, c->counters, c->h_meas, c->h_params, c->h_cfp, c->h_fixp,
+                  c->h_samples, c->h_tau, c->h_pred, c->h_bic, c->h_aic};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return CDM_OK;
+}
+
+cdm_status cdm_gridsearch(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_size,
+                          const double* meas, double* params, const double* CFP, const double* FixP,
+                          void* stream) {
+  CDM_TRY(check_common(c, nvox, nmeas, CFP_size, FixP_size));
+  if (!c->cfg.run_gridsearch) return cdm_fail(CDM_BAD_ARG, "context has no grid");
+  return run_gridsearch(c, nvox, nmeas, meas, params, CFP, FixP, (cudaStream_t)stream);
+}
+
+cdm_status cdm_levmar(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_size,
+                      const double* meas, double* params, const double* CFP, const double* FixP,
+                      void* stream) {
+  CDM_TRY(check_common(c, nvox, nmeas, CFP_size, FixP_size));
+  return run_levmar(c, nvox, nmeas, meas, params, CFP, FixP, (cudaStream_t)stream);
+}
+
+cdm_status cdm_mcmc(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_size,
+                    const double* meas, double* params, const double* CFP, const double* FixP,
+                    double* samples, double* tau_samples, void* stream) {
+  CDM_TRY(check_common(c, nvox, nmeas, CFP_size, FixP_size));
+  return run_mcmc(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau_samples, 0,
+                  (cudaStream_t)stream);
+}
+
+cdm_status cdm_bic_aic(cdm_ctx* c, int nvox, int nmeas, int nsamples, int CFP_size, int FixP_size,
+                       const double* meas, const double* samples, const double* CFP,
+                       const double* FixP, double* BIC, double* AIC, const double* tau_samples,
+                       void* stream) {
+  CDM_TRY(check_common(c, nvox, nmeas, CFP_size, FixP_size));
+  // Rician BIC only after a Rician MCMC (BIC_AIC.cu:208).
+  const bool rician = c->cfg.rician && c->cfg.run_mcmc && tau_samples;
+  return run_post(c, true, nvox, nmeas, nsamples, meas, samples, CFP, FixP, nullptr, BIC, AIC,
+                  tau_samples, rician, (cudaStream_t)stream);
+}
+
+cdm_status cdm_predicted_signal(cdm_ctx* c, int nvox, int nmeas, int nsamples, int CFP_size,
+                                int FixP_size, const double* samples, const double* CFP,
+                                const double* FixP, double* pred, void* stream) {
+  CDM_TRY(check_common(c, nvox, nmeas, CFP_size, FixP_size));
+  return run_post(c, false, nvox, nmeas, nsamples, nullptr, samples, CFP, FixP, pred, nullptr,
+                  nullptr, nullptr, false, (cudaStream_t)stream);
+}
+
+cdm_status cdm_fit(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
+                   const double* CFP, const double* FixP, double* samples, double* tau,
+                   double* pred, double* BIC, double* AIC, void* stream) {
+  CDM_TRY(check_common(c, nvox, nmeas, CDM_CFP_TSIZE, CDM_FIXP_TSIZE));
+  if (!samples) return cdm_fail(CDM_BAD_ARG, "samples is null");
+  if (c->cfg.run_mcmc && (c->cfg.sampleevery <= 0 || c->cfg.njumps < c->cfg.sampleevery))
+    return cdm_fail(CDM_BAD_ARG, "MCMC must record at least one sample: --nj must be >= --se");
+  if (c->cfg.run_mcmc && c->cfg.rician && !tau) return cdm_fail(CDM_BAD_ARG, "rician needs tau");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (nvox == 0) return CDM_OK;
+  CDM_TRY(reserve_fit(c, nvox, nmeas));
+  const std::vector<uintptr_t> key = {(uintptr_t)nvox, (uintptr_t)nmeas, (uintptr_t)meas,
+                                      (uintptr_t)params, (uintptr_t)CFP, (uintptr_t)FixP,
+                                      (uintptr_t)samples, (uintptr_t)tau, (uintptr_t)pred,
+                                      (uintptr_t)BIC, (uintptr_t)AIC, (uintptr_t)st};
+  if (!c->graph || key != c->graph_key) {
+    if (c->graph) {
+      cudaGraphExecDestroy(c->graph);
+      c->graph = nullptr;
+    }
+    // The legacy default stream cannot be captured; record on a private one.
+    cudaStream_t cap = st;
+    if (cap == nullptr || cap == cudaStreamLegacy || cap == cudaStreamPerThread) {
+      if (!c->own_stream) CDM_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+      cap = c->own_stream;
+    }
+    CDM_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    cdm_status s = fit_sequence(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau, pred, BIC,
+                                AIC, 0, cap);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(cap, &g);
+    if (s != CDM_OK) {
+      if (g) cudaGraphDestroy(g);
+      return s;
+    }
+    if (e != cudaSuccess) return cdm_fail(CDM_CUDA_ERROR, std::string("capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      c->graph = nullptr;
+      return cdm_fail(CDM_CUDA_ERROR, std::string("instantiate: ") + cudaGetErrorString(e));
+    }
+    c->graph_key = key;
+  }
+  CDM_CUDA(cudaMemsetAsync(c->counters, 0, 4 * sizeof(unsigned long long), st));
+  CDM_CUDA(cudaGraphLaunch(c->graph, st));
+  return CDM_OK;
+}
+
+cdm_status cdm_synchronize(cdm_ctx* c, void* stream, int64_t timeout_ms) {
+  if (!c) return cdm_fail(CDM_BAD_ARG, "null context");
+  cudaStream_t st = (cudaStream_t)stream;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t e = cudaStreamQuery(st);
+    if (e == cudaSuccess) break;
+    if (e != cudaErrorNotReady) return cdm_fail(CDM_CUDA_ERROR, cudaGetErrorString(e));
+    if (timeout_ms >= 0 &&
+        std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0)
+                .count() > timeout_ms)
+      return cdm_fail(CDM_TIMEOUT, "stream did not finish within the time limit");
+    std::this_thread::sleep_for(std::chrono::microseconds(200));
+  }
+  int err = 0;
+  CDM_CUDA(cudaMemcpy(&err, c->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) {
+    cudaMemset(c->err, 0, sizeof(int));
+    return cdm_fail(CDM_TIMEOUT, "a bounded device wait ran out (code " + std::to_string(err) + ")");
+  }
+  return CDM_OK;
+}
+
+cdm_status cdm_get_stats(cdm_ctx* c, cdm_stats* s) {
+  if (!c || !s) return cdm_fail(CDM_BAD_ARG, "null argument");
+  unsigned long long h[4] = {0, 0, 0, 0};
+  CDM_CUDA(cudaMemcpy(h, c->counters, sizeof(h), cudaMemcpyDeviceToHost));
+  s->lm_iterations = (int64_t)h[0];
+  s->lm_successes = (int64_t)h[1];
+  s->gs_recheck_voxels = (int64_t)h[2];
+  int err = 0;
+  CDM_CUDA(cudaMemcpy(&err, c->err, sizeof(int), cudaMemcpyDeviceToHost));
+  s->device_errors = err;
+  return CDM_OK;
+}
+
+cdm_status cdm_fit_host(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
+                        const double* CFP, const double* FixP, double* samples, double* tau,
+                        double* pred, double* BIC, double* AIC, int part_size, int64_t timeout_ms) {
+  CDM_TRY(check_common(c, nvox, nmeas, CDM_CFP_TSIZE, CDM_FIXP_TSIZE));
+  if (!meas || !params || !CFP || !samples || (CDM_FIXP_TSIZE > 0 && !FixP))
+    return cdm_fail(CDM_BAD_ARG, "null array");
+  (void)part_size;
+  const cdm_model_cfg& o = c->cfg;
+  const int ns = o.run_mcmc ? o.njumps / std::max(o.sampleevery, 1) : 1;
+  const size_t V = (size_t)nvox;
+  CDM_TRY(dev_alloc(&c->h_meas, &c->h_meas_cap, V * nmeas));
+  CDM_TRY(dev_alloc(&c->h_params, &c->h_params_cap, V * kNP));
+  CDM_TRY(dev_alloc(&c->h_cfp, &c->h_cfp_cap, (size_t)nmeas * CDM_CFP_TSIZE));
+  CDM_TRY(dev_alloc(&c->h_fixp, &c->h_fixp_cap, std::max<size_t>(1, V * CDM_FIXP_TSIZE)));
+  CDM_TRY(dev_alloc(&c->h_samples, &c->h_samples_cap, V * kNP * ns));
+  const bool want_tau = o.run_mcmc && o.rician && tau;
+  const bool want_pred = o.get_predicted && pred;
+  const bool want_bic = o.bic_aic && BIC && AIC;
+  if (want_tau) CDM_TRY(dev_alloc(&c->h_tau, &c->h_tau_cap, V * ns));
+  if (want_pred) CDM_TRY(dev_alloc(&c->h_pred, &c->h_pred_cap, V * nmeas));
+  if (want_bic) {
+    CDM_TRY(dev_alloc(&c->h_bic, &c->h_bic_cap, V));
+    CDM_TRY(dev_alloc(&c->h_aic, &c->h_aic_cap, V));
+  }
+  if (!c->own_stream) CDM_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+  cudaStream_t st = c->own_stream;
+  CDM_CUDA(cudaMemcpyAsync(c->h_meas, meas, V * nmeas * sizeof(double), cudaMemcpyHostToDevice, st));
+  CDM_CUDA(cudaMemcpyAsync(c->h_params, params, V * kNP * sizeof(double), cudaMemcpyHostToDevice, st));
+  CDM_CUDA(cudaMemcpyAsync(c->h_cfp, CFP, (size_t)nmeas * CDM_CFP_TSIZE * sizeof(double),
+                           cudaMemcpyHostToDevice, st));
+  if (CDM_FIXP_TSIZE > 0)
+    CDM_CUDA(cudaMemcpyAsync(c->h_fixp, FixP, V * CDM_FIXP_TSIZE * sizeof(double),
+                             cudaMemcpyHostToDevice, st));
+  CDM_TRY(cdm_fit(c, nvox, nmeas, c->h_meas, c->h_params, c->h_cfp, c->h_fixp, c->h_samples,
+                  want_tau ? c->h_tau : nullptr, want_pred ? c->h_pred : nullptr,
+                  want_bic ? c->h_bic : nullptr, want_bic ? c->h_aic : nullptr, st));
+  CDM_CUDA(cudaMemcpyAsync(params, c->h_params, V * kNP * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CDM_CUDA(cudaMemcpyAsync(samples, c->h_samples, V * kNP * ns * sizeof(double),
+                           cudaMemcpyDeviceToHost, st));
+  if (want_tau)
+    CDM_CUDA(cudaMemcpyAsync(tau, c->h_tau, V * ns * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (want_pred)
+    CDM_CUDA(cudaMemcpyAsync(pred, c->h_pred, V * nmeas * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (want_bic) {
+    CDM_CUDA(cudaMemcpyAsync(BIC, c->h_bic, V * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CDM_CUDA(cudaMemcpyAsync(AIC, c->h_aic, V * sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
+  return cdm_synchronize(c, st, timeout_ms);
+}
+
+}  // extern "C"

@@ -1,0 +1,115 @@
+// cdm_flops.cpp - operation counts of a model plugin, for the roofline.
+//
+// The plugin is compiled for the host with a counting number type: every
+// +, -, *, / on it adds one to `flops`, every *_gpu math call adds one to
+// `mufu` (transcendental or square root). Counting Derived_P separately from
+// Predicted_Signal gives the work done once per parameter change and the
+// work done per measurement. Built per model by cudimot_gb300/build.py.
+#define __device__
+#define __host__
+#define __global__
+#define __forceinline__ inline
+#include <cmath>
+#include <cstdint>
+#include <algorithm>
+using std::max;
+using std::min;
+#include "functions_gpu.h"
+
+namespace {
+thread_local int64_t g_flops = 0, g_mufu = 0;
+}
+
+struct cnt {
+  double v;
+  cnt() = default;
+  template <class U, class = typename std::enable_if<std::is_arithmetic<U>::value>::type>
+  cnt(U x) : v((double)x) {}
+  cnt(fp32 x) : v((double)x.v) {}
+  operator double() const { return v; }
+  cnt& operator+=(cnt o) { g_flops++; v += o.v; return *this; }
+  cnt& operator-=(cnt o) { g_flops++; v -= o.v; return *this; }
+  cnt& operator*=(cnt o) { g_flops++; v *= o.v; return *this; }
+  cnt& operator/=(cnt o) { g_flops++; v /= o.v; return *this; }
+};
+inline cnt operator-(cnt a) { return cnt(-a.v); }
+#define CNT_BIN(OP)                                                                      \
+  inline cnt operator OP(cnt a, cnt b) { g_flops++; return cnt(a.v OP b.v); }            \
+  template <class U, class = typename std::enable_if<std::is_arithmetic<U>::value>::type> \
+  inline cnt operator OP(cnt a, U b) { g_flops++; return cnt(a.v OP (double)b); }        \
+  template <class U, class = typename std::enable_if<std::is_arithmetic<U>::value>::type> \
+  inline cnt operator OP(U a, cnt b) { g_flops++; return cnt((double)a OP b.v); }
+CNT_BIN(+) CNT_BIN(-) CNT_BIN(*) CNT_BIN(/)
+#define CNT_CMP(OP)                                                                      \
+  inline bool operator OP(cnt a, cnt b) { return a.v OP b.v; }                           \
+  template <class U, class = typename std::enable_if<std::is_arithmetic<U>::value>::type> \
+  inline bool operator OP(cnt a, U b) { return a.v OP (double)b; }                       \
+  template <class U, class = typename std::enable_if<std::is_arithmetic<U>::value>::type> \
+  inline bool operator OP(U a, cnt b) { return (double)a OP b.v; }
+CNT_CMP(<) CNT_CMP(>) CNT_CMP(<=) CNT_CMP(>=) CNT_CMP(==) CNT_CMP(!=)
+#define CNT_MUFU(NAME, F) \
+  inline cnt NAME(cnt x) { g_mufu++; return cnt(F(x.v)); }
+CNT_MUFU(log_gpu, std::log) CNT_MUFU(exp_gpu, std::exp) CNT_MUFU(sin_gpu, std::sin)
+CNT_MUFU(cos_gpu, std::cos) CNT_MUFU(atan_gpu, std::atan) CNT_MUFU(tan_gpu, std::tan)
+CNT_MUFU(sqrt_gpu, std::sqrt) CNT_MUFU(acos_gpu, std::acos)
+inline cnt fabs_gpu(cnt x) { return cnt(std::fabs(x.v)); }
+template <> struct cdm_bin<cnt> {
+  static cnt mn(cnt a, cnt b) { return cnt(std::fmin(a.v, b.v)); }
+  static cnt mx(cnt a, cnt b) { return cnt(std::fmax(a.v, b.v)); }
+  static cnt at2(cnt a, cnt b) { g_mufu++; return cnt(std::atan2(a.v, b.v)); }
+  static cnt pw(cnt a, cnt b) { g_mufu++; return cnt(std::pow(a.v, b.v)); }
+};
+template <class B> struct cdm_math_result<cnt, B> { typedef cnt type; };
+template <class A> struct cdm_math_result<A, cnt> { typedef cnt type; };
+template <> struct cdm_math_result<cnt, cnt> { typedef cnt type; };
+
+#include "modelparameters.h"
+#include "macro_numerical.h"
+#include "modelfunctions.h"
+#include "cdm_plugin_tail.h"
+#include "cdm_model_sizes.h"
+
+constexpr int kNCOLS = CDM_CFP_TSIZE + CDM_NDCFP;
+
+// out[0] = FLOPs of Derived_P per call, out[1] = FLOPs of Predicted_Signal
+// per measurement, out[2] = FLOPs of Partial_Derivatives per measurement;
+// out[3..5] the same for transcendental/sqrt calls. Averaged over the nvox
+// parameter vectors and nmeas measurements given.
+extern "C" int cdm_count_ops(int nvox, const double* params, int nmeas, const double* cfp,
+                             const double* fixp, double* out) {
+  int64_t fd = 0, fs = 0, fj = 0, md = 0, ms = 0, mj = 0;
+  for (int v = 0; v < nvox; v++) {
+    cnt P[CDM_PSTORE], F[CDM_FIXP_TSIZE + 1], d[NPARAMS];
+    for (int i = 0; i < CDM_PSTORE; i++) P[i] = i < NPARAMS ? params[(size_t)v * NPARAMS + i] : 0.0;
+    for (int k = 0; k < CDM_FIXP_TSIZE; k++) F[k] = fixp[(size_t)v * CDM_FIXP_TSIZE + k];
+    g_flops = g_mufu = 0;
+    cdm_update_derived(P, F);
+    fd += g_flops;
+    md += g_mufu;
+    for (int m = 0; m < nmeas; m++) {
+      double raw[kNCOLS];
+      for (int k = 0; k < CDM_CFP_TSIZE; k++) raw[k] = cfp[(size_t)m * CDM_CFP_TSIZE + k];
+#ifdef CDM_DERIVED_CFP
+      Derived_CFP<double>(raw, raw + CDM_CFP_TSIZE);
+#endif
+      cnt c[kNCOLS];
+      for (int k = 0; k < kNCOLS; k++) c[k] = raw[k];
+      g_flops = g_mufu = 0;
+      (void)Predicted_Signal(NPARAMS, P, c, F);
+      fs += g_flops;
+      ms += g_mufu;
+      g_flops = g_mufu = 0;
+      Partial_Derivatives(NPARAMS, P, c, F, d);
+      fj += g_flops;
+      mj += g_mufu;
+    }
+  }
+  const double nv = nvox > 0 ? nvox : 1, nm = (double)nvox * nmeas > 0 ? (double)nvox * nmeas : 1;
+  out[0] = fd / nv;
+  out[1] = fs / nm;
+  out[2] = fj / nm;
+  out[3] = md / nv;
+  out[4] = ms / nm;
+  out[5] = mj / nm;
+  return 0;
+}

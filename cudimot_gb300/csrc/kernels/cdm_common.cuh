@@ -1,0 +1,203 @@
+// cdm_common.cuh - shared device pieces of the fitting kernels.
+//
+// Included after the model plugin (functions_gpu.h -> modelparameters.h ->
+// macro_numerical.h -> modelfunctions.h -> cdm_plugin_tail.h) and after
+// cdm_model_sizes.h, which the build generates from modelparameters.cc
+// (CDM_CFP_TSIZE, CDM_FIXP_TSIZE).
+//
+// Work decomposition: a voxel is processed by a group of G consecutive lanes
+// of one warp (G in {4, 8, 16, 32}); lane j of the group takes measurements
+// j, j+G, j+2G, ... Group sums are butterfly (xor) shuffles, which leave the
+// identical value in every lane, so every lane of a group takes the same
+// decisions without a broadcast. Several groups share a warp when G < 32.
+//
+// HBM layouts the kernels read (built by cdm_pack_* kernels):
+//   protocol  float [NCOLS][nmeas_pad]   NCOLS = CFP_Tsize + derived CFP
+//   signals   float [nchunk][nvox][G]    chunk c holds measurements cG..cG+G-1
+// so a warp's signal load is one contiguous 128-byte line.
+#pragma once
+
+#include <stdint.h>
+#include "philox.h"
+
+#ifndef CDM_NT
+#define CDM_NT 128  // threads per CTA
+#endif
+
+constexpr int kNP = NPARAMS;
+constexpr int kNPS = CDM_PSTORE;
+constexpr int kNCOLS = CDM_CFP_TSIZE + CDM_NDCFP;
+constexpr int kNFIX = CDM_FIXP_TSIZE > 0 ? CDM_FIXP_TSIZE : 1;
+
+// Error codes written to the device error word.
+#define CDM_DEVERR_STAGE_TIMEOUT 1
+
+// Bounds, priors and fixed flags as the kernels use them. Bounds and prior
+// arguments are floats, as in CUDIMOT's __constant__ copies.
+struct cdm_limits {
+  int btype[kNP];
+  float bmin[kNP];
+  float bmax[kNP];
+  int ptype[kNP];
+  float pa[kNP];
+  float pb[kNP];
+  int fixed[kNP];
+};
+
+template <int G>
+__device__ __forceinline__ unsigned cdm_group_mask() {
+  if (G == 32) return 0xFFFFFFFFu;
+  const unsigned lane = threadIdx.x & 31u;
+  return ((1u << G) - 1u) << (lane & ~(unsigned)(G - 1));
+}
+
+template <int G, class V>
+__device__ __forceinline__ V cdm_group_sum(V v, unsigned mask) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Protocol staging: one elected thread issues a bulk asynchronous copy
+// (cp.async.bulk, the TMA engine's 1-D form) of the whole protocol table from
+// HBM into shared memory; the CTA waits on an mbarrier. The wait is bounded
+// by the global timer: after 2 s the CTA records CDM_DEVERR_STAGE_TIMEOUT
+// and returns false instead of spinning forever.
+__device__ __forceinline__ bool cdm_stage_protocol(const float* __restrict__ gsrc, float* sdst,
+                                                   uint32_t bytes, int* err) {
+  __shared__ __align__(8) uint64_t bar;
+  const uint32_t sbar = (uint32_t)__cvta_generic_to_shared(&bar);
+  const uint32_t sdst_a = (uint32_t)__cvta_generic_to_shared(sdst);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sbar), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            sdst_a),
+        "l"(gsrc), "r"(bytes), "r"(sbar)
+        : "memory");
+  }
+  uint64_t t0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  uint32_t done = 0;
+  for (;;) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(sbar)
+        : "memory");
+    if (done) break;
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 > 2000000000ull) {
+      if (err) atomicOr(err, CDM_DEVERR_STAGE_TIMEOUT);
+      break;
+    }
+  }
+  __syncthreads();
+  return done != 0;
+}
+
+// Load one measurement's protocol values (raw CFP then derived) from the
+// staged table into a register array the plugin can index.
+__device__ __forceinline__ void cdm_load_cfp(const float* sproto, int nmeas_pad, int m, fp32* cf) {
+#pragma unroll
+  for (int k = 0; k < kNCOLS; k++) cf[k] = fp32(sproto[k * nmeas_pad + m]);
+}
+
+// Per-voxel view handed to the group cost routines.
+struct cdm_voxel_io {
+  const float* sig;  // this lane's first signal value (chunk 0)
+  size_t chunk_stride;
+  int nchunk;
+  int nmeas;
+  int nmeas_pad;
+  int lane;
+};
+
+// Sum of squared residuals over the voxel's measurements: each lane sums its
+// own measurements in FP32, the group total is formed in FP64.
+template <int G>
+__device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const float* sproto,
+                                                fp32* P, fp32* FixP, unsigned gmask) {
+  float acc = 0.0f;
+  for (int c = 0; c < io.nchunk; c++) {
+    const int m = c * G + io.lane;
+    const bool valid = m < io.nmeas;
+    fp32 cf[kNCOLS];
+    cdm_load_cfp(sproto, io.nmeas_pad, valid ? m : 0, cf);
+    const float y = io.sig[(size_t)c * io.chunk_stride];
+    const float s = (float)Predicted_Signal(NPARAMS, P, cf, FixP);
+    const float r = s - y;
+    acc = valid ? fmaf(r, r, acc) : acc;
+  }
+  return cdm_group_sum<G>((double)acc, gmask);
+}
+
+// log I0(x) with the polynomial approximations of Abramowitz & Stegun
+// 9.8.1/9.8.2, as CUDIMOT's logIo (MCMC.cu:32-49).
+__device__ __forceinline__ float cdm_log_i0(float x) {
+  const float b = fabsf(x);
+  if (b < 3.75f) {
+    float a = x / 3.75f;
+    a *= a;
+    return logf(1.0f + a * (3.5156229f + a * (3.0899424f + a * (1.2067492f + a * (0.2659732f +
+                        a * (0.0360768f + a * 0.0045813f))))));
+  }
+  const float a = 3.75f / b;
+  return b + logf((0.39894228f + a * (0.01328592f + a * (0.00225319f + a * (-0.00157565f +
+                  a * (0.00916281f + a * (-0.02057706f + a * (0.02635537f + a * (-0.01647633f +
+                  a * 0.00392377f)))))))) * rsqrtf(b));
+}
+
+// Rician log-likelihood sum without the voxel-constant sum of log(y)
+// (which cancels in every Metropolis ratio): sum of
+// -tau/2 (y^2 + S^2) + log I0(tau S y).
+template <int G>
+__device__ __forceinline__ double cdm_group_rician(const cdm_voxel_io& io, const float* sproto,
+                                                   fp32* P, fp32* FixP, float tau, unsigned gmask) {
+  float acc = 0.0f;
+  for (int c = 0; c < io.nchunk; c++) {
+    const int m = c * G + io.lane;
+    const bool valid = m < io.nmeas;
+    fp32 cf[kNCOLS];
+    cdm_load_cfp(sproto, io.nmeas_pad, valid ? m : 0, cf);
+    const float y = io.sig[(size_t)c * io.chunk_stride];
+    const float s = (float)Predicted_Signal(NPARAMS, P, cf, FixP);
+    const float t = -0.5f * tau * (y * y + s * s) + cdm_log_i0(tau * s * y);
+    acc = valid ? acc + t : acc;
+  }
+  return cdm_group_sum<G>((double)acc, gmask);
+}
+
+// Sum of log(y) over the voxel (for BIC/AIC, which need the full Rician
+// likelihood).
+template <int G>
+__device__ __forceinline__ double cdm_group_sum_log_meas(const cdm_voxel_io& io, unsigned gmask) {
+  float acc = 0.0f;
+  for (int c = 0; c < io.nchunk; c++) {
+    const int m = c * G + io.lane;
+    const float y = io.sig[(size_t)c * io.chunk_stride];
+    acc = (m < io.nmeas) ? acc + logf(y) : acc;
+  }
+  return cdm_group_sum<G>((double)acc, gmask);
+}
+
+__device__ __forceinline__ void cdm_load_params(const double* __restrict__ src, fp32* P) {
+#pragma unroll
+  for (int i = 0; i < kNPS; i++) P[i] = fp32(0.0f);
+#pragma unroll
+  for (int i = 0; i < kNP; i++) P[i] = fp32((float)src[i]);
+}
+
+__device__ __forceinline__ void cdm_load_fixp(const double* __restrict__ src, int fixp_tsize,
+                                              fp32* F) {
+#pragma unroll
+  for (int k = 0; k < kNFIX; k++) F[k] = fp32(k < fixp_tsize ? (float)src[k] : 0.0f);
+}

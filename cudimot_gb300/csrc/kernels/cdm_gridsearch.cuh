@@ -1,0 +1,212 @@
+// cdm_gridsearch.cuh - exhaustive grid search, one voxel per lane group.
+//
+// Semantics follow CUDIMOT's gridSearch_kernel (GridSearch.cu:97-248): the
+// grid parameters of each combination replace the voxel's parameters,
+// combinations outside the bounds are skipped (checkBounds, :25-47), and the
+// first combination with the lowest sum of squares wins (strict '<',
+// :216). Combination order is Model.cu's set_grid order.
+//
+// GB300 structure: costs are evaluated in FP32 (each lane sums its own
+// measurements, the group total in FP64). Each group tracks its four best
+// combinations. If the runner-up lies within `band` (relative) of the best,
+// the FP32 ranking is not trusted: the voxel is flagged and
+// cdm_gs_recheck_kernel re-evaluates the candidates (or, when more than
+// three are within the band, every combination) in FP64 with CUDIMOT's
+// summation order and keeps the first minimum. `band` is chosen well above
+// the measured FP32 cost error (~1e-6 relative), so the argmin equals the
+// FP64 argmin.
+#pragma once
+#include "cdm_common.cuh"
+
+constexpr int kGsTop = 4;
+
+struct cdm_gs_args {
+  int nvox, nmeas, nmeas_pad, nchunk, fixp_tsize;
+  uint32_t proto_bytes;
+  const float* proto;
+  const float* sig;
+  double* params;
+  const double* fixp;
+  const double* grid;  // [combs][ngp]
+  int ngp;
+  int combs;
+  int gpos[kNP];       // column of parameter p in the grid, or -1
+  float band;
+  int* flags;          // [nvox]: 0 decided, 1 recheck candidates, 2 recheck all
+  int* cand;           // [nvox][kGsTop]
+  int* best;           // [nvox] winning combination (or -1)
+  int* err;
+  cdm_limits lim;
+};
+
+__device__ __forceinline__ bool cdm_gs_in_bounds(const cdm_limits& L, const double* x) {
+#pragma unroll
+  for (int p = 0; p < kNP; p++) {
+    if (L.btype[p] == BMIN) {
+      if (x[p] < (double)L.bmin[p]) return false;
+    } else if (L.btype[p] == BMAX) {
+      if (x[p] > (double)L.bmax[p]) return false;
+    } else if (L.btype[p] == BMINMAX) {
+      if (x[p] < (double)L.bmin[p]) return false;
+      if (x[p] > (double)L.bmax[p]) return false;
+    }
+  }
+  return true;
+}
+
+template <int G>
+__global__ void __launch_bounds__(CDM_NT) cdm_gridsearch_kernel(const __grid_constant__ cdm_gs_args a) {
+  extern __shared__ __align__(16) float sproto[];
+  if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
+  const int v = blockIdx.x * (CDM_NT / G) + (int)threadIdx.x / G;
+  if (v >= a.nvox) return;
+  const unsigned gm = cdm_group_mask<G>();
+  const int lane = (int)threadIdx.x % G;
+  const cdm_limits& L = a.lim;
+
+  cdm_voxel_io io;
+  io.sig = a.sig + (size_t)v * G + lane;
+  io.chunk_stride = (size_t)a.nvox * G;
+  io.nchunk = a.nchunk;
+  io.nmeas = a.nmeas;
+  io.nmeas_pad = a.nmeas_pad;
+  io.lane = lane;
+
+  double base[kNP];
+#pragma unroll
+  for (int p = 0; p < kNP; p++) base[p] = a.params[(size_t)v * kNP + p];
+  fp32 FixP[kNFIX];
+  cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
+
+  double bcost[kGsTop];
+  int bcomb[kGsTop];
+#pragma unroll
+  for (int k = 0; k < kGsTop; k++) {
+    bcost[k] = 9e20;  // CUDIMOT's initial best cost (GridSearch.cu:178)
+    bcomb[k] = -1;
+  }
+  for (int c = 0; c < a.combs; c++) {
+    double trial[kNP];
+#pragma unroll
+    for (int p = 0; p < kNP; p++)
+      trial[p] = a.gpos[p] >= 0 ? __ldg(a.grid + (size_t)c * a.ngp + a.gpos[p]) : base[p];
+    if (!cdm_gs_in_bounds(L, trial)) continue;
+    fp32 P[kNPS];
+#pragma unroll
+    for (int i = 0; i < kNPS; i++) P[i] = fp32(0.0f);
+#pragma unroll
+    for (int p = 0; p < kNP; p++) P[p] = fp32((float)trial[p]);
+    cdm_update_derived(P, FixP);
+    const double cost = cdm_group_sse<G>(io, sproto, P, FixP, gm);
+    // Sorted insertion with constant indices (register arrays): entries
+    // strictly worse than `cost` move down one place, equal costs keep the
+    // earlier combination first (CUDIMOT's strict '<').
+#pragma unroll
+    for (int j = kGsTop - 1; j >= 0; j--) {
+      const bool above = (j > 0) && (cost < bcost[j > 0 ? j - 1 : 0]);
+      const bool here = cost < bcost[j];
+      if (above) {
+        bcost[j] = bcost[j - 1 >= 0 ? j - 1 : 0];
+        bcomb[j] = bcomb[j - 1 >= 0 ? j - 1 : 0];
+      } else if (here) {
+        bcost[j] = cost;
+        bcomb[j] = c;
+      }
+    }
+  }
+  if (lane != 0) return;
+  a.best[v] = bcomb[0];
+  if (bcomb[0] < 0) {
+    a.flags[v] = 0;
+    return;
+  }
+  const double lim = bcost[0] * (1.0 + (double)a.band);
+  int nin = 0;
+#pragma unroll
+  for (int k = 0; k < kGsTop; k++) nin += (bcomb[k] >= 0 && bcost[k] <= lim) ? 1 : 0;
+  a.flags[v] = nin <= 1 ? 0 : (nin < kGsTop ? 1 : 2);
+#pragma unroll
+  for (int k = 0; k < kGsTop; k++) a.cand[(size_t)v * kGsTop + k] = bcomb[k];
+#pragma unroll
+  for (int p = 0; p < kNP; p++)
+    if (a.gpos[p] >= 0) a.params[(size_t)v * kNP + p] = a.grid[(size_t)bcomb[0] * a.ngp + a.gpos[p]];
+}
+
+// ----------------------------------------------------------------------------
+// FP64 re-check of flagged voxels: one warp per voxel, lane l sums
+// measurements l, l+32, ... and the warp folds with the 16/8/4/2/1 shuffle
+// tree, CUDIMOT's summation order (GridSearch.cu:49-95).
+struct cdm_gs_recheck_args {
+  int nvox, nmeas, fixp_tsize;
+  const double* proto64;  // [nmeas][NCOLS]
+  const double* meas;     // [nvox][nmeas]
+  double* params;
+  const double* fixp;
+  const double* grid;
+  int ngp, combs;
+  int gpos[kNP];
+  const int* flags;
+  const int* cand;
+  int* best;
+  unsigned long long* rechecked;
+  cdm_limits lim;
+};
+
+__device__ __forceinline__ double cdm_warp_cost64(const cdm_gs_recheck_args& a, int v, double* P,
+                                                  double* FixP) {
+  const int lane = threadIdx.x & 31;
+  double acc = 0.0;
+  for (int m = lane; m < a.nmeas; m += 32) {
+    double cf[kNCOLS];
+#pragma unroll
+    for (int k = 0; k < kNCOLS; k++) cf[k] = a.proto64[(size_t)m * kNCOLS + k];
+    const double e = Predicted_Signal(NPARAMS, P, cf, FixP) - a.meas[(size_t)v * a.nmeas + m];
+    acc += e * e;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
+  return __shfl_sync(0xFFFFFFFFu, acc, 0);
+}
+
+__global__ void __launch_bounds__(CDM_NT) cdm_gs_recheck_kernel(const __grid_constant__ cdm_gs_recheck_args a) {
+  const int v = blockIdx.x * (CDM_NT / 32) + (int)threadIdx.x / 32;
+  if (v >= a.nvox) return;
+  const int flag = a.flags[v];
+  if (flag == 0) return;
+  const int lane = threadIdx.x & 31;
+  double base[kNP];
+#pragma unroll
+  for (int p = 0; p < kNP; p++) base[p] = a.params[(size_t)v * kNP + p];
+  double FixP[kNFIX];
+#pragma unroll
+  for (int k = 0; k < kNFIX; k++) FixP[k] = k < a.fixp_tsize ? a.fixp[(size_t)v * a.fixp_tsize + k] : 0.0;
+  const int ntry = flag == 1 ? kGsTop : a.combs;
+  double best = 9e20;
+  int bestc = -1;
+  for (int t = 0; t < ntry; t++) {
+    const int c = flag == 1 ? a.cand[(size_t)v * kGsTop + t] : t;
+    if (c < 0) continue;
+    double P[kNPS];
+#pragma unroll
+    for (int i = 0; i < kNPS; i++) P[i] = 0.0;
+#pragma unroll
+    for (int p = 0; p < kNP; p++)
+      P[p] = a.gpos[p] >= 0 ? a.grid[(size_t)c * a.ngp + a.gpos[p]] : base[p];
+    if (!cdm_gs_in_bounds(a.lim, P)) continue;
+    cdm_update_derived(P, FixP);
+    const double cost = cdm_warp_cost64(a, v, P, FixP);
+    // strict '<' in combination order; candidates arrive cost-sorted, so ties
+    // are broken towards the lower combination index explicitly.
+    if (cost < best || (cost == best && c < bestc)) {
+      best = cost;
+      bestc = c;
+    }
+  }
+  if (lane == 0 && bestc >= 0) {
+    a.best[v] = bestc;
+#pragma unroll
+    for (int p = 0; p < kNP; p++)
+      if (a.gpos[p] >= 0) a.params[(size_t)v * kNP + p] = a.grid[(size_t)bestc * a.ngp + a.gpos[p]];
+    if (a.rechecked) atomicAdd(a.rechecked, 1ull);
+  }
+}

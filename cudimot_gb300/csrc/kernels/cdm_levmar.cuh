@@ -1,0 +1,264 @@
+// cdm_levmar.cuh - bounded Levenberg-Marquardt, one voxel per lane group.
+//
+// Semantics follow CUDIMOT's levenberg_kernel (Levenberg_Marquardt.cu:
+// 409-623): parameters are optimised in a transformed space (log for
+// one-sided bounds, tan for two-sided bounds, with CUDIMOT's 1e-4 nudges and
+// speed factor 10; :37-118); the loop runs while
+// !(success && iter++ >= max_iters) so only accepted steps count; damping
+// is Marquardt's (1+lambda) diagonal scaling (or Levenberg's +lambda);
+// lambda starts at 0.1, is divided by 10 on success and multiplied by 10 on
+// failure; the fit ends when 2|dc| <= 1e-8 (|c|+|c'|+2e-16) after a success
+// or when lambda exceeds 1e20; FixConstraintsLM runs at the end.
+//
+// GB300 structure: one pass over the measurements per accepted step forms
+// the residual and the Jacobian once and accumulates J^T r and the upper
+// triangle of J^T J in FP32 registers (CUDIMOT evaluates S and dS twice, once
+// for the gradient and once for the Hessian, with a warp reduction per
+// element and 32-measurement chunk). The lane partials are summed across the
+// group in FP64 and the damped normal equations are solved in FP64 registers
+// by the same unpivoted Gauss-Jordan elimination as CUDIMOT's LUsolver
+// (:334-407). Undamped sums are kept, and damping is applied to a fresh copy
+// each iteration, which equals CUDIMOT's cumulative rescaling.
+#pragma once
+#include "cdm_common.cuh"
+
+struct cdm_lm_args {
+  int nvox, nmeas, nmeas_pad, nchunk, fixp_tsize;
+  uint32_t proto_bytes;
+  const float* proto;
+  const float* sig;
+  double* params;
+  const double* fixp;
+  int max_iters;
+  int marquardt;
+  int* err;
+  unsigned long long* iter_count;  // sum of loop passes, may be null
+  unsigned long long* succ_count;  // sum of accepted steps, may be null
+  cdm_limits lim;
+};
+
+constexpr float kTwoDivPIf = 0.636619772367581f;
+constexpr float kAvoidf = 1e-4f;
+constexpr float kSpeedf = 10.0f;
+
+__device__ __forceinline__ float cdm_minmax_inv(float x, float lo, float hi) {
+  float t = x - (lo + hi) * 0.5f;
+  t *= 2.0f / ((hi - lo) * kTwoDivPIf);
+  return tanf(t) * kSpeedf;
+}
+
+// invtransformAll (Levenberg_Marquardt.cu:90-103).
+__device__ __forceinline__ void cdm_lm_inv_transform(const cdm_limits& L, fp32* P, float* Pt) {
+#pragma unroll
+  for (int p = 0; p < kNP; p++) {
+    const float lo = L.bmin[p], hi = L.bmax[p];
+    float x = (float)P[p];
+    if (L.btype[p] == BMIN) {
+      Pt[p] = logf(x - lo);
+    } else if (L.btype[p] == BMAX) {
+      Pt[p] = logf(hi - x);
+    } else if (L.btype[p] == BMINMAX) {
+      if (x <= lo + kAvoidf) x += kAvoidf;
+      if (x >= hi - kAvoidf) x -= kAvoidf;
+      P[p] = fp32(x);
+      Pt[p] = cdm_minmax_inv(x, lo, hi);
+    } else {
+      Pt[p] = x;
+    }
+  }
+}
+
+// transformAll (Levenberg_Marquardt.cu:105-118); may nudge Pt.
+__device__ __forceinline__ void cdm_lm_transform(const cdm_limits& L, fp32* P, float* Pt) {
+#pragma unroll
+  for (int p = 0; p < kNP; p++) {
+    const float lo = L.bmin[p], hi = L.bmax[p];
+    if (L.btype[p] == BMIN) {
+      P[p] = fp32(expf(Pt[p]) + lo);
+    } else if (L.btype[p] == BMAX) {
+      P[p] = fp32(hi - expf(Pt[p]));
+    } else if (L.btype[p] == BMINMAX) {
+      float x = (hi - lo) * 0.5f * atanf(Pt[p] / kSpeedf) * kTwoDivPIf + (lo + hi) * 0.5f;
+      if (x <= lo + kAvoidf) {
+        x += kAvoidf;
+        Pt[p] = cdm_minmax_inv(x, lo, hi);
+      }
+      if (x >= hi - kAvoidf) {
+        x -= kAvoidf;
+        Pt[p] = cdm_minmax_inv(x, lo, hi);
+      }
+      P[p] = fp32(x);
+    } else {
+      P[p] = fp32(Pt[p]);
+    }
+  }
+}
+
+// d theta / d theta_t per parameter (derivative_transf, :120-135).
+__device__ __forceinline__ void cdm_lm_chain(const cdm_limits& L, const float* Pt, float* f) {
+#pragma unroll
+  for (int p = 0; p < kNP; p++) {
+    if (L.btype[p] == BMIN)
+      f[p] = expf(Pt[p]);
+    else if (L.btype[p] == BMAX)
+      f[p] = -expf(Pt[p]);
+    else if (L.btype[p] == BMINMAX)
+      f[p] = (L.bmax[p] - L.bmin[p]) * 0.5f * kTwoDivPIf * (kSpeedf / (kSpeedf * kSpeedf + Pt[p] * Pt[p]));
+    else
+      f[p] = 1.0f;
+  }
+}
+
+constexpr int kNH = kNP * (kNP + 1) / 2;
+
+template <int G>
+__global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constant__ cdm_lm_args a) {
+  extern __shared__ __align__(16) float sproto[];
+  if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
+  const int v = blockIdx.x * (CDM_NT / G) + (int)threadIdx.x / G;
+  if (v >= a.nvox) return;
+  const unsigned gm = cdm_group_mask<G>();
+  const int lane = (int)threadIdx.x % G;
+  const cdm_limits& L = a.lim;
+
+  cdm_voxel_io io;
+  io.sig = a.sig + (size_t)v * G + lane;
+  io.chunk_stride = (size_t)a.nvox * G;
+  io.nchunk = a.nchunk;
+  io.nmeas = a.nmeas;
+  io.nmeas_pad = a.nmeas_pad;
+  io.lane = lane;
+
+  fp32 P[kNPS], FixP[kNFIX];
+  float Pt[kNP];
+  cdm_load_params(a.params + (size_t)v * kNP, P);
+  cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
+  cdm_lm_inv_transform(L, P, Pt);
+  cdm_update_derived(P, FixP);
+  double pcf = cdm_group_sse<G>(io, sproto, P, FixP, gm);
+
+  double H[kNH], g[kNP];
+#pragma unroll
+  for (int i = 0; i < kNH; i++) H[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < kNP; i++) g[i] = 0.0;
+  double lambda = 0.1;
+  bool success = true, end = false;
+  int iter = 0, passes = 0, nsucc = 0;
+  while (!(success && iter++ >= a.max_iters)) {
+    passes++;
+    if (success) {
+      float chain[kNP];
+      cdm_lm_chain(L, Pt, chain);
+      float gl[kNP], hl[kNH];
+#pragma unroll
+      for (int i = 0; i < kNP; i++) gl[i] = 0.0f;
+#pragma unroll
+      for (int i = 0; i < kNH; i++) hl[i] = 0.0f;
+      for (int c = 0; c < io.nchunk; c++) {
+        const int m = c * G + lane;
+        const bool valid = m < io.nmeas;
+        fp32 cf[kNCOLS];
+        cdm_load_cfp(sproto, io.nmeas_pad, valid ? m : 0, cf);
+        const float y = io.sig[(size_t)c * io.chunk_stride];
+        const float r = valid ? (float)Predicted_Signal(NPARAMS, P, cf, FixP) - y : 0.0f;
+        fp32 d[kNP];
+        Partial_Derivatives(NPARAMS, P, cf, FixP, d);
+        float j[kNP];
+#pragma unroll
+        for (int i = 0; i < kNP; i++) j[i] = valid ? (float)d[i] * chain[i] : 0.0f;
+#pragma unroll
+        for (int i = 0; i < kNP; i++) gl[i] = fmaf(r, j[i], gl[i]);
+        int k = 0;
+#pragma unroll
+        for (int i = 0; i < kNP; i++)
+#pragma unroll
+          for (int q = i; q < kNP; q++) {
+            hl[k] = fmaf(j[i], j[q], hl[k]);
+            k++;
+          }
+      }
+      // Group sums in FP64; factor 2 of CUDIMOT's gradient/Hessian (:240, :308).
+#pragma unroll
+      for (int i = 0; i < kNP; i++) g[i] = L.fixed[i] ? 0.0 : 2.0 * cdm_group_sum<G>((double)gl[i], gm);
+      int k = 0;
+#pragma unroll
+      for (int i = 0; i < kNP; i++)
+#pragma unroll
+        for (int q = i; q < kNP; q++) {
+          const double s = 2.0 * cdm_group_sum<G>((double)hl[k], gm);
+          H[k++] = (L.fixed[i] || L.fixed[q]) ? (i == q ? 1.0 : 0.0) : s;
+        }
+    }
+    // Damped system and unpivoted Gauss-Jordan on [A | g].
+    double M[kNP][kNP + 1];
+    {
+      int k = 0;
+#pragma unroll
+      for (int i = 0; i < kNP; i++)
+#pragma unroll
+        for (int q = i; q < kNP; q++) {
+          M[i][q] = H[k];
+          M[q][i] = H[k];
+          k++;
+        }
+#pragma unroll
+      for (int i = 0; i < kNP; i++) {
+        M[i][i] = a.marquardt ? (1.0 + lambda) * M[i][i] : M[i][i] + lambda;
+        M[i][kNP] = g[i];
+      }
+    }
+#pragma unroll
+    for (int col = 0; col < kNP; col++) {
+      const double inv = 1.0 / M[col][col];
+#pragma unroll
+      for (int j = col; j <= kNP; j++) M[col][j] *= inv;
+#pragma unroll
+      for (int row = col + 1; row < kNP; row++) {
+        const double f = M[row][col];
+#pragma unroll
+        for (int j = col; j <= kNP; j++) M[row][j] -= f * M[col][j];
+      }
+    }
+#pragma unroll
+    for (int col = kNP - 1; col > 0; col--)
+#pragma unroll
+      for (int row = 0; row < col; row++) M[row][kNP] -= M[row][col] * M[col][kNP];
+
+    float step[kNP];
+#pragma unroll
+    for (int i = 0; i < kNP; i++) step[i] = Pt[i] - (float)M[i][kNP];
+    fp32 Pn[kNPS];
+#pragma unroll
+    for (int i = 0; i < kNPS; i++) Pn[i] = P[i];
+    cdm_lm_transform(L, Pn, step);
+    cdm_update_derived(Pn, FixP);
+    const double ncf = cdm_group_sse<G>(io, sproto, Pn, FixP, gm);
+    success = ncf < pcf;
+    if (success) {
+      nsucc++;
+#pragma unroll
+      for (int i = 0; i < kNP; i++) Pt[i] = step[i];
+#pragma unroll
+      for (int i = 0; i < kNPS; i++) P[i] = Pn[i];
+      lambda *= 0.1;
+      if (2.0 * fabs(pcf - ncf) <= 1.0e-8 * (fabs(pcf) + fabs(ncf) + 2.0e-16)) end = true;
+      pcf = ncf;
+    } else {
+      lambda *= 10.0;
+      if (lambda > 1.0e20) end = true;
+      // CUDIMOT re-derives P from Pt after a rejected step (:593), which can
+      // nudge Pt at a two-sided bound.
+      cdm_lm_transform(L, P, Pt);
+      cdm_update_derived(P, FixP);
+    }
+    if (end) break;
+  }
+  FixConstraintsLM(NPARAMS, P);
+  if (lane == 0) {
+#pragma unroll
+    for (int p = 0; p < kNP; p++) a.params[(size_t)v * kNP + p] = (double)(float)P[p];
+    if (a.iter_count) atomicAdd(a.iter_count, (unsigned long long)passes);
+    if (a.succ_count) atomicAdd(a.succ_count, (unsigned long long)nsucc);
+  }
+}

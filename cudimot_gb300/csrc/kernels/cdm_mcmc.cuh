@@ -1,0 +1,257 @@
+// cdm_mcmc.cuh - Metropolis-within-Gibbs sampler, one voxel per lane group.
+//
+// Semantics follow CUDIMOT's mcmc_kernel (MCMC.cu:327-683) launched twice by
+// MCMC<T>::run (MCMC.cu:799-847): a burn-in of max(bi,1) iterations that
+// always adapts the proposal widths, then a recording run of nj iterations
+// that keeps every se-th state. Here both runs are one launch with the chain
+// state kept in registers between them.
+//  * proposal widths start at P/10 (MCMC.cu:428) and are scaled by
+//    sqrt((accepted+1)/(rejected+1)) every se iterations, capped at 1e10
+//    (MCMC.cu:630-646);
+//  * parameters are clamped into bounds and priors initialised at the start
+//    of each run (MCMC.cu:97-139);
+//  * per iteration: the Rician precision tau (if enabled), then every
+//    parameter in order: propose, reject outside bounds or
+//    ConstraintsMCMC, otherwise accept if exp(E_old - E_new) > U
+//    (MCMC.cu:498-613);
+//  * Gaussian likelihood (n/2) log(SSE/2); Rician -n log(tau) - sum(...)
+//    (MCMC.cu:254-307).
+// Differences: draws come from Philox (philox.h), keyed by the seed and
+// counted by (voxel, iteration, parameter, part); fixed parameters skip the
+// likelihood evaluation CUDIMOT spends re-proposing them at their own value
+// (always accepted there too). Energies are kept in FP64; the SSE is summed
+// in FP32 per lane and in FP64 across lanes.
+#pragma once
+#include "cdm_common.cuh"
+
+struct cdm_mcmc_args {
+  int nvox, nmeas, nmeas_pad, nchunk, fixp_tsize;
+  uint32_t proto_bytes;
+  const float* proto;
+  const float* sig;
+  double* params;
+  const double* fixp;
+  double* samples;
+  double* tau_samples;
+  int nburn, njumps, sampleevery, nsamples, update_proposal;
+  uint64_t seed;
+  uint32_t stream;
+  uint32_t voxel_offset;
+  int* err;
+  cdm_limits lim;
+};
+
+__device__ __forceinline__ float cdm_prior(const cdm_limits& L, int p, fp32* P, int nmeas,
+                                           fp32* cfp_all, fp32* FixP) {
+  const float x = (float)P[p];
+  switch (L.ptype[p]) {
+    case GAUSSPRIOR: {
+      const float d = x - L.pa[p];
+      return d * d / (2.0f * L.pb[p] * L.pb[p]);
+    }
+    case GAMMAPRIOR:
+      return (1.0f - L.pa[p]) * logf(x) + L.pb[p] * x;
+    case ARDPRIOR:
+      return L.pa[p] * logf(x);
+    case SINPRIOR:
+      return -logf(fabsf(sinf(x) * 0.5f));
+    case CUSTOM:
+      return (float)custom_priors(p, P, nmeas, cfp_all, FixP);
+    default:
+      return 0.0f;
+  }
+}
+
+__device__ __forceinline__ bool cdm_in_bounds(const cdm_limits& L, int p, fp32* P) {
+  if (!ConstraintsMCMC(NPARAMS, P)) return false;
+  const float x = (float)P[p];
+  if (L.btype[p] == BMIN) return !(x < L.bmin[p]);
+  if (L.btype[p] == BMAX) return !(x > L.bmax[p]);
+  if (L.btype[p] == BMINMAX) return !(x < L.bmin[p]) && !(x > L.bmax[p]);
+  return true;
+}
+
+template <int G, bool RICIAN>
+__device__ __forceinline__ double cdm_likelihood(const cdm_voxel_io& io, const float* sproto,
+                                                 fp32* P, fp32* FixP, float tau, unsigned gmask) {
+  if (RICIAN) {
+    const double s = cdm_group_rician<G>(io, sproto, P, FixP, tau, gmask);
+    return -(double)io.nmeas * (double)logf(tau) - s;
+  }
+  const double sse = cdm_group_sse<G>(io, sproto, P, FixP, gmask);
+  return 0.5 * (double)io.nmeas * (double)logf((float)(sse * 0.5));
+}
+
+template <int G, bool RICIAN>
+__global__ void __launch_bounds__(CDM_NT) cdm_mcmc_kernel(const __grid_constant__ cdm_mcmc_args a) {
+  extern __shared__ __align__(16) float sproto[];
+  if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
+  const int v = blockIdx.x * (CDM_NT / G) + (int)threadIdx.x / G;
+  if (v >= a.nvox) return;
+  const unsigned gm = cdm_group_mask<G>();
+  const int lane = (int)threadIdx.x % G;
+  const cdm_limits& L = a.lim;
+
+  cdm_voxel_io io;
+  io.sig = a.sig + (size_t)v * G + lane;
+  io.chunk_stride = (size_t)a.nvox * G;
+  io.nchunk = a.nchunk;
+  io.nmeas = a.nmeas;
+  io.nmeas_pad = a.nmeas_pad;
+  io.lane = lane;
+
+  fp32 P[kNPS], FixP[kNFIX];
+  cdm_load_params(a.params + (size_t)v * kNP, P);
+  cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
+  float propSD[kNP], prior[kNP];
+  int acc[kNP], rej[kNP];
+#pragma unroll
+  for (int p = 0; p < kNP; p++) propSD[p] = (float)P[p] / 10.0f;
+  float tau = 0.0f, tauSD = 0.0f;
+  int tacc = 0, trej = 0;
+  const uint32_t vid = a.voxel_offset + (uint32_t)v;
+  const int nburn = a.nburn < 1 ? 1 : a.nburn;
+  // Custom priors receive the whole CFP array in CUDIMOT; with the staged
+  // SoA table there is no AoS copy, so they see the voxel's first
+  // measurement only (no shipped plugin defines one).
+  fp32 cf0[kNCOLS];
+  cdm_load_cfp(sproto, a.nmeas_pad, 0, cf0);
+
+  double energy = 0.0;
+  for (int phase = 0; phase < 2; phase++) {
+    const bool recording = phase == 1;
+    const int niters = recording ? a.njumps : nburn;
+#pragma unroll
+    for (int p = 0; p < kNP; p++) {
+      acc[p] = 0;
+      rej[p] = 0;
+      float x = (float)P[p];
+      if (L.btype[p] == BMIN) {
+        if (x < L.bmin[p]) x = L.bmin[p];
+      } else if (L.btype[p] == BMAX) {
+        if (x > L.bmax[p]) x = L.bmax[p];
+      } else if (L.btype[p] == BMINMAX) {
+        if (x < L.bmin[p]) x = L.bmin[p];
+        else if (x > L.bmax[p]) x = L.bmax[p];
+      }
+      P[p] = fp32(x);
+    }
+    cdm_update_derived(P, FixP);
+    float total_prior = 0.0f;
+#pragma unroll
+    for (int p = 0; p < kNP; p++) {
+      prior[p] = cdm_prior(L, p, P, a.nmeas, cf0, FixP);
+      total_prior += prior[p];
+    }
+    tacc = trej = 0;
+    if (RICIAN && !recording) {
+      // Initialise_TauRician (MCMC.cu:193-251): tau = 1 / variance of residuals.
+      float s1 = 0.0f;
+      for (int c = 0; c < io.nchunk; c++) {
+        const int m = c * G + lane;
+        fp32 cf[kNCOLS];
+        cdm_load_cfp(sproto, io.nmeas_pad, m < io.nmeas ? m : 0, cf);
+        const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - io.sig[(size_t)c * io.chunk_stride];
+        s1 = (m < io.nmeas) ? s1 + r : s1;
+      }
+      const float mean = (float)(cdm_group_sum<G>((double)s1, gm) / io.nmeas);
+      float s2 = 0.0f;
+      for (int c = 0; c < io.nchunk; c++) {
+        const int m = c * G + lane;
+        fp32 cf[kNCOLS];
+        cdm_load_cfp(sproto, io.nmeas_pad, m < io.nmeas ? m : 0, cf);
+        const float r = mean - ((float)Predicted_Signal(NPARAMS, P, cf, FixP) - io.sig[(size_t)c * io.chunk_stride]);
+        s2 = (m < io.nmeas) ? fmaf(r, r, s2) : s2;
+      }
+      tau = (float)((double)io.nmeas / cdm_group_sum<G>((double)s2, gm));
+      tauSD = tau * 0.5f;
+    }
+    energy = (double)total_prior + cdm_likelihood<G, RICIAN>(io, sproto, P, FixP, tau, gm);
+
+    for (int it = 0; it < niters; it++) {
+      const uint32_t git = (uint32_t)(recording ? nburn + it : it);
+      if (RICIAN) {
+        const cdm_draw d = cdm_mcmc_draw(a.seed, vid, git, CDM_RNG_SLOT_TAU, a.stream);
+        const float old = tau;
+        tau = tau + d.normal * tauSD;
+        if (tau > 0.0f) {
+          float tp = 0.0f;
+#pragma unroll
+          for (int p = 0; p < kNP; p++) tp += prior[p];
+          const double ne = (double)tp + cdm_likelihood<G, RICIAN>(io, sproto, P, FixP, tau, gm);
+          if (expf((float)(energy - ne)) > d.uniform) {
+            tacc++;
+            energy = ne;
+          } else {
+            trej++;
+            tau = old;
+          }
+        } else {
+          trej++;
+          tau = old;
+        }
+      }
+#pragma unroll
+      for (int p = 0; p < kNP; p++) {
+        if (L.fixed[p]) {
+          acc[p]++;
+          continue;
+        }
+        const cdm_draw d = cdm_mcmc_draw(a.seed, vid, git, (uint32_t)p, a.stream);
+        fp32 saved[kNPS];
+#pragma unroll
+        for (int i = 0; i < kNPS; i++) saved[i] = P[i];
+        P[p] = fp32((float)P[p] + d.normal * propSD[p]);
+        if (cdm_in_bounds(L, p, P)) {
+          cdm_update_derived(P, FixP);
+          const float np_ = cdm_prior(L, p, P, a.nmeas, cf0, FixP);
+          float tp = 0.0f;
+#pragma unroll
+          for (int q = 0; q < kNP; q++) tp += (q == p) ? np_ : prior[q];
+          const double ne = (double)tp + cdm_likelihood<G, RICIAN>(io, sproto, P, FixP, tau, gm);
+          if (expf((float)(energy - ne)) > d.uniform) {
+            acc[p]++;
+            energy = ne;
+            prior[p] = np_;
+          } else {
+            rej[p]++;
+#pragma unroll
+            for (int i = 0; i < kNPS; i++) P[i] = saved[i];
+          }
+        } else {
+          rej[p]++;
+#pragma unroll
+          for (int i = 0; i < kNPS; i++) P[i] = saved[i];
+        }
+      }
+      if (recording && (it % a.sampleevery) == 0) {
+        const int s = it / a.sampleevery;
+        if (s < a.nsamples && lane == 0) {
+          double* dst = a.samples + (size_t)v * kNP * a.nsamples + s;
+#pragma unroll
+          for (int p = 0; p < kNP; p++) dst[(size_t)p * a.nsamples] = (double)(float)P[p];
+          if (RICIAN && a.tau_samples) a.tau_samples[(size_t)v * a.nsamples + s] = (double)tau;
+        }
+      }
+      if ((!recording || a.update_proposal) && it > 0 && (it % a.sampleevery) == 0) {
+#pragma unroll
+        for (int p = 0; p < kNP; p++) {
+          propSD[p] *= sqrtf(((float)acc[p] + 1.0f) / ((float)rej[p] + 1.0f));
+          propSD[p] = fminf(propSD[p], 1e10f);
+          acc[p] = 0;
+          rej[p] = 0;
+        }
+        if (RICIAN) {
+          tauSD *= sqrtf(((float)tacc + 1.0f) / ((float)trej + 1.0f));
+          tauSD = fminf(tauSD, 1e10f);
+          tacc = 0;
+          trej = 0;
+        }
+      }
+    }
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int p = 0; p < kNP; p++) a.params[(size_t)v * kNP + p] = (double)(float)P[p];
+  }
+}

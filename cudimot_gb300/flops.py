@@ -1,0 +1,47 @@
+"""Algorithmic FP32 work per voxel, from the operation-count build of the
+plugin (csrc/host/cdm_flops.cpp).
+
+Work model (per voxel, one parameter proposal = one likelihood):
+  likelihood  = Derived_P + nmeas * (Predicted_Signal + 3)   [r=s-y, r*r, +]
+  MCMC        = (nburn + njumps) * free_params * likelihood
+  grid search = combinations * likelihood
+Counts +, -, *, / as one FLOP each; transcendental and square-root calls
+are reported separately (they run on the SFU/MUFU path).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .capi import LIBDIR
+
+
+def count_ops(model, params, cfp, fixp):
+    lib = C.CDLL(os.path.join(LIBDIR, f"libcdm_flops_{model}.so"))
+    lib.cdm_count_ops.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.cdm_count_ops.restype = C.c_int
+    params = np.ascontiguousarray(params, dtype=np.float64)
+    cfp = np.ascontiguousarray(cfp, dtype=np.float64)
+    fixp = np.ascontiguousarray(fixp, dtype=np.float64)
+    out = np.zeros(6)
+    lib.cdm_count_ops(params.shape[0], params.ctypes.data, cfp.shape[0], cfp.ctypes.data,
+                      fixp.ctypes.data, out.ctypes.data)
+    keys = ("derived_p", "signal", "jacobian", "derived_p_mufu", "signal_mufu", "jacobian_mufu")
+    return dict(zip(keys, out.tolist()))
+
+
+def likelihood_flops(ops, nmeas):
+    return ops["derived_p"] + nmeas * (ops["signal"] + 3.0)
+
+
+def watson_c1_flops_per_voxel(nburn=1250, njumps=1250, combs=968, nmeas=288, n=512, seed=1):
+    """NODDI-Watson FLOPs per voxel of the C1 workload, averaged over
+    parameters drawn from its prior and its 288-measurement protocol."""
+    from . import synth
+    rng = np.random.default_rng(seed)
+    cfp = synth.protocol(18, [(90, 1000.0), (90, 2000.0), (90, 3000.0)], rng)
+    truth, S0 = synth.watson_truth(n, rng)
+    ops = count_ops("NODDI_Watson", truth, cfp, S0[:, None])
+    like = likelihood_flops(ops, nmeas)
+    return {"ops": ops, "likelihood": like, "mcmc": (nburn + njumps) * 5 * like,
+            "gridsearch": combs * like}

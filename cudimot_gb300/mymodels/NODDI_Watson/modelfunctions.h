@@ -1,0 +1,348 @@
+// NODDI-Watson (Zhang et al., NeuroImage 61:1000-1016, 2012) in CUDIMOT's
+// parameterisation (mymodels/NODDI_Watson/modelfunctions.h:88-108):
+//
+//   S = S0 [ (1-fiso) ((1-fin) E + fin I) + fiso exp(-b Diso) ]
+//
+// P = {fiso, fintra, kappa, th, ph}; FixP = {S0}; CFP = {gx, gy, gz, b}.
+// E: hindered extra-cellular signal with the Watson-averaged tensor
+//    (WatsonFunctions.h:53-89); I: Watson-dispersed sticks expanded in
+//    even spherical harmonics up to order 12 (modelfunctions.h:45-86).
+//
+// The model, its branch points (kappa <= 0.4 series, kappa > 30 fits,
+// kappa < 1e-5 hindered-diffusion series, b*Dpar <= 0.05 integral series)
+// and its numerical derivatives for kappa, th, ph are CUDIMOT's. The
+// evaluation is reorganised so that it is accurate in single precision:
+//  * the seven Legendre-Gaussian integrals and exp(-b Diso) depend on b
+//    only; they are computed once per protocol in double (Derived_CFP) and
+//    appended to each measurement's CFP values;
+//  * everything that depends on the parameters only (orientation vector,
+//    equivalent diffusivities, SH coefficients of the Watson density) is
+//    computed once per parameter change (Derived_P) and appended to P;
+//  * for 0.4 < kappa <= 30 the SH coefficients are 2 sqrt(pi) sqrt(4l+1)
+//    <P_2l>_kappa with the Watson moments <P_2l> from a backward (Miller)
+//    three-term recurrence in the Legendre basis. The closed forms used by
+//    CUDIMOT (WatsonFunctions.h:112-172) cancel terms of size ~1e10 and
+//    are only usable in double; the recurrence is stable in float.
+//  * the seven Legendre polynomials P_0..P_12 are produced by one pass of
+//    the three-term recurrence instead of seven separate ones.
+
+#define WATSON_DISO 0.003
+#define WATSON_DPAR 0.0017
+
+// ---------------------------------------------------------------------------
+// Protocol-derived values (double, once per protocol).
+//   d[0]   = exp(-b Diso)
+//   d[1+l] = 0.5 sqrt((4l+1)/(4 pi)) * LGI_l(b Dpar),  l = 0..6,
+// with LGI_l(x) = int_{-1}^{1} P_2l(t) exp(-x t^2) dt.
+#define CDM_DERIVED_CFP 8
+
+__host__ __device__ inline void watson_lgi(double x, double* L) {
+  if (x > 0.05) {
+    // I_n = int_{-1}^{1} t^2n exp(-x t^2) dt by upward recurrence from
+    // I_0 = sqrt(pi) erf(sqrt x)/sqrt x. CUDIMOT takes erf in single
+    // precision here (LegendreFunctions.h:12); the recurrence and the
+    // Legendre combinations below amplify its 1e-7 error, and single-
+    // precision erf differs between math libraries (host vs device), so the
+    // double erf is used: these values are computed once per protocol.
+    double I[7];
+    const double sx = sqrt(x);
+    I[0] = 1.7724538509055160273 * erf(sx) / sx;
+    const double emx = -exp(-x);
+    for (int n = 1; n < 7; n++) I[n] = (emx + (n - 0.5) * I[n - 1]) / x;
+    // Coefficients of P_2l(t) in powers of t^2 (Legendre polynomials).
+    L[0] = I[0];
+    L[1] = (-I[0] + 3.0 * I[1]) / 2.0;
+    L[2] = (3.0 * I[0] - 30.0 * I[1] + 35.0 * I[2]) / 8.0;
+    L[3] = (-5.0 * I[0] + 105.0 * I[1] - 315.0 * I[2] + 231.0 * I[3]) / 16.0;
+    L[4] = (35.0 * I[0] - 1260.0 * I[1] + 6930.0 * I[2] - 12012.0 * I[3] + 6435.0 * I[4]) / 128.0;
+    L[5] = (-63.0 * I[0] + 3465.0 * I[1] - 30030.0 * I[2] + 90090.0 * I[3] - 109395.0 * I[4] +
+            46189.0 * I[5]) / 256.0;
+    L[6] = (231.0 * I[0] - 18018.0 * I[1] + 225225.0 * I[2] - 1021020.0 * I[3] +
+            2078505.0 * I[4] - 1939938.0 * I[5] + 676039.0 * I[6]) / 1024.0;
+  } else {
+    // Taylor series in x (LegendreFunctions.h:231-253).
+    const double x2 = x * x, x3 = x2 * x, x4 = x3 * x, x5 = x4 * x, x6 = x5 * x;
+    L[0] = 2.0 - 2.0 * x / 3.0 + x2 / 5.0 - x3 / 21.0 + x4 / 108.0;
+    L[1] = -4.0 * x / 15.0 + 4.0 * x2 / 35.0 - 2.0 * x3 / 63.0 + 2.0 * x4 / 297.0;
+    L[2] = 8.0 * x2 / 315.0 - 8.0 * x3 / 693.0 + 4.0 * x4 / 1287.0;
+    L[3] = -16.0 * x3 / 9009.0 + 16.0 * x4 / 19305.0;
+    L[4] = 32.0 * x4 / 328185.0;
+    L[5] = -64.0 * x5 / 14549535.0;
+    L[6] = 128.0 * x6 / 760543875.0;
+  }
+}
+
+template <typename T>
+__host__ __device__ inline void Derived_CFP(const T* cfp, T* d) {
+  const double b = (double)cfp[3];
+  d[0] = (T)exp(-b * WATSON_DISO);
+  double L[7];
+  watson_lgi(b * WATSON_DPAR, L);
+  for (int l = 0; l < 7; l++) d[1 + l] = (T)(0.14104739588693907 * sqrt(4.0 * l + 1.0) * L[l]);
+}
+
+// ---------------------------------------------------------------------------
+// Parameter-derived values (once per parameter change), stored after the
+// NPARAMS model parameters:
+//   P[5..7]   orientation vector (sin th cos ph, sin th sin ph, cos th)
+//   P[8]      perpendicular equivalent diffusivity dPerp_eq
+//   P[9]      dPar_eq - dPerp_eq
+//   P[10..15] SH coefficients c_1..c_6 of the Watson density (c_0 = 2 sqrt pi)
+//   P[16..18] cos th cos ph, cos th sin ph, sin th (orientation derivatives)
+//   P[19]     d<P_2>/dkappa
+//   P[20..25] dc_1/dkappa .. dc_6/dkappa
+#define CDM_DERIVED_P 21
+
+// Dawson's integral by Rybicki's sampling-theorem method (Numerical
+// Recipes 6.10; WatsonFunctions.h:13-51): h = 0.4, six terms, series for
+// |x| < 0.2. Only used for kappa > 30, where the results do not cancel.
+MACRO T watson_dawson(T x) {
+  const T ax = fabs_gpu(x);
+  if (ax < (T)0.2) {
+    const T x2 = x * x;
+    return x * ((T)1.0 - (T)(2.0 / 3.0) * x2 * ((T)1.0 - (T)0.4 * x2 * ((T)1.0 - (T)(2.0 / 7.0) * x2)));
+  }
+  // exp(-((2i+1) h)^2), i = 0..5
+  const double cw[6] = {0.8521437889662113, 0.23692775868212165, 0.01831563888873418,
+                        0.0003936690406550776, 2.352575200009771e-06, 3.90893843426485e-09};
+  const int n0 = 2 * (int)((T)0.5 * ax / (T)0.4 + (T)0.5);
+  const T xp = ax - (T)n0 * (T)0.4;
+  T e1 = exp_gpu((T)0.8 * xp);
+  const T e2 = e1 * e1;
+  T d1 = (T)(n0 + 1);
+  T d2 = d1 - (T)2.0;
+  T sum = (T)0.0;
+  for (int i = 0; i < 6; i++) {
+    sum += (T)cw[i] * (e1 / d1 + (T)1.0 / (d2 * e1));
+    d1 += (T)2.0;
+    d2 -= (T)2.0;
+    e1 *= e2;
+  }
+  const T r = (T)0.56418958354775628695 * exp_gpu(-xp * xp) * sum;
+  return x < (T)0.0 ? -r : r;
+}
+
+// Watson moments <P_2l>_kappa, l = 1..7, for the density exp(kappa t^2):
+// Lambda_n = int P_n(t) exp(kappa t^2) dt obeys (integration by parts with
+// (2n+1) P_n = P'_{n+1} - P'_{n-1})
+//   Lambda_{n-2} = (A_n/(2 kappa) - B_n) Lambda_n + C_n Lambda_{n+2},
+//   A_n = (2n-1)(2n+1)/(n-1), B_n = (2n+1)/((n-1)(2n+3)),
+//   C_n = (2n-1)(n+2)/((n-1)(2n+3)).
+// Lambda_n is the minimal solution, so the recurrence is run downwards from
+// Lambda_{N+2} = 0 (Miller's algorithm) and normalised by Lambda_0. N is
+// large enough that <P_N> is below 1e-9 for the kappa range it is used in.
+template <int N, typename T>
+__device__ inline void watson_miller(T kappa, T* mom) {
+  const T inv2k = (T)0.5 / kappa;
+  T hi = (T)0.0, cur = (T)1e-30;
+#pragma unroll
+  for (int n = N; n >= 2; n -= 2) {
+    if (n <= 14) mom[n / 2] = cur;
+    const double A = (double)((2 * n - 1) * (2 * n + 1)) / (double)(n - 1);
+    const double B = (double)(2 * n + 1) / (double)((n - 1) * (2 * n + 3));
+    const double C = (double)((2 * n - 1) * (n + 2)) / (double)((n - 1) * (2 * n + 3));
+    const T lo = ((T)A * inv2k - (T)B) * cur + (T)C * hi;
+    hi = cur;
+    cur = lo;
+  }
+  const T inv0 = (T)1.0 / cur;
+  mom[0] = (T)1.0;
+#pragma unroll
+  for (int l = 1; l <= 7; l++) mom[l] *= inv0;
+}
+
+// d<P_n>/dkappa = <t^2 P_n> - <t^2><P_n> with
+// t^2 P_n = a_n P_{n+2} + b_n P_n + g_n P_{n-2} (two uses of the Legendre
+// recurrence t P_n = ((n+1) P_{n+1} + n P_{n-1})/(2n+1)).
+MACRO T watson_dmoment(int l, const T* mom, T t2) {
+  const double n = 2.0 * l;
+  const double a = (n + 1) * (n + 2) / ((2 * n + 1) * (2 * n + 3));
+  const double b = (n + 1) * (n + 1) / ((2 * n + 1) * (2 * n + 3)) + n * n / ((2 * n + 1) * (2 * n - 1));
+  const double g = n * (n - 1) / ((2 * n + 1) * (2 * n - 1));
+  return (T)a * mom[l + 1] + ((T)b - t2) * mom[l] + (T)g * mom[l - 1];
+}
+
+// SH coefficients c_1..c_6 (c[1..6]), <P_2> for the hindered tensor, and
+// their kappa derivatives (dc[1..6], dp2).
+MACRO void watson_kappa_terms(T k, T* c, T& p2, T* dc, T& dp2) {
+  // 2 sqrt(pi) sqrt(4l+1)
+  const double norm[7] = {3.5449077018110318, 7.926654595212022, 10.634723105433096,
+                          12.781346485666884, 14.616028887632437, 16.244807875181,
+                          17.724538509055158};
+  if (k > (T)30.0) {
+    // Large-kappa fits in ln(kappa/30) (WatsonFunctions.h:97-111).
+    const double fit[6][7] = {
+        {7.52308, 0.411538, -0.214588, 0.0784091, -0.023981, 0.00731537, -0.0026467},
+        {8.93718, 1.62147, -0.733421, 0.191568, -0.0202906, -0.00779095, 0.00574847},
+        {8.87905, 3.35689, -1.15935, 0.0673053, 0.121857, -0.066642, 0.0180215},
+        {7.84352, 5.03178, -1.0193, -0.426362, 0.328816, -0.0688176, -0.0229398},
+        {6.30113, 6.09914, -0.16088, -1.05578, 0.338069, 0.0937157, -0.106935},
+        {4.65678, 6.30069, 1.13754, -1.38393, -0.0134758, 0.331686, -0.105954}};
+    const T L = log_gpu(k) - log_gpu((T)30.0);
+    const T ik = (T)1.0 / k;
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+      T acc = (T)fit[i][6], dacc = (T)(6.0 * fit[i][6]);
+#pragma unroll
+      for (int j = 5; j >= 0; j--) {
+        acc = acc * L + (T)fit[i][j];
+        if (j >= 1) dacc = dacc * L + (T)(j * fit[i][j]);
+      }
+      c[i + 1] = acc;
+      dc[i + 1] = dacc * ik;
+    }
+    // <t^2> = R1 = (s/D(s) - 1) / (2k), s = sqrt(k), with D' = 1 - 2 s D.
+    const T sk = sqrt_gpu(k);
+    const T D = watson_dawson(sk);
+    const T q = sk / D;
+    const T r1 = (q - (T)1.0) * (T)0.5 * ik;
+    const T dq = (D - sk + (T)2.0 * k * D) / ((T)2.0 * sk * D * D);
+    const T dr1 = (dq * (T)2.0 * k - (T)2.0 * (q - (T)1.0)) * (T)0.25 * ik * ik;
+    p2 = ((T)3.0 * r1 - (T)1.0) * (T)0.5;
+    dp2 = (T)1.5 * dr1;
+    return;
+  }
+  T mom[8];
+  if (k >= (T)1e-5) {
+    if (k > (T)12.0) {
+      watson_miller<52>(k, mom);
+    } else if (k > (T)4.0) {
+      watson_miller<36>(k, mom);
+    } else if (k > (T)1.0) {
+      watson_miller<24>(k, mom);
+    } else {
+      watson_miller<16>(k, mom);
+    }
+    const T t2 = ((T)1.0 + (T)2.0 * mom[1]) * (T)(1.0 / 3.0);
+    p2 = mom[1];
+    dp2 = watson_dmoment(1, mom, t2);
+    if (k > (T)0.4) {
+#pragma unroll
+      for (int l = 1; l <= 6; l++) {
+        c[l] = (T)norm[l] * mom[l];
+        dc[l] = (T)norm[l] * watson_dmoment(l, mom, t2);
+      }
+      return;
+    }
+  } else {
+    // Second-order series (WatsonFunctions.h:62-73).
+    p2 = (T)(2.0 / 15.0) * k + (T)(4.0 / 315.0) * k * k;
+    dp2 = (T)(2.0 / 15.0) + (T)(8.0 / 315.0) * k;
+  }
+  // Small-kappa series (WatsonFunctions.h:173-193) and their derivatives.
+  const T k2 = k * k, k3 = k2 * k, k4 = k3 * k, k5 = k4 * k, k6 = k5 * k;
+  const T r5 = (T)0.79266545952120224, r1 = (T)0.35449077018110318;   // sqrt(pi/5), 0.2 sqrt(pi)
+  const T r13 = (T)0.49159078480905764, r17 = (T)0.42988741044466255; // sqrt(pi/13), sqrt(pi/17)
+  const T c5k = (T)(64.0 * 0.38678062186808244 / 692835.0);           // 64 sqrt(pi/21)/692835
+  const T c6k = (T)(128.0 * 1.7724538509055160273 / 152108775.0);
+  c[1] = ((T)(4.0 / 3.0) * k + (T)(8.0 / 63.0) * k2) * r5;
+  c[2] = ((T)(8.0 / 21.0) * k2 + (T)(32.0 / 693.0) * k3) * r1;
+  c[3] = ((T)(16.0 / 693.0) * k3 + (T)(32.0 / 10395.0) * k4) * r13;
+  c[4] = (T)(32.0 / 19305.0) * k4 * r17;
+  c[5] = c5k * k5;
+  c[6] = c6k * k6;
+  dc[1] = ((T)(4.0 / 3.0) + (T)(16.0 / 63.0) * k) * r5;
+  dc[2] = ((T)(16.0 / 21.0) * k + (T)(96.0 / 693.0) * k2) * r1;
+  dc[3] = ((T)(48.0 / 693.0) * k2 + (T)(128.0 / 10395.0) * k3) * r13;
+  dc[4] = (T)(128.0 / 19305.0) * k3 * r17;
+  dc[5] = (T)5.0 * c5k * k4;
+  dc[6] = (T)6.0 * c6k * k5;
+}
+
+MACRO void Derived_P(T* P, T* FixP) {
+  const T st = sin_gpu(P[3]), ct = cos_gpu(P[3]);
+  const T sp = sin_gpu(P[4]), cp = cos_gpu(P[4]);
+  P[5] = st * cp;
+  P[6] = st * sp;
+  P[7] = ct;
+  P[16] = ct * cp;
+  P[17] = ct * sp;
+  P[18] = st;
+  T c[7], dc[7];
+  T p2, dp2;
+  watson_kappa_terms(P[2], c, p2, dc, dp2);
+  const T dperp = (T)WATSON_DPAR * ((T)1.0 - P[1]);
+  const T dgap = (T)WATSON_DPAR - dperp;
+  P[8] = dperp + dgap * ((T)1.0 - p2) * (T)(1.0 / 3.0);
+  P[9] = dgap * p2;
+  P[19] = dp2;
+#pragma unroll
+  for (int l = 1; l <= 6; l++) {
+    P[9 + l] = c[l];
+    P[19 + l] = dc[l];
+  }
+}
+
+// ---------------------------------------------------------------------------
+MACRO T Predicted_Signal(int npar, T* P, T* CFP, T* FixP) {
+  const T xv = CFP[0] * P[5] + CFP[1] * P[6] + CFP[2] * P[7];
+  const T extra = exp_gpu(-CFP[3] * (P[9] * xv * xv + P[8]));
+  // Legendre P_0..P_12 at the clamped cosine, one upward recurrence,
+  // accumulating the dispersed-stick SH sum on the way.
+  const T x = min_gpu(max_gpu(xv, (T)-1.0), (T)1.0);
+  T pm = (T)1.0, pc = x;
+  T intra = CFP[5] * (T)3.5449077018110318;
+#pragma unroll
+  for (int n = 1; n < 12; n++) {
+    const T pn = ((T)(2 * n + 1) * x * pc - (T)n * pm) * (T)(1.0 / (n + 1));
+    pm = pc;
+    pc = pn;
+    if ((n + 1) % 2 == 0) intra += CFP[5 + (n + 1) / 2] * P[9 + (n + 1) / 2] * pc;
+  }
+  if (intra < (T)0.0) intra = (T)0.5e-3;
+  const T aniso = ((T)1.0 - P[1]) * extra + P[1] * intra;
+  return FixP[0] * (((T)1.0 - P[0]) * aniso + P[0] * CFP[4]);
+}
+
+MACRO bool ConstraintsMCMC(int npar, T* P) { return true; }
+
+// Analytic derivatives (CUDIMOT takes kappa, th, ph numerically,
+// modelfunctions.h:145-155; single-precision central differences are too
+// coarse for LM, so all five are analytic here).
+MACRO void Partial_Derivatives(int npar, T* P, T* CFP, T* FixP, T* derivatives) {
+  const T xv = CFP[0] * P[5] + CFP[1] * P[6] + CFP[2] * P[7];
+  const T extra = exp_gpu(-CFP[3] * (P[9] * xv * xv + P[8]));
+  const T x = min_gpu(max_gpu(xv, (T)-1.0), (T)1.0);
+  const bool inside = (xv > (T)-1.0) && (xv < (T)1.0);
+  // P_n and P'_n (P'_{n+1} = P'_{n-1} + (2n+1) P_n) for n = 0..12.
+  T pm = (T)1.0, pc = x, dpm = (T)0.0, dpc = (T)1.0;
+  T intra = CFP[5] * (T)3.5449077018110318;
+  T dintra_x = (T)0.0, dintra_k = (T)0.0;
+#pragma unroll
+  for (int n = 1; n < 12; n++) {
+    const T pn = ((T)(2 * n + 1) * x * pc - (T)n * pm) * (T)(1.0 / (n + 1));
+    const T dpn = dpm + (T)(2 * n + 1) * pc;
+    pm = pc;
+    pc = pn;
+    dpm = dpc;
+    dpc = dpn;
+    if ((n + 1) % 2 == 0) {
+      const int l = (n + 1) / 2;
+      intra += CFP[5 + l] * P[9 + l] * pc;
+      dintra_x += CFP[5 + l] * P[9 + l] * dpc;
+      dintra_k += CFP[5 + l] * P[19 + l] * pc;
+    }
+  }
+  if (intra < (T)0.0) {
+    intra = (T)0.5e-3;
+    dintra_x = (T)0.0;
+    dintra_k = (T)0.0;
+  }
+  if (!inside) dintra_x = (T)0.0;
+  const T aniso = ((T)1.0 - P[1]) * extra + P[1] * intra;
+  const T s0w = FixP[0] * ((T)1.0 - P[0]);
+  // dE/dxv and dE/dkappa (dPerp_eq' = -dgap/3 dp2, (dPar_eq-dPerp_eq)' = dgap dp2).
+  const T dgap = (T)WATSON_DPAR * P[1];
+  const T dextra_x = extra * (-CFP[3]) * (T)2.0 * P[9] * xv;
+  const T dextra_k = extra * (-CFP[3]) * dgap * P[19] * (xv * xv - (T)(1.0 / 3.0));
+  const T dS_dx = s0w * (((T)1.0 - P[1]) * dextra_x + P[1] * dintra_x);
+  derivatives[0] = FixP[0] * (CFP[4] - aniso);
+  derivatives[1] = s0w * (intra - extra);
+  derivatives[2] = s0w * (((T)1.0 - P[1]) * dextra_k + P[1] * dintra_k);
+  derivatives[3] = dS_dx * (CFP[0] * P[16] + CFP[1] * P[17] - CFP[2] * P[18]);
+  derivatives[4] = dS_dx * (CFP[1] * P[5] - CFP[0] * P[6]);
+}
+
+MACRO void FixConstraintsLM(int npar, T* P) {}
+
+MACRO T custom_priors(int id_p, T* P, int nmeas, T* CFP, T* FixP) { return (T)0.0; }

@@ -1,0 +1,12 @@
+// NODDI-Watson: compile-time sizes in the CUDIMOT plugin layout.
+#ifndef MODEL_H_INCLUDED
+#define MODEL_H_INCLUDED
+typedef double MyType;
+#define NPARAMS 5  // fiso, fintra, kappa, theta, phi
+#define NCFP 2     // gradient direction (3 rows), b-value (1 row)
+#define NFIXP 1    // S0
+struct MODEL {
+  static int CFP_size[NCFP];
+  static int FixP_size[NFIXP];
+};
+#endif

@@ -1,0 +1,31 @@
+"""Shared workload builders for the tests (signals from the CPU oracle)."""
+import numpy as np
+
+from cudimot_gb300 import capi, synth
+from oracle.oracle import Oracle
+
+_ORACLES = {}
+
+
+def oracle(model):
+    if model not in _ORACLES:
+        _ORACLES[model] = Oracle(model)
+    return _ORACLES[model]
+
+
+def watson(nvox, seed=8219, snr=20.0):
+    o = oracle("NODDI_Watson")
+    return synth.noddi_watson(nvox, seed=seed, snr=snr,
+                              signal_fn=lambda t, cfp, s0: o.signal(t, cfp, s0[:, None]))
+
+
+def b1s(nvox, seed=8219):
+    return synth.ball_1_stick(nvox, seed=seed)
+
+
+def angle_deg(th1, ph1, th2, ph2):
+    """Angle between two axes (sign-insensitive), degrees."""
+    v1 = np.stack([np.sin(th1) * np.cos(ph1), np.sin(th1) * np.sin(ph1), np.cos(th1)], -1)
+    v2 = np.stack([np.sin(th2) * np.cos(ph2), np.sin(th2) * np.sin(ph2), np.cos(th2)], -1)
+    c = np.abs(np.sum(v1 * v2, -1)).clip(0, 1)
+    return np.degrees(np.arccos(c))
