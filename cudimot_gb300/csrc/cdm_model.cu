@@ -27,6 +27,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -723,3 +724,135 @@ cdm_status cdm_fit_host(cdm_ctx* c, int nvox, int nmeas, const double* meas, dou
 }
 
 }  // extern "C"
+
+// ============================================================ no-allocation
+// Levenberg-Marquardt for callers that may not allocate device memory.
+//
+// Some hosts cannot let a library call cudaMalloc: a real-time acquisition
+// or reconstruction pipeline that has reserved its whole device memory
+// budget up front, or a framework that owns all device memory through its
+// own pool and hands this library only its input and output buffers.
+// cudaMalloc/cudaFree can also synchronise the whole device, which such
+// hosts must avoid in the middle of a pipeline. cdm_levmar_noalloc takes
+// no context (cdm_create allocates) and keeps its working memory - the
+// staged protocol table, the lane-packed signals and the device error word
+// - in the fixed array below, which every GPU that loads this library holds
+// until the process exits.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 16u << 20;  // 16 MiB
+constexpr size_t kNoAllocHeader = 256;               // device error word
+
+static __device__ __align__(256) unsigned char cdm_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+std::mutex g_noalloc_mutex;
+
+// Device address of the scratch array for the current device. The first
+// call on a device resolves it with cudaGetSymbolAddress while that device
+// is current; later calls reuse the cached address.
+cdm_status noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  CDM_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return cdm_fail(CDM_NOT_SUPPORTED, "device index beyond the no-allocation table");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    CDM_CUDA(cudaGetSymbolAddress(&p, cdm_noalloc_scratch));
+    g_noalloc_ptr[dev] = (unsigned char*)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return CDM_OK;
+}
+
+template <int G>
+cdm_status noalloc_lm_launch(const cdm_model_cfg* cfg, unsigned char* scratch, int nvox, int nmeas,
+                             const double* meas, double* params, const double* CFP,
+                             const double* FixP, cudaStream_t st) {
+  const int pad = round_up(nmeas, 32);
+  const int nchunk = (nmeas + G - 1) / G;
+  const size_t pbytes = proto_bytes(pad);
+  const size_t sbytes = (size_t)nchunk * nvox * G * sizeof(float);
+  const size_t soff = kNoAllocHeader + (pbytes + 255) / 256 * 256;
+  if (soff + sbytes > kNoAllocScratchBytes)
+    return cdm_fail(CDM_BAD_ARG,
+                    "cdm_levmar_noalloc: " + std::to_string(nvox) + " voxels x " +
+                        std::to_string(nmeas) + " measurements need " +
+                        std::to_string(soff + sbytes) + " bytes of scratch; the fixed scratch holds " +
+                        std::to_string(kNoAllocScratchBytes) + " bytes (split the voxels into parts)");
+  int* err = (int*)scratch;
+  float* proto = (float*)(scratch + kNoAllocHeader);
+  float* sig = (float*)(scratch + soff);
+  // The error word accumulates with atomicOr and must start at zero; the
+  // protocol table and the signals are fully rewritten by every call.
+  CDM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+  cdm_prep_protocol_kernel<<<(pad + 127) / 128, 128, 0, st>>>(CFP, nmeas, pad, proto, nullptr);
+  CDM_CUDA(cudaGetLastError());
+  if (nvox == 0) return CDM_OK;
+  int dev = 0, sms = 0;
+  CDM_CUDA(cudaGetDevice(&dev));
+  CDM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const size_t total = (size_t)nchunk * nvox * G;
+  cdm_pack_signals_kernel<G><<<(int)std::min<size_t>((total + 255) / 256, (size_t)std::max(sms, 1) * 32),
+                               256, 0, st>>>(meas, nvox, nmeas, nchunk, sig);
+  CDM_CUDA(cudaGetLastError());
+  cdm_lm_args a;
+  a.nvox = nvox;
+  a.nmeas = nmeas;
+  a.nmeas_pad = pad;
+  a.nchunk = nchunk;
+  a.fixp_tsize = CDM_FIXP_TSIZE;
+  a.proto_bytes = (uint32_t)pbytes;
+  a.proto = proto;
+  a.sig = sig;
+  a.params = params;
+  a.fixp = FixP;
+  a.max_iters = cfg->iter_levmar;
+  a.marquardt = cfg->marquardt;
+  a.err = err;
+  a.iter_count = nullptr;
+  a.succ_count = nullptr;
+  for (int p = 0; p < kNP; p++) {
+    a.lim.btype[p] = cfg->bound_types[p];
+    a.lim.bmin[p] = (float)cfg->bounds_min[p];
+    a.lim.bmax[p] = (float)cfg->bounds_max[p];
+    a.lim.ptype[p] = cfg->prior_types[p];
+    a.lim.pa[p] = (float)cfg->priors_a[p];
+    a.lim.pb[p] = (float)cfg->priors_b[p];
+    a.lim.fixed[p] = cfg->fixed[p];
+  }
+  CDM_TRY(set_smem(cdm_levmar_kernel<G>, pbytes));
+  cdm_levmar_kernel<G><<<blocks_for(nvox, G), CDM_NT, pbytes, st>>>(a);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+}  // namespace
+
+extern "C" cdm_status cdm_levmar_noalloc(const cdm_model_cfg* cfg, int nvox, int nmeas,
+                                         int CFP_size, int FixP_size, const double* meas,
+                                         double* params, const double* CFP, const double* FixP,
+                                         void* stream) {
+  if (!cfg) return cdm_fail(CDM_BAD_ARG, "null cfg");
+  if (cfg->nparams != NPARAMS) return cdm_fail(CDM_BAD_ARG, "cfg.nparams != model NPARAMS");
+  CDM_TRY(cdm_validate_cfg(cfg, NPARAMS));
+  if (nvox < 0 || nmeas <= 0) return cdm_fail(CDM_BAD_ARG, "nvox must be >= 0 and nmeas > 0");
+  if (CFP_size != CDM_CFP_TSIZE || FixP_size != CDM_FIXP_TSIZE)
+    return cdm_fail(CDM_BAD_ARG, "CFP_size/FixP_size do not match the model");
+  if (proto_bytes(round_up(nmeas, 32)) > 48 * 1024)
+    return cdm_fail(CDM_BAD_ARG, "cdm_levmar_noalloc: protocol larger than 48 KB of shared memory");
+  unsigned char* scratch = nullptr;
+  CDM_TRY(noalloc_scratch(&scratch));
+  int G = cfg->lanes_levmar;
+  if (G == 0) G = 8;
+  cudaStream_t st = (cudaStream_t)stream;
+  switch (G) {
+    case 4: return noalloc_lm_launch<4>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
+    case 8: return noalloc_lm_launch<8>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
+    case 16: return noalloc_lm_launch<16>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
+    case 32: return noalloc_lm_launch<32>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
+  }
+  return cdm_fail(CDM_BAD_ARG, "lanes_levmar must be 0, 4, 8, 16 or 32");
+}

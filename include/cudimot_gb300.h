@@ -200,6 +200,24 @@ cdm_status cdm_fit_host(cdm_ctx* ctx, int nvox, int nmeas, const double* meas,
 cdm_status cdm_synchronize(cdm_ctx* ctx, void* stream, int64_t timeout_ms);
 cdm_status cdm_get_stats(cdm_ctx* ctx, cdm_stats* stats);
 
+/* Levenberg-Marquardt that allocates no device memory. No counterpart in
+ * CUDIMOT: it serves hosts that may not call cudaMalloc from inside this
+ * library (a pipeline that reserved its device memory up front, or a
+ * framework that owns all device memory through its own pool), since
+ * allocation can fail under such budgets and can synchronise the device.
+ * Same arguments and results as cdm_levmar, but no context: the fit
+ * options come from cfg, and the working memory (protocol table, packed
+ * signals, error word) is a fixed 16 MiB array in the library that every
+ * GPU loading it holds until exit. Calls needing more than 16 MiB
+ * (about nvox * nmeas * 4 bytes plus the protocol) return CDM_BAD_ARG;
+ * split the voxels into parts. The first call on a device looks up the
+ * array's device address (make it before any stream capture). All calls
+ * share the array: calls that overlap on the GPU (different streams, or
+ * different host threads) race and must be serialised by the caller. */
+cdm_status cdm_levmar_noalloc(const cdm_model_cfg* cfg, int nvox, int nmeas, int CFP_size,
+                              int FixP_size, const double* meas, double* params,
+                              const double* CFP, const double* FixP, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
