@@ -272,4 +272,19 @@ int orc_predicted(int prec, int nvox, int nmeas, int nsamples, const double* sam
 
 int orc_max_threads(void) { return omp_get_max_threads(); }
 
+// Philox4x32-10 block (known-answer tests) and the MCMC draw built on it.
+void orc_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
+  cdm_u32x4 c = {ctr[0], ctr[1], ctr[2], ctr[3]};
+  const cdm_u32x4 r = cdm_philox4x32_10(c, key[0], key[1]);
+  out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = r.w;
+}
+
+void orc_mcmc_draws(uint64_t seed, uint32_t voxel, uint32_t n, float* normal, float* uniform) {
+  for (uint32_t i = 0; i < n; i++) {
+    const cdm_draw d = cdm_mcmc_draw(seed, voxel, i, 0, 0);
+    normal[i] = d.normal;
+    uniform[i] = d.uniform;
+  }
+}
+
 }  // extern "C"

@@ -1,0 +1,83 @@
+"""The CPU oracle (with this repository's plugins) against the golden
+fixtures produced by CUDIMOT's own plugins (tests/golden/make_golden.py).
+
+Ball_1_Stick: the restated plugin is CUDIMOT's formula for formula, so the
+signal matches exactly and the LM fit to rounding.
+NODDI_Watson: CUDIMOT's FP64 plugin loses precision in two places (its
+Dawson-based closed-form SH coefficients for 0.4 < kappa < ~1.5, and the
+single-precision erf in its Legendre-Gaussian integrals at b = 1000); the
+fixtures also hold a quadrature evaluation of the same model. The oracle must
+match the quadrature values everywhere (2e-7 S0) and CUDIMOT's values outside
+those two zones (2e-6 S0).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from cudimot_gb300 import capi
+from tests.helpers import angle_deg, oracle
+
+G = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(G, name))
+
+
+def test_ball_1_stick_signal_and_jacobian_match_reference_plugin(built):
+    g = load("plugin_Ball_1_Stick.npz")
+    S, J = oracle("Ball_1_Stick").signal(g["params"], g["cfp"], g["fixp"], jac=True)
+    assert np.array_equal(S, g["signal"])
+    np.testing.assert_allclose(J, g["jacobian"], rtol=1e-12, atol=1e-12 * np.abs(g["jacobian"]).max())
+
+
+def test_watson_signal_matches_quadrature_everywhere(built):
+    g = load("plugin_NODDI_Watson.npz")
+    S = oracle("NODDI_Watson").signal(g["params"], g["cfp"], g["fixp"])
+    assert np.max(np.abs(S - g["signal_exact"]) / g["fixp"]) < 2e-7
+
+
+def test_watson_signal_matches_reference_plugin_where_it_is_accurate(built):
+    g = load("plugin_NODDI_Watson.npz")
+    S = oracle("NODDI_Watson").signal(g["params"], g["cfp"], g["fixp"])
+    k = g["params"][:, 2]
+    b = g["cfp"][:, 3]
+    zone = ((k <= 0.4) | (k >= 1.5))[:, None] & (b != 1000)[None, :]
+    d = np.abs(S - g["signal"]) / g["fixp"]
+    assert d[zone].max() < 2e-6
+    # where it differs, CUDIMOT's value is the one away from the exact model
+    ref_err = np.abs(g["signal"] - g["signal_exact"]) / g["fixp"]
+    assert np.all(d[~zone] <= ref_err[~zone] + 2e-7)
+
+
+def test_watson_jacobian_matches_reference_for_analytic_columns(built):
+    g = load("plugin_NODDI_Watson.npz")
+    _, J = oracle("NODDI_Watson").signal(g["params"], g["cfp"], g["fixp"], jac=True)
+    k = g["params"][:, 2]
+    zone = ((k <= 0.4) | (k >= 1.5))[:, None] & (g["cfp"][:, 3] != 1000)[None, :]
+    for p in (0, 1):  # CUDIMOT's analytic fiso / fintra derivatives
+        d = np.abs(J[..., p] - g["jacobian"][..., p]) / g["fixp"]
+        assert d[zone].max() < 2e-6
+
+
+def test_ball_1_stick_levmar_matches_reference_plugin_fit(built):
+    f = load("fit_Ball_1_Stick.npz")
+    cfg = capi.model_cfg("Ball_1_Stick")
+    o = oracle("Ball_1_Stick")
+    p, it, _, co = o.levmar(cfg, f["meas"], f["init"], f["cfp"], f["fixp"])
+    np.testing.assert_allclose(co, f["lm_cost"], rtol=1e-9)
+    assert np.all(angle_deg(p[:, 3], p[:, 4], f["lm"][:, 3], f["lm"][:, 4]) < 1e-4)
+
+
+def test_watson_gridsearch_and_levmar_match_reference_plugin_fit(built):
+    f = load("fit_NODDI_Watson.npz")
+    from cudimot_gb300 import synth
+    cfg = capi.model_cfg("NODDI_Watson", grid=synth.WATSON_GRID)
+    o = oracle("NODDI_Watson")
+    gs, best, _ = o.gridsearch(cfg, f["meas"], f["init"], f["cfp"], f["fixp"])
+    assert np.mean(best == f["gs_best"]) >= 0.95
+    lm, _, _, co = o.levmar(cfg, f["meas"], f["gs"], f["cfp"], f["fixp"])
+    # same start, models differ only by CUDIMOT's precision loss
+    rel = (co - f["lm_cost"]) / f["lm_cost"]
+    assert np.median(np.abs(rel)) < 1e-4
