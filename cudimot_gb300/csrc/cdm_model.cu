@@ -126,7 +126,7 @@ cdm_status ensure_base(cdm_ctx* c) {
   return CDM_OK;
 }
 
-size_t proto_bytes(int nmeas_pad) { return (size_t)kNCOLS * nmeas_pad * sizeof(float); }
+size_t proto_bytes(int nmeas_pad) { return (size_t)kNCOLS4 * nmeas_pad * sizeof(float); }
 
 cdm_status check_common(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_size) {
   if (!c) return cdm_fail(CDM_BAD_ARG, "null context");
@@ -146,7 +146,7 @@ cdm_status check_common(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_
 // Protocol tables from CUDIMOT's CFP array (device pointer).
 cdm_status prep_protocol(cdm_ctx* c, int nmeas, const double* CFP, cudaStream_t st) {
   const int pad = round_up(nmeas, 32);
-  CDM_TRY(dev_alloc(&c->proto32, &c->proto32_cap, (size_t)kNCOLS * pad));
+  CDM_TRY(dev_alloc(&c->proto32, &c->proto32_cap, (size_t)kNCOLS4 * pad));
   CDM_TRY(dev_alloc(&c->proto64, &c->proto64_cap, (size_t)kNCOLS * nmeas));
   c->nmeas_pad = pad;
   cdm_prep_protocol_kernel<<<(pad + 127) / 128, 128, 0, st>>>(CFP, nmeas, pad, c->proto32, c->proto64);
@@ -168,12 +168,14 @@ cdm_status pack_signals_g(cdm_ctx* c, int nvox, int nmeas, const double* meas, c
 
 cdm_status pack_signals(cdm_ctx* c, int G, int nvox, int nmeas, const double* meas, cudaStream_t st) {
   switch (G) {
+    case 1: return pack_signals_g<1>(c, nvox, nmeas, meas, st);
+    case 2: return pack_signals_g<2>(c, nvox, nmeas, meas, st);
     case 4: return pack_signals_g<4>(c, nvox, nmeas, meas, st);
     case 8: return pack_signals_g<8>(c, nvox, nmeas, meas, st);
     case 16: return pack_signals_g<16>(c, nvox, nmeas, meas, st);
     case 32: return pack_signals_g<32>(c, nvox, nmeas, meas, st);
   }
-  return cdm_fail(CDM_BAD_ARG, "lanes per voxel must be 4, 8, 16 or 32");
+  return cdm_fail(CDM_BAD_ARG, "lanes per voxel must be 1, 2, 4, 8, 16 or 32");
 }
 
 template <class K>
@@ -182,16 +184,19 @@ cdm_status set_smem(K kernel, size_t bytes) {
   return CDM_OK;
 }
 
-// Lanes per voxel: explicit choice, else a shape-based default. Every lane
-// of a group redoes the parameter-only work, so fewer lanes are better while
-// there are enough voxels to fill the GPU (>= ~8 resident groups per SM
-// slot); with few voxels, more lanes share each voxel.
-int pick_lanes(const cdm_ctx* c, int requested, int nvox, int nmeas) {
-  if (requested == 4 || requested == 8 || requested == 16 || requested == 32) return requested;
-  const long slots = (long)std::max(c->num_sms, 1) * 1024;  // resident threads of interest
-  int g = 8;
-  while (g < 32 && (long)nvox * g < 2 * slots) g *= 2;
-  if (nmeas < 2 * g && g > 4) g = std::max(4, g / 2);
+// Lanes per voxel: explicit choice, else a per-stage default measured on
+// GB300 for a 200k-voxel, 288-measurement NODDI-Watson fit (MCMC and LM: 4,
+// grid search: 8). Each lane repeats the parameter-only work and takes part
+// in the group reductions, so few lanes are best while there are enough
+// voxels to fill the GPU; with fewer voxels than about four waves of
+// resident threads the group is widened.
+int pick_lanes(const cdm_ctx* c, int requested, int base, int nvox) {
+  if (requested == 1 || requested == 2 || requested == 4 || requested == 8 || requested == 16 ||
+      requested == 32)
+    return requested;
+  const long resident = (long)std::max(c->num_sms, 1) * 512;
+  int g = base;
+  while (g < 32 && (long)nvox * g < 4 * resident) g *= 2;
   return g;
 }
 
@@ -238,7 +243,7 @@ cdm_status run_gridsearch(cdm_ctx* c, int nvox, int nmeas, const double* meas, d
                           const double* CFP, const double* FixP, cudaStream_t st) {
   if (c->cfg.grid_combs <= 0 || c->cfg.n_grid_params <= 0) return CDM_OK;
   CDM_TRY(prep_protocol(c, nmeas, CFP, st));
-  const int G = pick_lanes(c, c->cfg.lanes_gridsearch, nvox, nmeas);
+  const int G = pick_lanes(c, c->cfg.lanes_gridsearch, 8, nvox);
   CDM_TRY(pack_signals(c, G, nvox, nmeas, meas, st));
   const size_t n = (size_t)std::max(nvox, 1);
   CDM_TRY(dev_alloc(&c->gs_flags, &c->gs_flags_cap, n));
@@ -246,10 +251,13 @@ cdm_status run_gridsearch(cdm_ctx* c, int nvox, int nmeas, const double* meas, d
   CDM_TRY(dev_alloc(&c->gs_best, &c->gs_best_cap, n));
   if (nvox == 0) return CDM_OK;
   switch (G) {
+    case 1: CDM_TRY(launch_gs<1>(c, nvox, nmeas, params, FixP, st)); break;
+    case 2: CDM_TRY(launch_gs<2>(c, nvox, nmeas, params, FixP, st)); break;
     case 4: CDM_TRY(launch_gs<4>(c, nvox, nmeas, params, FixP, st)); break;
     case 8: CDM_TRY(launch_gs<8>(c, nvox, nmeas, params, FixP, st)); break;
     case 16: CDM_TRY(launch_gs<16>(c, nvox, nmeas, params, FixP, st)); break;
-    default: CDM_TRY(launch_gs<32>(c, nvox, nmeas, params, FixP, st)); break;
+    case 32: CDM_TRY(launch_gs<32>(c, nvox, nmeas, params, FixP, st)); break;
+    default: return cdm_fail(CDM_BAD_ARG, "bad lane count");
   }
   cdm_gs_recheck_args r;
   r.nvox = nvox;
@@ -294,14 +302,17 @@ cdm_status launch_lm(cdm_ctx* c, int nvox, int nmeas, double* params, const doub
 cdm_status run_levmar(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
                       const double* CFP, const double* FixP, cudaStream_t st) {
   CDM_TRY(prep_protocol(c, nmeas, CFP, st));
-  const int G = pick_lanes(c, c->cfg.lanes_levmar, nvox, nmeas);
+  const int G = pick_lanes(c, c->cfg.lanes_levmar, 4, nvox);
   CDM_TRY(pack_signals(c, G, nvox, nmeas, meas, st));
   if (nvox == 0) return CDM_OK;
   switch (G) {
+    case 1: return launch_lm<1>(c, nvox, nmeas, params, FixP, st);
+    case 2: return launch_lm<2>(c, nvox, nmeas, params, FixP, st);
     case 4: return launch_lm<4>(c, nvox, nmeas, params, FixP, st);
     case 8: return launch_lm<8>(c, nvox, nmeas, params, FixP, st);
     case 16: return launch_lm<16>(c, nvox, nmeas, params, FixP, st);
-    default: return launch_lm<32>(c, nvox, nmeas, params, FixP, st);
+    case 32: return launch_lm<32>(c, nvox, nmeas, params, FixP, st);
+    default: return cdm_fail(CDM_BAD_ARG, "bad lane count");
   }
 }
 
@@ -338,7 +349,7 @@ cdm_status run_mcmc(cdm_ctx* c, int nvox, int nmeas, const double* meas, double*
   if (!samples) return cdm_fail(CDM_BAD_ARG, "samples is null");
   if (c->cfg.rician && !tau) return cdm_fail(CDM_BAD_ARG, "rician MCMC needs tau_samples");
   CDM_TRY(prep_protocol(c, nmeas, CFP, st));
-  const int G = pick_lanes(c, c->cfg.lanes_mcmc, nvox, nmeas);
+  const int G = pick_lanes(c, c->cfg.lanes_mcmc, 4, nvox);
   CDM_TRY(pack_signals(c, G, nvox, nmeas, meas, st));
   if (nvox == 0) return CDM_OK;
   const bool ric = c->cfg.rician != 0;
@@ -347,6 +358,8 @@ cdm_status run_mcmc(cdm_ctx* c, int nvox, int nmeas, const double* meas, double*
     return ric ? launch_mcmc<GG, true>(c, nvox, nmeas, params, FixP, samples, tau, voxel_offset, st) \
                : launch_mcmc<GG, false>(c, nvox, nmeas, params, FixP, samples, tau, voxel_offset, st);
   switch (G) {
+    CDM_MCMC_CASE(1)
+    CDM_MCMC_CASE(2)
     CDM_MCMC_CASE(4)
     CDM_MCMC_CASE(8)
     CDM_MCMC_CASE(16)
@@ -421,10 +434,10 @@ cdm_status fit_sequence(cdm_ctx* c, int nvox, int nmeas, const double* meas, dou
 // captured graph contains no allocation.
 cdm_status reserve_fit(cdm_ctx* c, int nvox, int nmeas) {
   const int pad = round_up(nmeas, 32);
-  CDM_TRY(dev_alloc(&c->proto32, &c->proto32_cap, (size_t)kNCOLS * pad));
+  CDM_TRY(dev_alloc(&c->proto32, &c->proto32_cap, (size_t)kNCOLS4 * pad));
   CDM_TRY(dev_alloc(&c->proto64, &c->proto64_cap, (size_t)kNCOLS * nmeas));
   size_t sig = 0;
-  for (int G : {4, 8, 16, 32}) sig = std::max(sig, (size_t)((nmeas + G - 1) / G) * std::max(nvox, 1) * G);
+  for (int G : {1, 2, 4, 8, 16, 32}) sig = std::max(sig, (size_t)((nmeas + G - 1) / G) * std::max(nvox, 1) * G);
   CDM_TRY(dev_alloc(&c->sig, &c->sig_cap, sig));
   const size_t n = (size_t)std::max(nvox, 1);
   CDM_TRY(dev_alloc(&c->gs_flags, &c->gs_flags_cap, n));
@@ -432,6 +445,7 @@ cdm_status reserve_fit(cdm_ctx* c, int nvox, int nmeas) {
   CDM_TRY(dev_alloc(&c->gs_best, &c->gs_best_cap, n));
   // kernel attributes are set outside capture too
   const size_t sm = proto_bytes(pad);
+  CDM_TRY(set_smem(cdm_gridsearch_kernel<1>, sm)); CDM_TRY(set_smem(cdm_gridsearch_kernel<2>, sm));
   CDM_TRY(set_smem(cdm_gridsearch_kernel<4>, sm)); CDM_TRY(set_smem(cdm_gridsearch_kernel<8>, sm));
   CDM_TRY(set_smem(cdm_gridsearch_kernel<16>, sm)); CDM_TRY(set_smem(cdm_gridsearch_kernel<32>, sm));
   return CDM_OK;
@@ -849,10 +863,12 @@ extern "C" cdm_status cdm_levmar_noalloc(const cdm_model_cfg* cfg, int nvox, int
   if (G == 0) G = 8;
   cudaStream_t st = (cudaStream_t)stream;
   switch (G) {
+    case 1: return noalloc_lm_launch<1>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
+    case 2: return noalloc_lm_launch<2>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
     case 4: return noalloc_lm_launch<4>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
     case 8: return noalloc_lm_launch<8>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
     case 16: return noalloc_lm_launch<16>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
     case 32: return noalloc_lm_launch<32>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
   }
-  return cdm_fail(CDM_BAD_ARG, "lanes_levmar must be 0, 4, 8, 16 or 32");
+  return cdm_fail(CDM_BAD_ARG, "lanes_levmar must be 0, 1, 2, 4, 8, 16 or 32");
 }

@@ -71,13 +71,16 @@ template <> struct cdm_math_result<cnt, cnt> { typedef cnt type; };
 
 constexpr int kNCOLS = CDM_CFP_TSIZE + CDM_NDCFP;
 
-// out[0] = FLOPs of Derived_P per call, out[1] = FLOPs of Predicted_Signal
-// per measurement, out[2] = FLOPs of Partial_Derivatives per measurement;
-// out[3..5] the same for transcendental/sqrt calls. Averaged over the nvox
-// parameter vectors and nmeas measurements given.
+// out[0] = FLOPs of Derived_P from scratch, out[1] = FLOPs of
+// Predicted_Signal per measurement, out[2] = FLOPs of Partial_Derivatives per
+// measurement; out[3..5] the same for transcendental/sqrt calls; out[6]/[7]
+// FLOPs/transcendentals of Derived_P after a change of one parameter (the
+// sampler's case; plugins may reuse cached parameter-only blocks), averaged
+// over the parameters. Averaged over the nvox parameter vectors and nmeas
+// measurements given.
 extern "C" int cdm_count_ops(int nvox, const double* params, int nmeas, const double* cfp,
                              const double* fixp, double* out) {
-  int64_t fd = 0, fs = 0, fj = 0, md = 0, ms = 0, mj = 0;
+  int64_t fd = 0, fs = 0, fj = 0, md = 0, ms = 0, mj = 0, fw = 0, mw = 0;
   for (int v = 0; v < nvox; v++) {
     cnt P[CDM_PSTORE], F[CDM_FIXP_TSIZE + 1], d[NPARAMS];
     for (int i = 0; i < CDM_PSTORE; i++) P[i] = i < NPARAMS ? params[(size_t)v * NPARAMS + i] : 0.0;
@@ -86,6 +89,16 @@ extern "C" int cdm_count_ops(int nvox, const double* params, int nmeas, const do
     cdm_update_derived(P, F);
     fd += g_flops;
     md += g_mufu;
+    for (int p = 0; p < NPARAMS; p++) {
+      const cnt keep = P[p];
+      P[p] = P[p].v * (1.0 + 1e-3) + 1e-6;
+      g_flops = g_mufu = 0;
+      cdm_update_derived(P, F);
+      fw += g_flops;
+      mw += g_mufu;
+      P[p] = keep;
+      cdm_update_derived(P, F);
+    }
     for (int m = 0; m < nmeas; m++) {
       double raw[kNCOLS];
       for (int k = 0; k < CDM_CFP_TSIZE; k++) raw[k] = cfp[(size_t)m * CDM_CFP_TSIZE + k];
@@ -111,5 +124,7 @@ extern "C" int cdm_count_ops(int nvox, const double* params, int nmeas, const do
   out[3] = md / nv;
   out[4] = ms / nm;
   out[5] = mj / nm;
+  out[6] = fw / (nv * NPARAMS);
+  out[7] = mw / (nv * NPARAMS);
   return 0;
 }

@@ -66,8 +66,8 @@ cdm_status cdm_validate_cfg(const cdm_model_cfg* c, int nparams) {
     if (c->nburn < 0) return cdm_fail(CDM_BAD_ARG, "nburn < 0");
   }
   for (int l : {c->lanes_gridsearch, c->lanes_levmar, c->lanes_mcmc})
-    if (!(l == 0 || l == 4 || l == 8 || l == 16 || l == 32))
-      return cdm_fail(CDM_BAD_ARG, "lanes per voxel must be 0, 4, 8, 16 or 32");
+    if (!(l == 0 || l == 1 || l == 2 || l == 4 || l == 8 || l == 16 || l == 32))
+      return cdm_fail(CDM_BAD_ARG, "lanes per voxel must be 0, 1, 2, 4, 8, 16 or 32");
   return CDM_OK;
 }
 

@@ -6,13 +6,14 @@
 // (CDM_CFP_TSIZE, CDM_FIXP_TSIZE).
 //
 // Work decomposition: a voxel is processed by a group of G consecutive lanes
-// of one warp (G in {4, 8, 16, 32}); lane j of the group takes measurements
+// of one warp (G in {1, 2, 4, 8, 16, 32}); lane j of the group takes measurements
 // j, j+G, j+2G, ... Group sums are butterfly (xor) shuffles, which leave the
 // identical value in every lane, so every lane of a group takes the same
 // decisions without a broadcast. Several groups share a warp when G < 32.
 //
 // HBM layouts the kernels read (built by cdm_pack_* kernels):
-//   protocol  float [NCOLS][nmeas_pad]   NCOLS = CFP_Tsize + derived CFP
+//   protocol  float [nmeas_pad][NCOLS4]  NCOLS = CFP_Tsize + derived CFP,
+//                                        rows padded to NCOLS4 (16 bytes)
 //   signals   float [nchunk][nvox][G]    chunk c holds measurements cG..cG+G-1
 // so a warp's signal load is one contiguous 128-byte line.
 #pragma once
@@ -23,10 +24,15 @@
 #ifndef CDM_NT
 #define CDM_NT 128  // threads per CTA
 #endif
+#ifndef CDM_SSE_UNROLL
+#define CDM_SSE_UNROLL 1  // measurement-loop unroll of the cost sums
+#endif
 
+constexpr int kSseUnroll = CDM_SSE_UNROLL;
 constexpr int kNP = NPARAMS;
 constexpr int kNPS = CDM_PSTORE;
 constexpr int kNCOLS = CDM_CFP_TSIZE + CDM_NDCFP;
+constexpr int kNCOLS4 = (kNCOLS + 3) / 4 * 4;  // protocol row stride (floats)
 constexpr int kNFIX = CDM_FIXP_TSIZE > 0 ? CDM_FIXP_TSIZE : 1;
 
 // Error codes written to the device error word.
@@ -47,6 +53,7 @@ struct cdm_limits {
 template <int G>
 __device__ __forceinline__ unsigned cdm_group_mask() {
   if (G == 32) return 0xFFFFFFFFu;
+  if (G == 1) return 1u << (threadIdx.x & 31u);
   const unsigned lane = threadIdx.x & 31u;
   return ((1u << G) - 1u) << (lane & ~(unsigned)(G - 1));
 }
@@ -105,10 +112,20 @@ __device__ __forceinline__ bool cdm_stage_protocol(const float* __restrict__ gsr
 }
 
 // Load one measurement's protocol values (raw CFP then derived) from the
-// staged table into a register array the plugin can index.
+// staged table into a register array the plugin can index: one 16-byte
+// shared-memory load per four values. The G lanes of a group read G
+// consecutive rows (distinct banks for 48-byte rows); other groups of the
+// warp read the same rows (broadcast).
 __device__ __forceinline__ void cdm_load_cfp(const float* sproto, int nmeas_pad, int m, fp32* cf) {
+  const float4* row = reinterpret_cast<const float4*>(sproto + (size_t)m * kNCOLS4);
 #pragma unroll
-  for (int k = 0; k < kNCOLS; k++) cf[k] = fp32(sproto[k * nmeas_pad + m]);
+  for (int q = 0; q < kNCOLS4 / 4; q++) {
+    const float4 v = row[q];
+    if (4 * q + 0 < kNCOLS) cf[4 * q + 0] = fp32(v.x);
+    if (4 * q + 1 < kNCOLS) cf[4 * q + 1] = fp32(v.y);
+    if (4 * q + 2 < kNCOLS) cf[4 * q + 2] = fp32(v.z);
+    if (4 * q + 3 < kNCOLS) cf[4 * q + 3] = fp32(v.w);
+  }
 }
 
 // Per-voxel view handed to the group cost routines.
@@ -127,6 +144,7 @@ template <int G>
 __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const float* sproto,
                                                 fp32* P, fp32* FixP, unsigned gmask) {
   float acc = 0.0f;
+#pragma unroll kSseUnroll
   for (int c = 0; c < io.nchunk; c++) {
     const int m = c * G + io.lane;
     const bool valid = m < io.nmeas;

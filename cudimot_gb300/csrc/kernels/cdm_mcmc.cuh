@@ -41,9 +41,13 @@ struct cdm_mcmc_args {
   cdm_limits lim;
 };
 
-__device__ __forceinline__ float cdm_prior(const cdm_limits& L, int p, fp32* P, int nmeas,
+template <int N>
+__device__ __forceinline__ float cdm_prior(const cdm_limits& L, int p, fp32 (&P)[N], int nmeas,
                                            fp32* cfp_all, fp32* FixP) {
-  const float x = (float)P[p];
+  fp32 xv = P[0];
+#pragma unroll
+  for (int k = 1; k < N; k++) xv = (k == p) ? P[k] : xv;
+  const float x = (float)xv;
   switch (L.ptype[p]) {
     case GAUSSPRIOR: {
       const float d = x - L.pa[p];
@@ -62,13 +66,34 @@ __device__ __forceinline__ float cdm_prior(const cdm_limits& L, int p, fp32* P, 
   }
 }
 
-__device__ __forceinline__ bool cdm_in_bounds(const cdm_limits& L, int p, fp32* P) {
+template <int N>
+__device__ __forceinline__ bool cdm_in_bounds(const cdm_limits& L, int p, fp32 (&P)[N]) {
   if (!ConstraintsMCMC(NPARAMS, P)) return false;
-  const float x = (float)P[p];
+  fp32 xv = P[0];
+#pragma unroll
+  for (int k = 1; k < N; k++) xv = (k == p) ? P[k] : xv;
+  const float x = (float)xv;
   if (L.btype[p] == BMIN) return !(x < L.bmin[p]);
   if (L.btype[p] == BMAX) return !(x > L.bmax[p]);
   if (L.btype[p] == BMINMAX) return !(x < L.bmin[p]) && !(x > L.bmax[p]);
   return true;
+}
+
+// Register arrays indexed by a runtime parameter id: the proposal loop over
+// parameters is kept rolled (one copy of the inlined likelihood in the
+// instruction cache instead of NPARAMS), and these unrolled selects keep
+// the arrays in registers.
+template <class V, int N>
+__device__ __forceinline__ V cdm_get(const V (&a)[N], int i) {
+  V v = a[0];
+#pragma unroll
+  for (int k = 1; k < N; k++) v = (k == i) ? a[k] : v;
+  return v;
+}
+template <class V, int N>
+__device__ __forceinline__ void cdm_set(V (&a)[N], int i, V x) {
+#pragma unroll
+  for (int k = 0; k < N; k++) a[k] = (k == i) ? x : a[k];
 }
 
 template <int G, bool RICIAN>
@@ -79,11 +104,16 @@ __device__ __forceinline__ double cdm_likelihood(const cdm_voxel_io& io, const f
     return -(double)io.nmeas * (double)logf(tau) - s;
   }
   const double sse = cdm_group_sse<G>(io, sproto, P, FixP, gmask);
-  return 0.5 * (double)io.nmeas * (double)logf((float)(sse * 0.5));
+  return (double)(0.5f * (float)io.nmeas * logf(0.5f * (float)sse));
 }
 
+// Minimum resident CTAs per SM requested from the register allocator.
+#ifndef CDM_MCMC_MIN_BLOCKS
+#define CDM_MCMC_MIN_BLOCKS 4
+#endif
+
 template <int G, bool RICIAN>
-__global__ void __launch_bounds__(CDM_NT) cdm_mcmc_kernel(const __grid_constant__ cdm_mcmc_args a) {
+__global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(const __grid_constant__ cdm_mcmc_args a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
   const int v = blockIdx.x * (CDM_NT / G) + (int)threadIdx.x / G;
@@ -191,37 +221,39 @@ __global__ void __launch_bounds__(CDM_NT) cdm_mcmc_kernel(const __grid_constant_
           tau = old;
         }
       }
-#pragma unroll
+#pragma unroll 1
       for (int p = 0; p < kNP; p++) {
         if (L.fixed[p]) {
-          acc[p]++;
+          cdm_set(acc, p, cdm_get(acc, p) + 1);
           continue;
         }
         const cdm_draw d = cdm_mcmc_draw(a.seed, vid, git, (uint32_t)p, a.stream);
-        fp32 saved[kNPS];
-#pragma unroll
-        for (int i = 0; i < kNPS; i++) saved[i] = P[i];
-        P[p] = fp32((float)P[p] + d.normal * propSD[p]);
+        const fp32 old = cdm_get(P, p);
+        cdm_set(P, p, fp32((float)old + d.normal * cdm_get(propSD, p)));
+        bool accepted = false;
+        bool derived = false;
         if (cdm_in_bounds(L, p, P)) {
           cdm_update_derived(P, FixP);
+          derived = true;
           const float np_ = cdm_prior(L, p, P, a.nmeas, cf0, FixP);
           float tp = 0.0f;
 #pragma unroll
           for (int q = 0; q < kNP; q++) tp += (q == p) ? np_ : prior[q];
           const double ne = (double)tp + cdm_likelihood<G, RICIAN>(io, sproto, P, FixP, tau, gm);
           if (expf((float)(energy - ne)) > d.uniform) {
-            acc[p]++;
+            accepted = true;
             energy = ne;
-            prior[p] = np_;
-          } else {
-            rej[p]++;
-#pragma unroll
-            for (int i = 0; i < kNPS; i++) P[i] = saved[i];
+            cdm_set(prior, p, np_);
           }
+        }
+        if (accepted) {
+          cdm_set(acc, p, cdm_get(acc, p) + 1);
         } else {
-          rej[p]++;
-#pragma unroll
-          for (int i = 0; i < kNPS; i++) P[i] = saved[i];
+          cdm_set(rej, p, cdm_get(rej, p) + 1);
+          // Derived_P is a function of P: restoring the parameter and
+          // deriving again restores the derived values exactly.
+          cdm_set(P, p, old);
+          if (derived) cdm_update_derived(P, FixP);
         }
       }
       if (recording && (it % a.sampleevery) == 0) {

@@ -100,8 +100,9 @@ __global__ void __launch_bounds__(CDM_NT) cdm_bic_aic_kernel(const __grid_consta
 // ---------------------------------------------------------------------------
 // Layout kernels.
 // Protocol: CUDIMOT's CFP [nmeas][CFP_Tsize] (double) plus the plugin's
-// derived values -> FP32 [NCOLS][nmeas_pad] (padding repeats measurement 0)
-// and FP64 [nmeas][NCOLS] for the grid-search re-check.
+// derived values -> FP32 [nmeas_pad][NCOLS4] (padding rows repeat
+// measurement 0, padding columns are 0) and FP64 [nmeas][NCOLS] for the
+// grid-search re-check.
 __global__ void cdm_prep_protocol_kernel(const double* __restrict__ cfp, int nmeas, int nmeas_pad,
                                          float* __restrict__ p32, double* __restrict__ p64) {
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nmeas_pad; m += gridDim.x * blockDim.x) {
@@ -113,10 +114,10 @@ __global__ void cdm_prep_protocol_kernel(const double* __restrict__ cfp, int nme
     Derived_CFP<double>(row, row + CDM_CFP_TSIZE);
 #endif
 #pragma unroll
-    for (int k = 0; k < kNCOLS; k++) {
-      p32[(size_t)k * nmeas_pad + m] = (float)row[k];
+    for (int k = 0; k < kNCOLS4; k++) p32[(size_t)m * kNCOLS4 + k] = k < kNCOLS ? (float)row[k] : 0.0f;
+#pragma unroll
+    for (int k = 0; k < kNCOLS; k++)
       if (m < nmeas && p64) p64[(size_t)m * kNCOLS + k] = row[k];
-    }
   }
 }
 

@@ -36,7 +36,15 @@ using std::fabs; using std::fmin; using std::fmax; using std::erf;
   FUNC fp32 NAME(fp32 x) { return fp32(FF(x.v)); }
 
 CDM_UNARY(log_gpu, logf, log)
+// Build option CDM_FAST_EXP: fp32 exp through the hardware ex2 approximation
+// (__expf, a few ulp more error) instead of the correctly rounded-ish expf.
+#if defined(CDM_FAST_EXP) && defined(__CUDA_ARCH__)
+FUNC float exp_gpu(float x) { return expf(x); }
+FUNC double exp_gpu(double x) { return exp(x); }
+FUNC fp32 exp_gpu(fp32 x) { return fp32(__expf(x.v)); }
+#else
 CDM_UNARY(exp_gpu, expf, exp)
+#endif
 CDM_UNARY(fabs_gpu, fabsf, fabs)
 CDM_UNARY(sin_gpu, sinf, sin)
 CDM_UNARY(cos_gpu, cosf, cos)

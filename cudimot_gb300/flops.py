@@ -3,8 +3,9 @@ plugin (csrc/host/cdm_flops.cpp).
 
 Work model (per voxel, one parameter proposal = one likelihood):
   likelihood  = Derived_P + nmeas * (Predicted_Signal + 3)   [r=s-y, r*r, +]
-  MCMC        = (nburn + njumps) * free_params * likelihood
-  grid search = combinations * likelihood
+  MCMC        = (nburn + njumps) * free_params * likelihood, with Derived_P
+                counted after a single-parameter change (cached blocks reused)
+  grid search = combinations * likelihood, Derived_P from scratch
 Counts +, -, *, / as one FLOP each; transcendental and square-root calls
 are reported separately (they run on the SFU/MUFU path).
 """
@@ -23,10 +24,11 @@ def count_ops(model, params, cfp, fixp):
     params = np.ascontiguousarray(params, dtype=np.float64)
     cfp = np.ascontiguousarray(cfp, dtype=np.float64)
     fixp = np.ascontiguousarray(fixp, dtype=np.float64)
-    out = np.zeros(6)
+    out = np.zeros(8)
     lib.cdm_count_ops(params.shape[0], params.ctypes.data, cfp.shape[0], cfp.ctypes.data,
                       fixp.ctypes.data, out.ctypes.data)
-    keys = ("derived_p", "signal", "jacobian", "derived_p_mufu", "signal_mufu", "jacobian_mufu")
+    keys = ("derived_p", "signal", "jacobian", "derived_p_mufu", "signal_mufu", "jacobian_mufu",
+            "derived_p_one_param", "derived_p_one_param_mufu")
     return dict(zip(keys, out.tolist()))
 
 
@@ -43,5 +45,6 @@ def watson_c1_flops_per_voxel(nburn=1250, njumps=1250, combs=968, nmeas=288, n=5
     truth, S0 = synth.watson_truth(n, rng)
     ops = count_ops("NODDI_Watson", truth, cfp, S0[:, None])
     like = likelihood_flops(ops, nmeas)
-    return {"ops": ops, "likelihood": like, "mcmc": (nburn + njumps) * 5 * like,
-            "gridsearch": combs * like}
+    like_prop = ops["derived_p_one_param"] + nmeas * (ops["signal"] + 3.0)
+    return {"ops": ops, "likelihood": like, "likelihood_proposal": like_prop,
+            "mcmc": (nburn + njumps) * 5 * like_prop, "gridsearch": combs * like}

@@ -23,8 +23,8 @@
 //    three-term recurrence in the Legendre basis. The closed forms used by
 //    CUDIMOT (WatsonFunctions.h:112-172) cancel terms of size ~1e10 and
 //    are only usable in double; the recurrence is stable in float.
-//  * the seven Legendre polynomials P_0..P_12 are produced by one pass of
-//    the three-term recurrence instead of seven separate ones.
+//  * the seven even Legendre polynomials P_0..P_12 come from one pass of a
+//    recurrence in x^2 instead of seven separate recurrences.
 
 #define WATSON_DISO 0.003
 #define WATSON_DPAR 0.0017
@@ -91,7 +91,13 @@ __host__ __device__ inline void Derived_CFP(const T* cfp, T* d) {
 //   P[16..18] cos th cos ph, cos th sin ph, sin th (orientation derivatives)
 //   P[19]     d<P_2>/dkappa
 //   P[20..25] dc_1/dkappa .. dc_6/dkappa
-#define CDM_DERIVED_P 21
+//   P[26]     <P_2>
+//   P[27..29] kappa, th, ph the cached blocks were computed for
+//   P[30]     1 once the caches hold values (callers zero the derived slots)
+// A sampler changes one parameter per proposal; the kappa block (Miller
+// recurrence) and the trigonometric block are only recomputed when their
+// own inputs changed.
+#define CDM_DERIVED_P 26
 
 // Dawson's integral by Rybicki's sampling-theorem method (Numerical
 // Recipes 6.10; WatsonFunctions.h:13-51): h = 0.4, six terms, series for
@@ -250,44 +256,74 @@ MACRO void watson_kappa_terms(T k, T* c, T& p2, T* dc, T& dp2) {
 }
 
 MACRO void Derived_P(T* P, T* FixP) {
-  const T st = sin_gpu(P[3]), ct = cos_gpu(P[3]);
-  const T sp = sin_gpu(P[4]), cp = cos_gpu(P[4]);
-  P[5] = st * cp;
-  P[6] = st * sp;
-  P[7] = ct;
-  P[16] = ct * cp;
-  P[17] = ct * sp;
-  P[18] = st;
-  T c[7], dc[7];
-  T p2, dp2;
-  watson_kappa_terms(P[2], c, p2, dc, dp2);
+  const bool valid = P[30] != (T)0.0;
+  if (!valid || P[2] != P[27]) {
+    T c[7], dc[7];
+    T p2, dp2;
+    watson_kappa_terms(P[2], c, p2, dc, dp2);
+#pragma unroll
+    for (int l = 1; l <= 6; l++) {
+      P[9 + l] = c[l];
+      P[19 + l] = dc[l];
+    }
+    P[19] = dp2;
+    P[26] = p2;
+    P[27] = P[2];
+  }
+  if (!valid || P[3] != P[28] || P[4] != P[29]) {
+    const T st = sin_gpu(P[3]), ct = cos_gpu(P[3]);
+    const T sp = sin_gpu(P[4]), cp = cos_gpu(P[4]);
+    P[5] = st * cp;
+    P[6] = st * sp;
+    P[7] = ct;
+    P[16] = ct * cp;
+    P[17] = ct * sp;
+    P[18] = st;
+    P[28] = P[3];
+    P[29] = P[4];
+  }
   const T dperp = (T)WATSON_DPAR * ((T)1.0 - P[1]);
   const T dgap = (T)WATSON_DPAR - dperp;
-  P[8] = dperp + dgap * ((T)1.0 - p2) * (T)(1.0 / 3.0);
-  P[9] = dgap * p2;
-  P[19] = dp2;
-#pragma unroll
-  for (int l = 1; l <= 6; l++) {
-    P[9 + l] = c[l];
-    P[19 + l] = dc[l];
-  }
+  P[8] = dperp + dgap * ((T)1.0 - P[26]) * (T)(1.0 / 3.0);
+  P[9] = dgap * P[26];
+  P[30] = (T)1.0;
+}
+
+// Even Legendre polynomials by the recurrence in y = x^2 obtained from two
+// uses of t P_n = ((n+1) P_{n+1} + n P_{n-1})/(2n+1):
+//   P_{n+2} = (a_n y - b_n) P_n - g_n P_{n-2},  n = 0, 2, ..., 10,
+// a_n = 1/alpha, b_n = beta/alpha, g_n = gamma/alpha with
+// alpha = (n+1)(n+2)/((2n+1)(2n+3)),
+// beta = (n+1)^2/((2n+1)(2n+3)) + n^2/((2n+1)(2n-1)),
+// gamma = n(n-1)/((2n+1)(2n-1)).
+__host__ __device__ constexpr double watson_leg_a(int l) {
+  return l == 0 ? 1.5 : l == 1 ? 2.9166666666666665 : l == 2 ? 3.2999999999999998
+       : l == 3 ? 3.4821428571428572 : l == 4 ? 3.588888888888889 : 3.6590909090909087;
+}
+__host__ __device__ constexpr double watson_leg_b(int l) {
+  return l == 0 ? 0.5 : l == 1 ? 1.5277777777777775 : l == 2 ? 1.6714285714285715
+       : l == 3 ? 1.7516233766233769 : l == 4 ? 1.8007407407407408 : 1.8337320574162681;
+}
+__host__ __device__ constexpr double watson_leg_g(int l) {
+  return l == 0 ? 0.0 : l == 1 ? 0.3888888888888889 : l == 2 ? 0.62857142857142856
+       : l == 3 ? 0.73051948051948057 : l == 4 ? 0.78814814814814815 : 0.82535885167464107;
 }
 
 // ---------------------------------------------------------------------------
 MACRO T Predicted_Signal(int npar, T* P, T* CFP, T* FixP) {
   const T xv = CFP[0] * P[5] + CFP[1] * P[6] + CFP[2] * P[7];
   const T extra = exp_gpu(-CFP[3] * (P[9] * xv * xv + P[8]));
-  // Legendre P_0..P_12 at the clamped cosine, one upward recurrence,
-  // accumulating the dispersed-stick SH sum on the way.
+  // Dispersed-stick SH sum over P_0..P_12 at the clamped cosine.
   const T x = min_gpu(max_gpu(xv, (T)-1.0), (T)1.0);
-  T pm = (T)1.0, pc = x;
+  const T y = x * x;
+  T pm = (T)0.0, pc = (T)1.0;
   T intra = CFP[5] * (T)3.5449077018110318;
 #pragma unroll
-  for (int n = 1; n < 12; n++) {
-    const T pn = ((T)(2 * n + 1) * x * pc - (T)n * pm) * (T)(1.0 / (n + 1));
+  for (int l = 0; l < 6; l++) {
+    const T pn = ((T)watson_leg_a(l) * y - (T)watson_leg_b(l)) * pc - (T)watson_leg_g(l) * pm;
     pm = pc;
     pc = pn;
-    if ((n + 1) % 2 == 0) intra += CFP[5 + (n + 1) / 2] * P[9 + (n + 1) / 2] * pc;
+    intra += CFP[6 + l] * P[10 + l] * pc;
   }
   if (intra < (T)0.0) intra = (T)0.5e-3;
   const T aniso = ((T)1.0 - P[1]) * extra + P[1] * intra;
@@ -304,24 +340,25 @@ MACRO void Partial_Derivatives(int npar, T* P, T* CFP, T* FixP, T* derivatives) 
   const T extra = exp_gpu(-CFP[3] * (P[9] * xv * xv + P[8]));
   const T x = min_gpu(max_gpu(xv, (T)-1.0), (T)1.0);
   const bool inside = (xv > (T)-1.0) && (xv < (T)1.0);
-  // P_n and P'_n (P'_{n+1} = P'_{n-1} + (2n+1) P_n) for n = 0..12.
-  T pm = (T)1.0, pc = x, dpm = (T)0.0, dpc = (T)1.0;
+  const T y = x * x;
+  // P_2l and dP_2l/dx by the even recurrence and its derivative
+  // dP_{n+2} = 2 a_n x P_n + (a_n y - b_n) dP_n - g_n dP_{n-2}.
+  T pm = (T)0.0, pc = (T)1.0, dpm = (T)0.0, dpc = (T)0.0;
   T intra = CFP[5] * (T)3.5449077018110318;
   T dintra_x = (T)0.0, dintra_k = (T)0.0;
 #pragma unroll
-  for (int n = 1; n < 12; n++) {
-    const T pn = ((T)(2 * n + 1) * x * pc - (T)n * pm) * (T)(1.0 / (n + 1));
-    const T dpn = dpm + (T)(2 * n + 1) * pc;
+  for (int l = 0; l < 6; l++) {
+    const T a = (T)watson_leg_a(l);
+    const T f = a * y - (T)watson_leg_b(l);
+    const T pn = f * pc - (T)watson_leg_g(l) * pm;
+    const T dpn = (T)2.0 * a * x * pc + f * dpc - (T)watson_leg_g(l) * dpm;
     pm = pc;
     pc = pn;
     dpm = dpc;
     dpc = dpn;
-    if ((n + 1) % 2 == 0) {
-      const int l = (n + 1) / 2;
-      intra += CFP[5 + l] * P[9 + l] * pc;
-      dintra_x += CFP[5 + l] * P[9 + l] * dpc;
-      dintra_k += CFP[5 + l] * P[19 + l] * pc;
-    }
+    intra += CFP[6 + l] * P[10 + l] * pc;
+    dintra_x += CFP[6 + l] * P[10 + l] * dpc;
+    dintra_k += CFP[6 + l] * P[20 + l] * pc;
   }
   if (intra < (T)0.0) {
     intra = (T)0.5e-3;

@@ -99,7 +99,7 @@ typedef struct {
   uint64_t seed;         /* --seed (8219)                             */
   int id_part;           /* --idPart (0)                              */
   /* GB300 launch shape: lanes cooperating on one voxel per stage
-   * (0 = chosen by the built-in tuner; otherwise one of 4, 8, 16, 32). */
+   * (0 = chosen by the built-in tuner; otherwise one of 1, 2, 4, 8, 16, 32). */
   int lanes_gridsearch;
   int lanes_levmar;
   int lanes_mcmc;
