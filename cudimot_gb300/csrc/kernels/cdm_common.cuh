@@ -25,7 +25,7 @@
 #define CDM_NT 128  // threads per CTA
 #endif
 #ifndef CDM_SSE_UNROLL
-#define CDM_SSE_UNROLL 1  // measurement-loop unroll of the cost sums
+#define CDM_SSE_UNROLL 2  // measurement-loop unroll of the cost sums
 #endif
 
 constexpr int kSseUnroll = CDM_SSE_UNROLL;
@@ -139,20 +139,30 @@ struct cdm_voxel_io {
 };
 
 // Sum of squared residuals over the voxel's measurements: each lane sums its
-// own measurements in FP32, the group total is formed in FP64.
+// own measurements in FP32, the group total is formed in FP64. The loop walks
+// a protocol-row pointer and a signal pointer; chunks where every lane has a
+// measurement need no bounds test, only the last chunk may be partial.
 template <int G>
 __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const float* sproto,
                                                 fp32* P, fp32* FixP, unsigned gmask) {
   float acc = 0.0f;
+  const int full = io.nmeas / G;
+  const float* row = sproto + (size_t)io.lane * kNCOLS4;
+  const float* sig = io.sig;
 #pragma unroll kSseUnroll
-  for (int c = 0; c < io.nchunk; c++) {
-    const int m = c * G + io.lane;
-    const bool valid = m < io.nmeas;
+  for (int c = 0; c < full; c++) {
     fp32 cf[kNCOLS];
-    cdm_load_cfp(sproto, io.nmeas_pad, valid ? m : 0, cf);
-    const float y = io.sig[(size_t)c * io.chunk_stride];
-    const float s = (float)Predicted_Signal(NPARAMS, P, cf, FixP);
-    const float r = s - y;
+    cdm_load_cfp(row, 0, 0, cf);
+    const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - *sig;
+    acc = fmaf(r, r, acc);
+    row += G * kNCOLS4;
+    sig += io.chunk_stride;
+  }
+  if (full < io.nchunk) {
+    const bool valid = full * G + io.lane < io.nmeas;
+    fp32 cf[kNCOLS];
+    cdm_load_cfp(valid ? row : sproto, 0, 0, cf);
+    const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - *sig;
     acc = valid ? fmaf(r, r, acc) : acc;
   }
   return cdm_group_sum<G>((double)acc, gmask);

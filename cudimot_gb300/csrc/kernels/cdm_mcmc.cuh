@@ -41,12 +41,11 @@ struct cdm_mcmc_args {
   cdm_limits lim;
 };
 
-template <int N>
-__device__ __forceinline__ float cdm_prior(const cdm_limits& L, int p, fp32 (&P)[N], int nmeas,
+__device__ __forceinline__ float cdm_prior(const cdm_limits& L, int p, fp32* P, int nmeas,
                                            fp32* cfp_all, fp32* FixP) {
   fp32 xv = P[0];
 #pragma unroll
-  for (int k = 1; k < N; k++) xv = (k == p) ? P[k] : xv;
+  for (int k = 1; k < kNP; k++) xv = (k == p) ? P[k] : xv;
   const float x = (float)xv;
   switch (L.ptype[p]) {
     case GAUSSPRIOR: {
@@ -66,12 +65,11 @@ __device__ __forceinline__ float cdm_prior(const cdm_limits& L, int p, fp32 (&P)
   }
 }
 
-template <int N>
-__device__ __forceinline__ bool cdm_in_bounds(const cdm_limits& L, int p, fp32 (&P)[N]) {
+__device__ __forceinline__ bool cdm_in_bounds(const cdm_limits& L, int p, fp32* P) {
   if (!ConstraintsMCMC(NPARAMS, P)) return false;
   fp32 xv = P[0];
 #pragma unroll
-  for (int k = 1; k < N; k++) xv = (k == p) ? P[k] : xv;
+  for (int k = 1; k < kNP; k++) xv = (k == p) ? P[k] : xv;
   const float x = (float)xv;
   if (L.btype[p] == BMIN) return !(x < L.bmin[p]);
   if (L.btype[p] == BMAX) return !(x > L.bmax[p]);
@@ -83,17 +81,18 @@ __device__ __forceinline__ bool cdm_in_bounds(const cdm_limits& L, int p, fp32 (
 // parameters is kept rolled (one copy of the inlined likelihood in the
 // instruction cache instead of NPARAMS), and these unrolled selects keep
 // the arrays in registers.
-template <class V, int N>
-__device__ __forceinline__ V cdm_get(const V (&a)[N], int i) {
+// Only the first kNP entries are ever selected (the model parameters).
+template <class V>
+__device__ __forceinline__ V cdm_get(const V* a, int i) {
   V v = a[0];
 #pragma unroll
-  for (int k = 1; k < N; k++) v = (k == i) ? a[k] : v;
+  for (int k = 1; k < kNP; k++) v = (k == i) ? a[k] : v;
   return v;
 }
-template <class V, int N>
-__device__ __forceinline__ void cdm_set(V (&a)[N], int i, V x) {
+template <class V>
+__device__ __forceinline__ void cdm_set(V* a, int i, V x) {
 #pragma unroll
-  for (int k = 0; k < N; k++) a[k] = (k == i) ? x : a[k];
+  for (int k = 0; k < kNP; k++) a[k] = (k == i) ? x : a[k];
 }
 
 template <int G, bool RICIAN>

@@ -1,0 +1,128 @@
+"""The GPU library against CUDIMOT's own kernels, run unmodified on the same
+GPU and inputs (oracle/refkernels: the reference .cu files compiled to
+sm_103a cubins where the CUDIMOT tree is available; skipped elsewhere).
+
+This pins the fitting loops to the reference implementation itself:
+  * Ball_1_Stick: predicted signal, LM fit, BIC/AIC and MCMC posterior
+    statistics (CUDIMOT's plugin is restated formula for formula);
+  * NODDI_Watson: grid-search winners and LM fits. CUDIMOT's Watson plugin
+    carries its own numerical errors (documented in the design doc), so cost
+    comparisons use our FP64 model for both fits."""
+import numpy as np
+import pytest
+import torch
+
+from cudimot_gb300 import capi, synth
+from tests.helpers import angle_deg, b1s, oracle, watson
+
+pytestmark = pytest.mark.gpu
+
+rk = pytest.importorskip("oracle.refkernels.refkernels")
+
+
+def need(model):
+    if not rk.available(model):
+        pytest.skip(f"reference cubins for {model} not built")
+
+
+def T(x, dev):
+    return torch.as_tensor(np.ascontiguousarray(x, dtype=np.float64), device=dev)
+
+
+def test_b1s_predicted_and_bic_vs_reference_kernels(built, cuda):
+    need("Ball_1_Stick")
+    wl = b1s(4000)
+    ref = rk.RefKernels("Ball_1_Stick", 5)
+    ours = capi.Cudimot("Ball_1_Stick", capi.model_cfg("Ball_1_Stick"))
+    s = T(wl.truth[:, :, None], cuda)
+    p1 = torch.zeros(wl.nvox, wl.nmeas, dtype=torch.float64, device=cuda)
+    p2 = torch.zeros_like(p1)
+    ref.predicted(s, T(wl.cfp, cuda), None, p1)
+    ours.predicted_signal(s, T(wl.cfp, cuda), T(wl.fixp, cuda), p2)
+    torch.cuda.synchronize()
+    a, b = p1.cpu().numpy(), p2.cpu().numpy()
+    assert np.all(np.abs(a - b) <= 2e-5 * np.abs(a) + 2e-6 * wl.truth[:, :1])
+    b1, a1 = torch.zeros(wl.nvox, dtype=torch.float64, device=cuda), torch.zeros(wl.nvox, dtype=torch.float64, device=cuda)
+    b2, a2 = torch.zeros_like(b1), torch.zeros_like(a1)
+    ref.bic_aic(T(wl.meas, cuda), s, T(wl.cfp, cuda), None, b1, a1)
+    ours.bic_aic(T(wl.meas, cuda), s, T(wl.cfp, cuda), T(wl.fixp, cuda), b2, a2)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(b2.cpu().numpy(), b1.cpu().numpy(), rtol=5e-6)
+    np.testing.assert_allclose(a2.cpu().numpy(), a1.cpu().numpy(), rtol=5e-6)
+
+
+def test_b1s_levmar_vs_reference_kernels(built, cuda):
+    need("Ball_1_Stick")
+    wl = b1s(4000)
+    cfg = capi.model_cfg("Ball_1_Stick")
+    ref = rk.RefKernels("Ball_1_Stick", 5)
+    ours = capi.Cudimot("Ball_1_Stick", cfg)
+    pr, po = T(wl.init, cuda), T(wl.init, cuda)
+    ref.levmar(cfg, T(wl.meas, cuda), pr, T(wl.cfp, cuda), None)
+    ours.levmar(T(wl.meas, cuda), po, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    torch.cuda.synchronize()
+    r, g = pr.cpu().numpy(), po.cpu().numpy()
+    o = oracle("Ball_1_Stick")
+    cr, cg = o.cost(wl.meas, r, wl.cfp), o.cost(wl.meas, g, wl.cfp)
+    rel = (cg - cr) / cr
+    ang = angle_deg(r[:, 3], r[:, 4], g[:, 3], g[:, 4])
+    assert np.mean(rel <= 1e-4) >= 0.995, np.quantile(rel, [0.5, 0.99, 1])
+    assert np.mean(ang <= 0.5) >= 0.995
+
+
+def test_b1s_mcmc_vs_reference_kernels(built, cuda):
+    need("Ball_1_Stick")
+    wl = b1s(512, seed=9)
+    cfg = capi.model_cfg("Ball_1_Stick", run_mcmc=1, nburn=500, njumps=2000, sampleevery=10)
+    o = oracle("Ball_1_Stick")
+    start, _, _, _ = o.levmar(cfg, wl.meas, wl.init, wl.cfp, wl.fixp)
+    ref = rk.RefKernels("Ball_1_Stick", 5)
+    ours = capi.Cudimot("Ball_1_Stick", cfg)
+    ns = 200
+    sr = torch.zeros(wl.nvox, 5, ns, dtype=torch.float64, device=cuda)
+    so = torch.zeros_like(sr)
+    ref.mcmc(cfg, T(wl.meas, cuda), T(start, cuda), T(wl.cfp, cuda), None, sr)
+    ours.mcmc(T(wl.meas, cuda), T(start, cuda), T(wl.cfp, cuda), T(wl.fixp, cuda), so)
+    torch.cuda.synchronize()
+    r, g = sr.cpu().numpy(), so.cpu().numpy()
+    for p in (0, 1, 2):
+        def se(x):
+            bm = x.reshape(x.shape[0], 10, -1).mean(2)
+            return bm.std(1, ddof=1) / np.sqrt(10)
+        z = (g[:, p].mean(1) - r[:, p].mean(1)) / np.sqrt(se(g[:, p]) ** 2 + se(r[:, p]) ** 2 + 1e-30)
+        assert abs(np.median(z)) < 0.5, (p, np.median(z))
+        assert np.mean(np.abs(z) < 4) > 0.95, (p, np.mean(np.abs(z) < 4))
+        ratio = np.median(g[:, p].std(1) / np.maximum(r[:, p].std(1), 1e-30))
+        assert 0.8 < ratio < 1.25, (p, ratio)
+
+
+def test_watson_gridsearch_and_levmar_vs_reference_kernels(built, cuda):
+    need("NODDI_Watson")
+    wl = watson(4000, seed=13)
+    cfg = capi.model_cfg("NODDI_Watson", grid=synth.WATSON_GRID)
+    ref = rk.RefKernels("NODDI_Watson", 5)
+    ours = capi.Cudimot("NODDI_Watson", cfg)
+    grid = T(cfg.grid_array, cuda)
+    pr, po = T(wl.init, cuda), T(wl.init, cuda)
+    ref.gridsearch(cfg, T(wl.meas, cuda), pr, T(wl.cfp, cuda), T(wl.fixp, cuda), grid)
+    ours.gridsearch(T(wl.meas, cuda), po, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    torch.cuda.synchronize()
+    r, g = pr.cpu().numpy(), po.cpu().numpy()
+    same = np.all(r == g, axis=1)
+    assert same.mean() >= 0.99, same.mean()
+    # where the winners differ, their costs under the exact model are within
+    # CUDIMOT's own model error of each other
+    o = oracle("NODDI_Watson")
+    cr, cg = o.cost(wl.meas, r, wl.cfp, wl.fixp), o.cost(wl.meas, g, wl.cfp, wl.fixp)
+    assert np.all(cg[~same] <= cr[~same] * (1 + 2e-3))
+    # LM from the reference's grid-search result
+    pr2, po2 = T(r, cuda), T(r, cuda)
+    ref.levmar(cfg, T(wl.meas, cuda), pr2, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    ours.levmar(T(wl.meas, cuda), po2, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    torch.cuda.synchronize()
+    r2, g2 = pr2.cpu().numpy(), po2.cpu().numpy()
+    cr2, cg2 = o.cost(wl.meas, r2, wl.cfp, wl.fixp), o.cost(wl.meas, g2, wl.cfp, wl.fixp)
+    rel = (cg2 - cr2) / cr2
+    assert np.mean(rel <= 1e-4) >= 0.98, np.quantile(rel, [0.5, 0.98, 1])
+    ang = angle_deg(r2[:, 3], r2[:, 4], g2[:, 3], g2[:, 4])
+    assert np.mean(ang <= 0.5) >= 0.98, np.quantile(ang, [0.5, 0.98, 1])
