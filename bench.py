@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--nvox", type=int, default=NVOX)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="voxels for the CPU baseline")
+    ap.add_argument("--profile-stage", choices=["gridsearch", "levmar", "mcmc"], default=None,
+                    help="run the preceding stages, then one launch of this stage (for ncu)")
+    ap.add_argument("--nburn", type=int, default=NBURN)
+    ap.add_argument("--njumps", type=int, default=NJUMPS)
     return ap.parse_args()
 
 
@@ -206,9 +210,54 @@ def run_reference(a, rank, world):
     print(json.dumps(line))
 
 
+def profile_stage(a):
+    """One launch of one stage on a small case, for ncu captures."""
+    import torch
+    from cudimot_gb300 import capi, synth
+    dev = torch.device("cuda:0")
+    cfp, meas, fixp, init, _ = make_workload(a.nvox, 8219, dev)
+    cfg = capi.model_cfg(MODEL, grid=synth.WATSON_GRID, run_mcmc=1, nburn=a.nburn,
+                         njumps=a.njumps, sampleevery=SE)
+    lib = capi.Cudimot(MODEL, cfg)
+    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
+    m, c, f, p = t(meas), t(cfp), t(fixp), t(init)
+    if a.profile_stage in ("levmar", "mcmc"):
+        lib.gridsearch(m, p, c, f)
+    if a.profile_stage == "mcmc":
+        lib.levmar(m, p, c, f)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    if a.profile_stage == "gridsearch":
+        lib.gridsearch(m, p, c, f)
+    elif a.profile_stage == "levmar":
+        lib.levmar(m, p, c, f)
+    else:
+        s = torch.zeros(a.nvox, 5, max(a.njumps // SE, 1), dtype=torch.float64, device=dev)
+        lib.mcmc(m, p, c, f, s)
+    e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"stage": a.profile_stage, "nvox": a.nvox, "ms": e0.elapsed_time(e1)}))
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the MCMC kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "mcmc_kernel_noddi_watson.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1].split()[0])
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
+
+
 def main():
     a = parse()
     rank, world, local = dist_env()
+    if a.profile_stage:
+        profile_stage(a)
+        return
     if a.impl == "reference":
         if world > 1:
             import torch.distributed as dist
@@ -279,7 +328,8 @@ def main():
         achieved = per_voxel_mcmc * nvox / (mcmc_ms / 1e3) / 1e12
         roofline = {"bound": "fp32", "kernel": "cdm_mcmc_kernel", "achieved": achieved,
                     "peak": fp32_peak["tflops"], "unit": "TFLOP/s", "frac": achieved / fp32_peak["tflops"],
-                    "peak_source": fp32_peak["source"], "traffic": None,
+                    "peak_source": fp32_peak["source"], "traffic": profiled_traffic(),
+                    "traffic_source": "profiles/mcmc_kernel_noddi_watson.md (small-case ncu capture scaled by voxels)",
                     "flop_per_voxel": per_voxel_mcmc, "launch_ms": mcmc_ms}
     line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -290,17 +340,49 @@ def main():
                        "parallelism": f"voxel shards x{world}"},
             "gpu_launches": gpu_launches_per_step(cfg) * a.steps,
             "clocks": clk.summary(),
-            "lm_iterations_per_voxel": stats.lm_iterations / max(nvox, 1) / max(a.steps + a.warmup, 1),
+            # cdm_fit clears the counters, so they hold the last step alone
+            "lm_iterations_per_voxel": stats.lm_iterations / max(nvox, 1),
             "gs_recheck_voxels": stats.gs_recheck_voxels,
             "roofline": roofline, "e2e": e2e}
     if os.environ.get("CDM_BENCH_CPU", "1") != "0":
-        n = a.cpu_sample or 64
+        n = a.cpu_sample or 4096
         from oracle.oracle import Oracle  # noqa: F401
         v, threads, dt = cpu_baseline(cfp, meas, fixp, init, n, cfg)
         line["cpu_baseline"] = {"value": v, "unit": "voxels/s", "cores": threads, "kind": "port",
                                 "sample": f"{n} voxels of this workload, grid search -> LM -> MCMC, "
                                           f"FP64 CPU oracle, {dt:.1f} s"}
+    if os.environ.get("CDM_BENCH_REFK", "1") != "0":
+        line["reference_kernels"] = reference_kernels_leg(cfp, meas, fixp, init, cfg, dev)
     print(json.dumps(line))
+
+
+def reference_kernels_leg(cfp, meas, fixp, init, cfg, dev, n=2048):
+    """CUDIMOT's own GridSearch/LM/MCMC kernels (unmodified sources compiled
+    for sm_103a, T = double as shipped) on the first n voxels of this
+    workload, same GPU; wall time of the three stages."""
+    import time
+    import torch
+    try:
+        from oracle.refkernels.refkernels import RefKernels, available
+        if not available(MODEL):
+            return {"unavailable": "CUDIMOT kernels were not compiled (source tree absent at build time)"}
+        ref = RefKernels(MODEL, 5)
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
+    m, c, f, p = t(meas[:n]), t(cfp), t(fixp[:n]), t(init[:n])
+    s = torch.zeros(n, 5, NJUMPS // SE, dtype=torch.float64, device=dev)
+    grid = t(cfg.grid_array)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref.gridsearch(cfg, m, p, c, f, grid)
+    ref.levmar(cfg, m, p, c, f)
+    ref.mcmc(cfg, m, p, c, f, s)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "voxels/s", "seconds": dt,
+            "sample": f"first {n} voxels of this workload, grid search -> LM -> MCMC, "
+                      "one warp per voxel as CUDIMOT launches them"}
 
 
 def gpu_launches_per_step(cfg):
