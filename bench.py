@@ -168,8 +168,10 @@ def cpu_baseline(cfp, meas, fixp, init, n, cfg):
 
 
 def flop_model():
-    """Algorithmic FP32 work per voxel: counted by the
-    library's FLOP-count build of the plugin, when available."""
+    """Algorithmic FP32 work per voxel of the MCMC stage: operations of one
+    likelihood (Derived_P after a one-parameter change + nmeas x (signal + 3))
+    x free parameters x (burn-in + jumps), counted by the library's
+    operation-count build of the plugin (cudimot_gb300/flops.py)."""
     try:
         from cudimot_gb300 import flops
         return flops.watson_c1_flops_per_voxel()

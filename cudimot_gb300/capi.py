@@ -163,6 +163,14 @@ MODEL_LIMITS = {
     "NODDI_Watson": dict(bounds={0: (0.0, 1.0), 1: (0.0, 1.0), 2: (0.0, 64.0),
                                  3: (-100.0, 100.0), 4: (-100.0, 100.0)},
                          priors={3: (SINPRIOR,)}),
+    "DiffusionTensor": dict(bounds={0: (0.1, 10000.0), 1: (0.0, 0.01), 2: (None, None),
+                                    3: (None, None), 4: (0.0, 0.01), 5: (None, None),
+                                    6: (0.0, 0.01)},
+                            priors={}),
+    "Ball_2_Sticks": dict(bounds={0: (0.0, 10000.0), 1: (0.0, 0.01), 2: (0.0, 1.0),
+                                  3: (-100.0, 100.0), 4: (-100.0, 100.0), 5: (0.0, 1.0),
+                                  6: (-100.0, 100.0), 7: (-100.0, 100.0)},
+                          priors={3: (SINPRIOR,), 5: (ARDPRIOR, 1.0), 6: (SINPRIOR,)}),
 }
 
 

@@ -7,8 +7,11 @@
 // !(success && iter++ >= max_iters) so only accepted steps count; damping
 // is Marquardt's (1+lambda) diagonal scaling (or Levenberg's +lambda);
 // lambda starts at 0.1, is divided by 10 on success and multiplied by 10 on
-// failure; the fit ends when 2|dc| <= 1e-8 (|c|+|c'|+2e-16) after a success
-// or when lambda exceeds 1e20; FixConstraintsLM runs at the end.
+// failure; the fit ends when 2|dc| <= tol (|c|+|c'|+2e-16) after a success
+// or when lambda exceeds 1e20; FixConstraintsLM runs at the end. Two
+// departures, both for single-precision costs: tol is CDM_LM_CFTOL (1e-6)
+// instead of 1e-8, and a rejected step that changed no parameter ends the
+// fit (every later trial would be the same point).
 //
 // GB300 structure: one pass over the measurements per accepted step forms
 // the residual and the Jacobian once and accumulates J^T r and the upper
@@ -16,7 +19,7 @@
 // for the gradient and once for the Hessian, with a warp reduction per
 // element and 32-measurement chunk). The lane partials are summed across the
 // group in FP64 and the damped normal equations are solved in FP64 registers
-// by the same unpivoted Gauss-Jordan elimination as CUDIMOT's LUsolver
+// by symmetric elimination in the pivot order of CUDIMOT's unpivoted LUsolver
 // (:334-407). Undamped sums are kept, and damping is applied to a fresh copy
 // each iteration, which equals CUDIMOT's cumulative rescaling.
 #pragma once
@@ -111,6 +114,58 @@ __device__ __forceinline__ void cdm_lm_chain(const cdm_limits& L, const float* P
 
 constexpr int kNH = kNP * (kNP + 1) / 2;
 
+// Index of (i, q), i <= q, in the packed upper triangle (row-major).
+__host__ __device__ constexpr int cdm_hidx(int i, int q) { return i * kNP - i * (i - 1) / 2 + (q - i); }
+
+// Convergence tolerance on the relative cost change of an accepted step.
+// CUDIMOT's is 1e-8 (Levenberg_Marquardt.cu:21,34), below the resolution of
+// a cost built from single-precision residuals (relative noise ~1e-7), so
+// an FP32 fit would only stop on lambda > 1e20 or the iteration limit after
+// dozens of noise-driven steps. 1e-6 stops where the FP32 cost stops
+// carrying information; the final cost then differs from a fully converged
+// FP64 fit by a few 1e-6 relative.
+#ifndef CDM_LM_CFTOL
+#define CDM_LM_CFTOL 1.0e-6
+#endif
+
+// Damped normal equations (H + damping) x = g in FP64, all in registers:
+// symmetric Gaussian elimination on the packed upper triangle (no pivoting,
+// the pivot order of CUDIMOT's Gauss-Jordan LUsolver,
+// Levenberg_Marquardt.cu:334-407), then back substitution. ~n^3/6
+// multiply-adds instead of Gauss-Jordan's ~n^3/2.
+__device__ __forceinline__ void cdm_lm_solve(const double (&H)[kNH], const double (&g)[kNP],
+                                             double lambda, bool marquardt, double (&x)[kNP]) {
+  double A[kNH], b[kNP];
+#pragma unroll
+  for (int i = 0; i < kNP; i++) {
+    b[i] = g[i];
+#pragma unroll
+    for (int q = i; q < kNP; q++) {
+      const double h = H[cdm_hidx(i, q)];
+      A[cdm_hidx(i, q)] = i == q ? (marquardt ? (1.0 + lambda) * h : h + lambda) : h;
+    }
+  }
+  double dinv[kNP];
+#pragma unroll
+  for (int j = 0; j < kNP; j++) {
+    dinv[j] = 1.0 / A[cdm_hidx(j, j)];
+#pragma unroll
+    for (int i = j + 1; i < kNP; i++) {
+      const double f = A[cdm_hidx(j, i)] * dinv[j];
+#pragma unroll
+      for (int q = i; q < kNP; q++) A[cdm_hidx(i, q)] -= f * A[cdm_hidx(j, q)];
+      b[i] -= f * b[j];
+    }
+  }
+#pragma unroll
+  for (int i = kNP - 1; i >= 0; i--) {
+    double acc = b[i];
+#pragma unroll
+    for (int q = i + 1; q < kNP; q++) acc -= A[cdm_hidx(i, q)] * x[q];
+    x[i] = acc * dinv[i];
+  }
+}
+
 template <int G>
 __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constant__ cdm_lm_args a) {
   extern __shared__ __align__(16) float sproto[];
@@ -190,44 +245,12 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
           H[k++] = (L.fixed[i] || L.fixed[q]) ? (i == q ? 1.0 : 0.0) : s;
         }
     }
-    // Damped system and unpivoted Gauss-Jordan on [A | g].
-    double M[kNP][kNP + 1];
-    {
-      int k = 0;
-#pragma unroll
-      for (int i = 0; i < kNP; i++)
-#pragma unroll
-        for (int q = i; q < kNP; q++) {
-          M[i][q] = H[k];
-          M[q][i] = H[k];
-          k++;
-        }
-#pragma unroll
-      for (int i = 0; i < kNP; i++) {
-        M[i][i] = a.marquardt ? (1.0 + lambda) * M[i][i] : M[i][i] + lambda;
-        M[i][kNP] = g[i];
-      }
-    }
-#pragma unroll
-    for (int col = 0; col < kNP; col++) {
-      const double inv = 1.0 / M[col][col];
-#pragma unroll
-      for (int j = col; j <= kNP; j++) M[col][j] *= inv;
-#pragma unroll
-      for (int row = col + 1; row < kNP; row++) {
-        const double f = M[row][col];
-#pragma unroll
-        for (int j = col; j <= kNP; j++) M[row][j] -= f * M[col][j];
-      }
-    }
-#pragma unroll
-    for (int col = kNP - 1; col > 0; col--)
-#pragma unroll
-      for (int row = 0; row < col; row++) M[row][kNP] -= M[row][col] * M[col][kNP];
+    double x[kNP];
+    cdm_lm_solve(H, g, lambda, a.marquardt != 0, x);
 
     float step[kNP];
 #pragma unroll
-    for (int i = 0; i < kNP; i++) step[i] = Pt[i] - (float)M[i][kNP];
+    for (int i = 0; i < kNP; i++) step[i] = Pt[i] - (float)x[i];
     fp32 Pn[kNPS];
 #pragma unroll
     for (int i = 0; i < kNPS; i++) Pn[i] = P[i];
@@ -242,11 +265,16 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
 #pragma unroll
       for (int i = 0; i < kNPS; i++) P[i] = Pn[i];
       lambda *= 0.1;
-      if (2.0 * fabs(pcf - ncf) <= 1.0e-8 * (fabs(pcf) + fabs(ncf) + 2.0e-16)) end = true;
+      if (2.0 * fabs(pcf - ncf) <= CDM_LM_CFTOL * (fabs(pcf) + fabs(ncf) + 2.0e-16)) end = true;
       pcf = ncf;
     } else {
+      // A rejected step that moved no parameter at all: larger damping only
+      // shrinks the step further, so every later trial is the same point.
+      bool moved = false;
+#pragma unroll
+      for (int i = 0; i < kNP; i++) moved |= (float)Pn[i] != (float)P[i];
       lambda *= 10.0;
-      if (lambda > 1.0e20) end = true;
+      if (lambda > 1.0e20 || !moved) end = true;
       // CUDIMOT re-derives P from Pt after a rejected step (:593), which can
       // nudge Pt at a two-sided bound.
       cdm_lm_transform(L, P, Pt);

@@ -81,6 +81,33 @@ def b1s_signal(P, cfp):
     return S0 * ((1 - f) * np.exp(-b * d) + f * np.exp(-b * d * gv * gv))
 
 
+def dti_fit(meas, cfp):
+    """Log-linear tensor fit per voxel -> (S0 [n], tensor entries [n][6] in
+    the order Dxx, Dxy, Dxz, Dyy, Dyz, Dzz, eigenvalues [n][3] descending,
+    eigenvectors [n][3][3] with column k the k-th eigenvector)."""
+    g = cfp[:, :3]
+    b = cfp[:, 3]
+    X = np.stack([np.ones_like(b), -b * g[:, 0] ** 2, -2 * b * g[:, 0] * g[:, 1],
+                  -2 * b * g[:, 0] * g[:, 2], -b * g[:, 1] ** 2, -2 * b * g[:, 1] * g[:, 2],
+                  -b * g[:, 2] ** 2], axis=1)
+    y = np.log(np.maximum(meas, 1e-3))
+    coef, *_ = np.linalg.lstsq(X, y.T, rcond=None)
+    coef = coef.T
+    S0 = np.exp(coef[:, 0])
+    t = coef[:, 1:]
+    D = np.zeros((meas.shape[0], 3, 3))
+    D[:, 0, 0], D[:, 1, 1], D[:, 2, 2] = t[:, 0], t[:, 3], t[:, 5]
+    D[:, 0, 1] = D[:, 1, 0] = t[:, 1]
+    D[:, 0, 2] = D[:, 2, 0] = t[:, 2]
+    D[:, 1, 2] = D[:, 2, 1] = t[:, 4]
+    w, V = np.linalg.eigh(D)
+    return S0, t, w[:, ::-1].copy(), V[:, :, ::-1].copy()
+
+
+def _angles(v):
+    return np.arccos(np.clip(v[:, 2], -1.0, 1.0)), np.arctan2(v[:, 1], v[:, 0])
+
+
 def dti_init(meas, cfp):
     """Log-linear tensor fit per voxel -> (S0, mean diffusivity, FA, V1).
 
@@ -164,3 +191,87 @@ def noddi_watson(nvox=200_000, seed=DEFAULT_SEED, signal_fn=None, snr=20.0) -> W
     init = np.stack([np.full(nvox, 0.4), np.full(nvox, 0.8), np.full(nvox, 5.0), thi, phi], axis=1)
     return Workload("noddi_watson_gs_lm_mcmc", "NODDI_Watson", cfp, meas, truth, init,
                     s0_est[:, None].copy(), grid=WATSON_GRID)
+
+
+def dt_signal(P, cfp):
+    """Diffusion-tensor signal S0 exp(-b g^T D g), numpy."""
+    g = cfp[:, :3]
+    b = cfp[:, 3]
+    q = np.stack([b * g[:, 0] ** 2, 2 * b * g[:, 0] * g[:, 1], 2 * b * g[:, 0] * g[:, 2],
+                  b * g[:, 1] ** 2, 2 * b * g[:, 1] * g[:, 2], b * g[:, 2] ** 2], axis=1)
+    return P[:, :1] * np.exp(-(P[:, 1:7] @ q.T))
+
+
+def random_rotations(n, rng):
+    """Uniform random rotation matrices (QR of Gaussian matrices, sign-fixed)."""
+    A = rng.standard_normal((n, 3, 3))
+    Q, R = np.linalg.qr(A)
+    Q = Q * np.sign(np.diagonal(R, axis1=1, axis2=2))[:, None, :]
+    det = np.linalg.det(Q)
+    Q[:, :, 0] *= det[:, None]
+    return Q
+
+
+def diffusion_tensor(nvox=400_000, seed=DEFAULT_SEED, snr=25.0) -> Workload:
+    """Diffusion tensor, LM (+ MCMC): 7 b0 + 64@1000 (71 measurements);
+    eigenvalues l1~U(1.2e-3,2e-3), l2,l3~U(0.2e-3,0.8e-3) under a uniform
+    random rotation, S0~U(500,1500); Rician noise sigma = S0/snr; initialised
+    from the log-linear tensor fit."""
+    r_proto, r_par, r_noise = _streams(seed, 3)
+    cfp = protocol(7, [(64, 1000.0)], r_proto)
+    S0 = r_par.uniform(500, 1500, nvox)
+    lam = np.stack([r_par.uniform(1.2e-3, 2e-3, nvox), r_par.uniform(0.2e-3, 0.8e-3, nvox),
+                    r_par.uniform(0.2e-3, 0.8e-3, nvox)], axis=1)
+    R = random_rotations(nvox, r_par)
+    D = np.einsum("nij,nj,nkj->nik", R, lam, R)
+    truth = np.stack([S0, D[:, 0, 0], D[:, 0, 1], D[:, 0, 2], D[:, 1, 1], D[:, 1, 2], D[:, 2, 2]],
+                     axis=1)
+    meas = rician(dt_signal(truth, cfp), S0 / snr, r_noise)
+    s0i, t, _, _ = dti_fit(meas, cfp)
+    init = np.concatenate([np.clip(s0i, 1.0, 9000.0)[:, None], t], axis=1)
+    for k in (1, 4, 6):
+        init[:, k] = np.clip(init[:, k], 1e-6, 9e-3)
+    return Workload("diffusion_tensor", "DiffusionTensor", cfp, meas, truth, init,
+                    np.zeros((nvox, 0)))
+
+
+def b2s_signal(P, cfp):
+    """Ball & 2 Sticks signal, numpy."""
+    S0, d, f1, t1, p1, f2, t2, p2 = (P[:, i:i + 1] for i in range(8))
+    g = cfp[None, :, :3]
+    b = cfp[None, :, 3]
+
+    def dot(th, ph):
+        v = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], axis=-1)
+        return np.sum(g * v, axis=-1)
+
+    x1, x2 = dot(t1, p1), dot(t2, p2)
+    return S0 * ((1 - f1 - f2) * np.exp(-b * d) + f1 * np.exp(-b * d * x1 * x1) +
+                 f2 * np.exp(-b * d * x2 * x2))
+
+
+def ball_2_sticks(nvox=300_000, seed=DEFAULT_SEED, snr=25.0) -> Workload:
+    """Ball & 2 Sticks, LM (+ MCMC): 6 b0 + 64@1000 + 64@2000 (134
+    measurements); S0~U(500,1500), d~U(0.5e-3,2.5e-3), f1~U(0.2,0.6),
+    f2~U(0,f1), orientations uniform; Rician sigma = S0/snr. Initialised as
+    CUDIMOT's Ball_2_Sticks pipeline does from dtifit: S0, L1, FA, V1, FA/4,
+    V2."""
+    r_proto, r_par, r_noise = _streams(seed, 3)
+    cfp = protocol(6, [(64, 1000.0), (64, 2000.0)], r_proto)
+    S0 = r_par.uniform(500, 1500, nvox)
+    d = r_par.uniform(0.5e-3, 2.5e-3, nvox)
+    f1 = r_par.uniform(0.2, 0.6, nvox)
+    f2 = r_par.uniform(0.0, 1.0, nvox) * f1
+    t1, p1 = sphere_angles(nvox, r_par)
+    t2, p2 = sphere_angles(nvox, r_par)
+    truth = np.stack([S0, d, f1, t1, p1, f2, t2, p2], axis=1)
+    meas = rician(b2s_signal(truth, cfp), S0 / snr, r_noise)
+    s0i, _, w, V = dti_fit(meas, cfp)
+    md = w.mean(axis=1)
+    fa = np.sqrt(1.5 * np.sum((w - md[:, None]) ** 2, axis=1) / np.maximum(np.sum(w * w, axis=1), 1e-30))
+    fa = np.clip(fa, 0.02, 0.95)
+    th1, ph1 = _angles(V[:, :, 0])
+    th2, ph2 = _angles(V[:, :, 1])
+    init = np.stack([np.clip(s0i, 1.0, 9000.0), np.clip(w[:, 0], 1e-5, 9e-3), fa, th1, ph1,
+                     fa / 4.0, th2, ph2], axis=1)
+    return Workload("ball_2_sticks", "Ball_2_Sticks", cfp, meas, truth, init, np.zeros((nvox, 0)))

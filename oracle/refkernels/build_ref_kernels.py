@@ -34,7 +34,10 @@ def nvcc():
     raise FileNotFoundError("nvcc")
 
 
-def build_cubins(reference, models=("Ball_1_Stick", "NODDI_Watson"), jobs=8):
+MODELS = ("Ball_1_Stick", "NODDI_Watson", "DiffusionTensor", "Ball_2_Sticks")
+
+
+def build_cubins(reference, models=MODELS, jobs=8):
     todo = []
     for m in models:
         out = os.path.join(REF_OUT, m)
@@ -84,7 +87,7 @@ def available(model):
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", required=True)
-    ap.add_argument("--models", nargs="*", default=["Ball_1_Stick", "NODDI_Watson"])
+    ap.add_argument("--models", nargs="*", default=list(MODELS))
     a = ap.parse_args()
     errs = build_cubins(a.reference, a.models)
     for e in errs:

@@ -14,6 +14,7 @@ needed to run them):
   fit_<Model>.npz     grid search (Watson) and LM results of the oracle's
                       fitting loops driven by the reference plugin on
                       48 synthetic voxels.
+Models: Ball_1_Stick, NODDI_Watson, DiffusionTensor, Ball_2_Sticks.
 """
 import os
 import sys
@@ -34,6 +35,20 @@ def plugin_inputs(model, rng):
     if model == "Ball_1_Stick":
         P = np.stack([rng.uniform(500, 1500, n), rng.uniform(0.3e-3, 3e-3, n),
                       rng.uniform(0.02, 0.95, n), rng.uniform(-3, 3, n), rng.uniform(-3, 3, n)], 1)
+        F = np.zeros((n, 0))
+    elif model == "DiffusionTensor":
+        lam = np.stack([rng.uniform(1e-3, 2.5e-3, n), rng.uniform(0.1e-3, 1e-3, n),
+                        rng.uniform(0.1e-3, 1e-3, n)], 1)
+        R = synth.random_rotations(n, rng)
+        D = np.einsum("nij,nj,nkj->nik", R, lam, R)
+        P = np.stack([rng.uniform(500, 1500, n), D[:, 0, 0], D[:, 0, 1], D[:, 0, 2], D[:, 1, 1],
+                      D[:, 1, 2], D[:, 2, 2]], 1)
+        F = np.zeros((n, 0))
+    elif model == "Ball_2_Sticks":
+        f1 = rng.uniform(0.05, 0.7, n)
+        P = np.stack([rng.uniform(500, 1500, n), rng.uniform(0.3e-3, 3e-3, n), f1,
+                      rng.uniform(-3, 3, n), rng.uniform(-3, 3, n), rng.uniform(0, 1, n) * (1 - f1),
+                      rng.uniform(-3, 3, n), rng.uniform(-3, 3, n)], 1)
         F = np.zeros((n, 0))
     else:
         k = np.concatenate([np.exp(rng.uniform(np.log(1e-3), np.log(64), n - 6)),
@@ -140,6 +155,21 @@ def main():
             np.savez_compressed(os.path.join(HERE, f"fit_{model}.npz"), cfp=wl.cfp, meas=wl.meas,
                                 init=wl.init, fixp=wl.fixp, gs=gs, gs_best=best, gs_cost=bc,
                                 lm=lm, lm_iters=it, lm_cost=co)
+        print(model, "done")
+    # models added later draw from their own stream (earlier fixtures unchanged)
+    rng = np.random.default_rng(20240602)
+    makers = {"DiffusionTensor": synth.diffusion_tensor, "Ball_2_Sticks": synth.ball_2_sticks}
+    for model in ("DiffusionTensor", "Ball_2_Sticks"):
+        ref = Oracle(model, reference=True)
+        P, cfp, F = plugin_inputs(model, rng)
+        S, J = ref.signal(P, cfp, F, jac=True)
+        np.savez_compressed(os.path.join(HERE, f"plugin_{model}.npz"), params=P, cfp=cfp,
+                            fixp=F, signal=S, jacobian=J)
+        wl = makers[model](48, seed=77)
+        cfg = capi.model_cfg(model)
+        lm, it, su, co = ref.levmar(cfg, wl.meas, wl.init, wl.cfp, wl.fixp)
+        np.savez_compressed(os.path.join(HERE, f"fit_{model}.npz"), cfp=wl.cfp, meas=wl.meas,
+                            init=wl.init, fixp=wl.fixp, lm=lm, lm_iters=it, lm_cost=co)
         print(model, "done")
 
 

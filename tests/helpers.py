@@ -23,6 +23,14 @@ def b1s(nvox, seed=8219):
     return synth.ball_1_stick(nvox, seed=seed)
 
 
+def dt(nvox, seed=8219):
+    return synth.diffusion_tensor(nvox, seed=seed)
+
+
+def b2s(nvox, seed=8219):
+    return synth.ball_2_sticks(nvox, seed=seed)
+
+
 def angle_deg(th1, ph1, th2, ph2):
     """Angle between two axes (sign-insensitive), degrees."""
     v1 = np.stack([np.sin(th1) * np.cos(ph1), np.sin(th1) * np.sin(ph1), np.cos(th1)], -1)

@@ -18,7 +18,10 @@ def declared():
     return sorted(set(re.findall(r"\b(cdm_[a-z_0-9]+)\s*\(", text)))
 
 
-@pytest.mark.parametrize("model", ["Ball_1_Stick", "NODDI_Watson"])
+MODELS = ["Ball_1_Stick", "NODDI_Watson", "DiffusionTensor", "Ball_2_Sticks"]
+
+
+@pytest.mark.parametrize("model", MODELS)
 def test_exports(built, model):
     lib = C.CDLL(capi.lib_path(model))
     names = declared()
@@ -28,7 +31,7 @@ def test_exports(built, model):
     assert set(capi.EXPORTED) <= set(names)
 
 
-@pytest.mark.parametrize("model", ["Ball_1_Stick", "NODDI_Watson"])
+@pytest.mark.parametrize("model", MODELS)
 def test_model_info_matches_oracle(built, model):
     from tests.helpers import oracle
     lib = capi.load_library(model)

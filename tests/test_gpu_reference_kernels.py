@@ -5,15 +5,16 @@ sm_103a cubins where the CUDIMOT tree is available; skipped elsewhere).
 This pins the fitting loops to the reference implementation itself:
   * Ball_1_Stick: predicted signal, LM fit, BIC/AIC and MCMC posterior
     statistics (CUDIMOT's plugin is restated formula for formula);
+  * DiffusionTensor: LM fit; Ball_2_Sticks: MCMC posterior statistics;
   * NODDI_Watson: grid-search winners and LM fits. CUDIMOT's Watson plugin
-    carries its own numerical errors (documented in the design doc), so cost
+    carries its own numerical errors (see mymodels/NODDI_Watson), so cost
     comparisons use our FP64 model for both fits."""
 import numpy as np
 import pytest
 import torch
 
 from cudimot_gb300 import capi, synth
-from tests.helpers import angle_deg, b1s, oracle, watson
+from tests.helpers import angle_deg, b1s, b2s, dt, oracle, watson
 
 pytestmark = pytest.mark.gpu
 
@@ -126,3 +127,47 @@ def test_watson_gridsearch_and_levmar_vs_reference_kernels(built, cuda):
     assert np.mean(rel <= 1e-4) >= 0.98, np.quantile(rel, [0.5, 0.98, 1])
     ang = angle_deg(r2[:, 3], r2[:, 4], g2[:, 3], g2[:, 4])
     assert np.mean(ang <= 0.5) >= 0.98, np.quantile(ang, [0.5, 0.98, 1])
+
+
+def test_dt_levmar_vs_reference_kernels(built, cuda):
+    need("DiffusionTensor")
+    wl = dt(4000, seed=3)
+    cfg = capi.model_cfg("DiffusionTensor")
+    ref = rk.RefKernels("DiffusionTensor", 7)
+    ours = capi.Cudimot("DiffusionTensor", cfg)
+    pr, po = T(wl.init, cuda), T(wl.init, cuda)
+    ref.levmar(cfg, T(wl.meas, cuda), pr, T(wl.cfp, cuda), None)
+    ours.levmar(T(wl.meas, cuda), po, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    torch.cuda.synchronize()
+    r, g = pr.cpu().numpy(), po.cpu().numpy()
+    o = oracle("DiffusionTensor")
+    cr, cg = o.cost(wl.meas, r, wl.cfp), o.cost(wl.meas, g, wl.cfp)
+    rel = (cg - cr) / cr
+    assert np.mean(np.abs(rel) <= 1e-4) >= 0.995, np.quantile(rel, [0, 0.5, 0.99, 1])
+
+
+def test_b2s_mcmc_vs_reference_kernels(built, cuda):
+    need("Ball_2_Sticks")
+    wl = b2s(512, seed=9)
+    cfg = capi.model_cfg("Ball_2_Sticks", run_mcmc=1, nburn=500, njumps=2000, sampleevery=10)
+    o = oracle("Ball_2_Sticks")
+    start, _, _, _ = o.levmar(cfg, wl.meas, wl.init, wl.cfp, wl.fixp)
+    ref = rk.RefKernels("Ball_2_Sticks", 8)
+    ours = capi.Cudimot("Ball_2_Sticks", cfg)
+    ns = 200
+    sr = torch.zeros(wl.nvox, 8, ns, dtype=torch.float64, device=cuda)
+    so = torch.zeros_like(sr)
+    ref.mcmc(cfg, T(wl.meas, cuda), T(start, cuda), T(wl.cfp, cuda), None, sr)
+    ours.mcmc(T(wl.meas, cuda), T(start, cuda), T(wl.cfp, cuda), T(wl.fixp, cuda), so)
+    torch.cuda.synchronize()
+    r, g = sr.cpu().numpy(), so.cpu().numpy()
+    assert np.all(r[:, 2] >= r[:, 5]) and np.all(g[:, 2] >= g[:, 5])
+    for p in (0, 1, 2, 5):
+        def se(x):
+            bm = x.reshape(x.shape[0], 10, -1).mean(2)
+            return bm.std(1, ddof=1) / np.sqrt(10)
+        z = (g[:, p].mean(1) - r[:, p].mean(1)) / np.sqrt(se(g[:, p]) ** 2 + se(r[:, p]) ** 2 + 1e-30)
+        assert abs(np.median(z)) < 0.5, (p, np.median(z))
+        assert np.mean(np.abs(z) < 4) > 0.95, (p, np.mean(np.abs(z) < 4))
+        ratio = np.median(g[:, p].std(1) / np.maximum(r[:, p].std(1), 1e-30))
+        assert 0.8 < ratio < 1.25, (p, ratio)

@@ -3,6 +3,8 @@ fixtures produced by CUDIMOT's own plugins (tests/golden/make_golden.py).
 
 Ball_1_Stick: the restated plugin is CUDIMOT's formula for formula, so the
 signal matches exactly and the LM fit to rounding.
+DiffusionTensor, Ball_2_Sticks: restated with CUDIMOT's operation order
+(and its quirks), so signal, Jacobian and the LM fit match bit for bit.
 NODDI_Watson: CUDIMOT's FP64 plugin loses precision in two places (its
 Dawson-based closed-form SH coefficients for 0.4 < kappa < ~1.5, and the
 single-precision erf in its Legendre-Gaussian integrals at b = 1000); the
@@ -81,3 +83,16 @@ def test_watson_gridsearch_and_levmar_match_reference_plugin_fit(built):
     # same start, models differ only by CUDIMOT's precision loss
     rel = (co - f["lm_cost"]) / f["lm_cost"]
     assert np.median(np.abs(rel)) < 1e-4
+
+
+@pytest.mark.parametrize("model", ["DiffusionTensor", "Ball_2_Sticks"])
+def test_signal_jacobian_and_levmar_bit_exact_with_reference_plugin(built, model):
+    g = load(f"plugin_{model}.npz")
+    S, J = oracle(model).signal(g["params"], g["cfp"], g["fixp"], jac=True)
+    assert np.array_equal(S, g["signal"])
+    assert np.array_equal(J, g["jacobian"])
+    f = load(f"fit_{model}.npz")
+    p, it, _, co = oracle(model).levmar(capi.model_cfg(model), f["meas"], f["init"], f["cfp"],
+                                        f["fixp"])
+    assert np.array_equal(p, f["lm"])
+    assert np.array_equal(it, f["lm_iters"])
