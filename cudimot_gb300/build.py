@@ -146,6 +146,24 @@ def build_peak(force=False):
     return out, None
 
 
+def build_batch(force=False):
+    """Graph batching library over model contexts (include/cdm_batch.h)."""
+    src = os.path.join(CSRC, "batch", "cdm_batch.cpp")
+    hdr = os.path.join(ROOT, "include", "cdm_batch.h")
+    out = os.path.join(LIBDIR, "libcdm_batch.so")
+    newest = max(os.path.getmtime(src), os.path.getmtime(hdr))
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
+        return out, None
+    os.makedirs(LIBDIR, exist_ok=True)
+    cmd = [nvcc_path(), "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+           "-I", os.path.join(ROOT, "include"), src, "-o", out + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return out, (r.stdout + r.stderr)[-4000:]
+    os.replace(out + ".tmp", out)
+    return out, None
+
+
 def build_all(models=None, model_dirs=(), jobs=None, verbose=False, force=False):
     todo = [(os.path.join(MODELS, m), m) for m in (models or shipped_models())]
     todo += [(d, None) for d in model_dirs]
@@ -154,6 +172,7 @@ def build_all(models=None, model_dirs=(), jobs=None, verbose=False, force=False)
     with cf.ThreadPoolExecutor(jobs + 1) as ex:
         futs = {ex.submit(build_model, d, n, (), verbose, force): (d, n) for d, n in todo}
         futs[ex.submit(build_peak, force)] = ("peak", None)
+        futs[ex.submit(build_batch, force)] = ("batch", None)
         for f in cf.as_completed(futs):
             out, err = f.result()
             if err:

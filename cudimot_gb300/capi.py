@@ -210,6 +210,8 @@ def _declare(lib):
         "cdm_predicted_signal": [_vp, i, i, i, i, i, _vp, _vp, _vp, _vp, _vp],
         "cdm_fit": [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "cdm_fit_host": [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, i, i64],
+        "cdm_fit_reserve": [_vp, i, i],
+        "cdm_fit_enqueue": [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "cdm_synchronize": [_vp, _vp, i64],
         "cdm_get_stats": [_vp, C.POINTER(Stats)],
     }
@@ -227,7 +229,7 @@ EXPORTED = ("cdm_get_model_info", "cdm_default_cfg", "cdm_status_string", "cdm_l
             "cdm_parse_priors", "cdm_parse_grid", "cdm_parse_fixed", "cdm_read_cfp_list",
             "cdm_create", "cdm_destroy", "cdm_gridsearch", "cdm_levmar", "cdm_mcmc",
             "cdm_bic_aic", "cdm_predicted_signal", "cdm_fit", "cdm_fit_host",
-            "cdm_synchronize", "cdm_get_stats")
+            "cdm_fit_reserve", "cdm_fit_enqueue", "cdm_synchronize", "cdm_get_stats")
 
 
 def lib_path(model: str) -> str:
@@ -344,6 +346,14 @@ class Cudimot:
                                                p(samples), p(tau), p(pred), p(bic), p(aic),
                                                part_size, timeout_ms), "fit_host")
 
+    def fit_enqueue(self, meas, params, cfp, fixp, samples, tau=None, pred=None, bic=None, aic=None):
+        """The stage sequence as plain launches on the current stream."""
+        nv, nm = meas.shape
+        _check(self.lib, self.lib.cdm_fit_enqueue(self.ctx, nv, nm, _dptr(meas), _dptr(params),
+                                                  _dptr(cfp), _dptr(fixp), _dptr(samples),
+                                                  _dptr(tau), _dptr(pred), _dptr(bic), _dptr(aic),
+                                                  self._stream()), "fit_enqueue")
+
     def synchronize(self, timeout_ms=-1):
         _check(self.lib, self.lib.cdm_synchronize(self.ctx, self._stream(), timeout_ms), "synchronize")
 
@@ -363,3 +373,59 @@ def parse_priors(model: str, path: str, nparams: int):
     _check(lib, lib.cdm_parse_priors(path.encode(), C.byref(cfg.struct), C.cast(p_init, C.c_void_p),
                                      C.byref(given)), "parse_priors")
     return cfg, (list(p_init)[:nparams] if given.value else None)
+
+
+class Batch:
+    """Several fits - any mix of models, protocols and volumes - recorded as
+    parallel branches of one CUDA graph (include/cdm_batch.h) and launched
+    together on the current torch stream."""
+
+    def __init__(self):
+        path = os.path.join(LIBDIR, "libcdm_batch.so")
+        if not os.path.exists(path):
+            raise CdmError(f"{path} is not built (python -m cudimot_gb300.build)")
+        self.lib = C.CDLL(path)
+        vp, i = C.c_void_p, C.c_int
+        self.lib.cdm_batch_create.argtypes = [C.POINTER(vp)]
+        self.lib.cdm_batch_destroy.argtypes = [vp]
+        self.lib.cdm_batch_add.argtypes = [vp, vp, vp, vp, i, i] + [vp] * 10 + [C.c_double]
+        self.lib.cdm_batch_run.argtypes = [vp, vp]
+        self.lib.cdm_batch_last_error.restype = C.c_char_p
+        for f in ("cdm_batch_create", "cdm_batch_destroy", "cdm_batch_add", "cdm_batch_run"):
+            getattr(self.lib, f).restype = C.c_int
+        h = C.c_void_p()
+        self._check(self.lib.cdm_batch_create(C.byref(h)), "create")
+        self.h = h
+        self._keep = []
+
+    def _check(self, status, what):
+        if status != 0:
+            raise CdmError(f"batch {what}: {STATUS.get(status, status)}: "
+                           f"{self.lib.cdm_batch_last_error().decode(errors='replace')}")
+
+    def add(self, fit: Cudimot, meas, params, cfp, fixp, samples, tau=None, pred=None, bic=None,
+            aic=None, work=0.0):
+        nv, nm = meas.shape
+        self._keep.append((fit, meas, params, cfp, fixp, samples, tau, pred, bic, aic))
+        reserve = C.cast(fit.lib.cdm_fit_reserve, C.c_void_p)
+        enqueue = C.cast(fit.lib.cdm_fit_enqueue, C.c_void_p)
+        self._check(self.lib.cdm_batch_add(self.h, reserve, enqueue, fit.ctx, nv, nm, _dptr(meas),
+                                           _dptr(params), _dptr(cfp), _dptr(fixp), _dptr(samples),
+                                           _dptr(tau), _dptr(pred), _dptr(bic), _dptr(aic),
+                                           float(work)), "add")
+
+    def run(self):
+        import torch
+        self._check(self.lib.cdm_batch_run(self.h, C.c_void_p(torch.cuda.current_stream().cuda_stream)),
+                    "run")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cdm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -651,6 +651,41 @@ cdm_status cdm_fit(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* 
   return CDM_OK;
 }
 
+cdm_status cdm_fit_reserve(cdm_ctx* c, int nvox, int nmeas) {
+  CDM_TRY(check_common(c, nvox, nmeas, CDM_CFP_TSIZE, CDM_FIXP_TSIZE));
+  return reserve_fit(c, nvox, nmeas);
+}
+
+cdm_status cdm_fit_enqueue(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
+                           const double* CFP, const double* FixP, double* samples, double* tau,
+                           double* pred, double* BIC, double* AIC, void* stream) {
+  CDM_TRY(check_common(c, nvox, nmeas, CDM_CFP_TSIZE, CDM_FIXP_TSIZE));
+  if (!samples) return cdm_fail(CDM_BAD_ARG, "samples is null");
+  if (c->cfg.run_mcmc && (c->cfg.sampleevery <= 0 || c->cfg.njumps < c->cfg.sampleevery))
+    return cdm_fail(CDM_BAD_ARG, "MCMC must record at least one sample: --nj must be >= --se");
+  if (c->cfg.run_mcmc && c->cfg.rician && !tau) return cdm_fail(CDM_BAD_ARG, "rician needs tau");
+  if (nvox == 0) return CDM_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CDM_CUDA(cudaStreamIsCapturing(st, &cs));
+  if (cs == cudaStreamCaptureStatusActive) {
+    // no allocation may happen under capture: the shape must be reserved
+    const int pad = round_up(nmeas, 32);
+    size_t sig = 0;
+    for (int G : {1, 2, 4, 8, 16, 32})
+      sig = std::max(sig, (size_t)((nmeas + G - 1) / G) * std::max(nvox, 1) * G);
+    if (c->proto32_cap < (size_t)kNCOLS4 * pad || c->sig_cap < sig ||
+        c->gs_flags_cap < (size_t)std::max(nvox, 1))
+      return cdm_fail(CDM_BAD_ARG, "cdm_fit_enqueue under stream capture needs cdm_fit_reserve "
+                                   "for this shape first");
+  } else {
+    CDM_TRY(reserve_fit(c, nvox, nmeas));
+  }
+  CDM_CUDA(cudaMemsetAsync(c->counters, 0, 4 * sizeof(unsigned long long), st));
+  return fit_sequence(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau, pred, BIC, AIC, 0,
+                      st);
+}
+
 cdm_status cdm_synchronize(cdm_ctx* c, void* stream, int64_t timeout_ms) {
   if (!c) return cdm_fail(CDM_BAD_ARG, "null context");
   cudaStream_t st = (cudaStream_t)stream;

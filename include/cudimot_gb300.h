@@ -195,6 +195,19 @@ cdm_status cdm_fit_host(cdm_ctx* ctx, int nvox, int nmeas, const double* meas,
                         double* samples, double* tau, double* pred, double* BIC, double* AIC,
                         int part_size, int64_t timeout_ms);
 
+/* The stage sequence of cdm_fit recorded as plain launches on `stream`
+ * (no graph of its own), so that a caller can capture several contexts -
+ * other models, protocols or volumes - into one CUDA graph (cdm_batch.h).
+ * Same arguments and results as cdm_fit. Under stream capture it makes no
+ * allocation and returns CDM_BAD_ARG unless cdm_fit_reserve was called for
+ * this (nvox, nmeas) before the capture. Replaces, like cdm_fit, the
+ * per-part stage sequence of cudimot.cc:80-125. */
+cdm_status cdm_fit_reserve(cdm_ctx* ctx, int nvox, int nmeas);
+cdm_status cdm_fit_enqueue(cdm_ctx* ctx, int nvox, int nmeas, const double* meas,
+                           double* params, const double* CFP, const double* FixP,
+                           double* samples, double* tau, double* pred, double* BIC,
+                           double* AIC, void* stream);
+
 /* Wait for all work of the context on `stream`, polling at most timeout_ms
  * (< 0 = no limit); CDM_TIMEOUT if it did not finish. */
 cdm_status cdm_synchronize(cdm_ctx* ctx, void* stream, int64_t timeout_ms);

@@ -11,7 +11,11 @@ parity tests):
     cost difference <= 1e-5, >= 75 % of voxels not worse than 1e-4, mean cost
     within 1 %;
   * MCMC: posterior means agree within Monte Carlo error (z-scores) and
-    posterior SDs within 25 %.
+    posterior SDs within 25 %. The z-scores use batch-means standard errors
+    (10 batches), which understate the error of slowly mixing chains: two
+    FP64 oracle chains with different seeds give |z| < 4 for 99-100 % of
+    voxels on DiffusionTensor but only 90-99 % on Ball_2_Sticks (stick 2
+    under the ARD prior), so the bound is 95 % and 85 % respectively.
 """
 import numpy as np
 import pytest
@@ -96,9 +100,9 @@ def _z_and_ratio(g, r):
     return z, ratio
 
 
-@pytest.mark.parametrize("model,check", [("DiffusionTensor", (0, 1, 2, 3, 4, 5, 6)),
-                                         ("Ball_2_Sticks", (0, 1, 2, 5))])
-def test_mcmc_posterior_matches_oracle(built, cuda, model, check):
+@pytest.mark.parametrize("model,check,zfrac", [("DiffusionTensor", (0, 1, 2, 3, 4, 5, 6), 0.95),
+                                               ("Ball_2_Sticks", (0, 1, 2, 5), 0.85)])
+def test_mcmc_posterior_matches_oracle(built, cuda, model, check, zfrac):
     wl = MAKERS[model](256, seed=21)
     o = oracle(model)
     cfg = capi.model_cfg(model, run_mcmc=1, nburn=500, njumps=2000, sampleevery=10)
@@ -117,5 +121,5 @@ def test_mcmc_posterior_matches_oracle(built, cuda, model, check):
     for p in check:
         z, ratio = _z_and_ratio(g[:, p], r[:, p])
         assert abs(np.median(z)) < 0.5, (p, np.median(z))
-        assert np.mean(np.abs(z) < 4) > 0.95, (p, np.mean(np.abs(z) < 4))
+        assert np.mean(np.abs(z) < 4) > zfrac, (p, np.mean(np.abs(z) < 4))
         assert 0.8 < ratio < 1.25, (p, ratio)
