@@ -164,6 +164,25 @@ def build_batch(force=False):
     return out, None
 
 
+def build_mlp(force=False):
+    """Learned-initialiser library: tcgen05 GEMMs, training and inference
+    (include/cdm_mlp.h)."""
+    src = os.path.join(CSRC, "mlp", "cdm_mlp.cu")
+    deps = [src, os.path.join(CSRC, "mlp", "cdm_umma.cuh"), os.path.join(ROOT, "include", "cdm_mlp.h")]
+    out = os.path.join(LIBDIR, "libcdm_mlp.so")
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= max(map(os.path.getmtime, deps)):
+        return out, None
+    os.makedirs(LIBDIR, exist_ok=True)
+    cmd = [nvcc_path(), "-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-shared",
+           "-I", os.path.join(ROOT, "include"), "-I", os.path.join(CSRC, "mlp"), src,
+           "-o", out + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return out, (r.stdout + r.stderr)[-4000:]
+    os.replace(out + ".tmp", out)
+    return out, None
+
+
 def build_all(models=None, model_dirs=(), jobs=None, verbose=False, force=False):
     todo = [(os.path.join(MODELS, m), m) for m in (models or shipped_models())]
     todo += [(d, None) for d in model_dirs]
@@ -173,6 +192,7 @@ def build_all(models=None, model_dirs=(), jobs=None, verbose=False, force=False)
         futs = {ex.submit(build_model, d, n, (), verbose, force): (d, n) for d, n in todo}
         futs[ex.submit(build_peak, force)] = ("peak", None)
         futs[ex.submit(build_batch, force)] = ("batch", None)
+        futs[ex.submit(build_mlp, force)] = ("mlp", None)
         for f in cf.as_completed(futs):
             out, err = f.result()
             if err:

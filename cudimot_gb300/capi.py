@@ -388,7 +388,7 @@ class Batch:
         vp, i = C.c_void_p, C.c_int
         self.lib.cdm_batch_create.argtypes = [C.POINTER(vp)]
         self.lib.cdm_batch_destroy.argtypes = [vp]
-        self.lib.cdm_batch_add.argtypes = [vp, vp, vp, vp, i, i] + [vp] * 10 + [C.c_double]
+        self.lib.cdm_batch_add.argtypes = [vp, vp, vp, vp, i, i] + [vp] * 9 + [C.c_double]
         self.lib.cdm_batch_run.argtypes = [vp, vp]
         self.lib.cdm_batch_last_error.restype = C.c_char_p
         for f in ("cdm_batch_create", "cdm_batch_destroy", "cdm_batch_add", "cdm_batch_run"):

@@ -1,0 +1,317 @@
+// cdm_umma.cuh - BF16 GEMM on the 5th-generation tensor cores (tcgen05).
+//
+//   D[M x N] = A[M x K] * B[N x K]^T (+ epilogue),  A, B bf16 row-major with
+//   K contiguous (both K-major), FP32 accumulation in tensor memory.
+//
+// One CTA computes a 128 x BN tile (BN <= 256, a multiple of 16) with 128
+// threads:
+//   * warp 0, lane 0 - TMA producer: 128x64 (A) and BNx64 (B) bf16 boxes of
+//     the tensor maps, 128-byte swizzle, into a ring of kStages shared-memory
+//     stages, each completing a "full" mbarrier with its transaction bytes;
+//   * warp 1, lane 0 - MMA issuer: per stage four tcgen05.mma
+//     (kind::f16, M=128, N=BN, K=16) reading both operands through shared
+//     memory descriptors, accumulating into BN TMEM columns;
+//     tcgen05.commit frees the stage ("empty" mbarrier) and, after the last
+//     stage, signals the epilogue;
+//   * all four warps - epilogue: warp w owns TMEM lanes 32w..32w+31 (= tile
+//     rows), reads 32 columns at a time with tcgen05.ld, applies the fused
+//     epilogue and stores to global memory.
+// Every mbarrier wait is bounded (%globaltimer, 2 s): on expiry the thread
+// raises CDM_DEVERR_MMA_TIMEOUT in the error word and the CTA skips to the
+// TMEM release, so no wait can hang the GPU.
+#pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace cdm_mma {
+
+constexpr int kBM = 128;     // tile rows (TMEM lanes)
+constexpr int kBK = 64;      // bf16 elements per 128-byte swizzle row
+constexpr int kStages = 4;
+constexpr int kThreads = 128;
+constexpr int kErrTimeout = 0x4D4D41;  // "MMA"
+constexpr unsigned long long kWaitNs = 2000000000ull;
+
+enum Epilogue : int {
+  EPI_F32 = 0,        // out_f32[row][col] = acc
+  EPI_BIAS_F32 = 1,   // out_f32 = acc + bias[col]
+  EPI_BIAS_GELU = 2,  // z = acc + bias; out_bf16 = gelu(z); aux_bf16 = z; out_t (if set) = gelu(z)^T
+  EPI_DGELU = 3       // out_bf16 = acc * gelu'(aux_bf16[row][col]); out_t (if set) = same^T
+};
+
+struct gemm_args {
+  int M, N, K;             // valid sizes (rows of A, rows of B, reduction length)
+  float* out_f32;          // [M][ld_out]
+  __nv_bfloat16* out_bf16; // [M][ld_out]
+  __nv_bfloat16* aux_bf16; // [M][ld_out] (pre-activation: written by BIAS_GELU, read by DGELU)
+  __nv_bfloat16* out_t;    // [N][ld_t] transposed copy (optional)
+  const float* bias;       // [N]
+  int ld_out, ld_t;
+  int* err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long gtime() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the phase with the given parity; false on time-out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = gtime();
+  while (!mbar_try(bar, parity)) {
+    if (gtime() - t0 > kWaitNs) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, "
+      "{%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor, K-major operand in 128-byte swizzle
+// atoms of 8 rows x 128 bytes: start address >> 4 (bits 0-13), leading
+// byte offset (unused for swizzled K-major, 16 B), stride byte offset 1024 B
+// between 8-row groups (bits 32-45), descriptor version 1 (bits 46-47),
+// layout SWIZZLE_128B = 2 (bits 61-63).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)(16 >> 4) << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Instruction descriptor for kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
+// (bits 7-9 = 1, bits 10-12 = 1), both K-major (bits 15, 16 = 0),
+// N >> 3 in bits 17-22, M >> 4 in bits 24-28.
+__host__ __device__ constexpr uint32_t instr_desc_bf16(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(da), "l"(db), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float gelu(float z) {
+  return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f));
+}
+
+__device__ __forceinline__ float gelu_grad(float z) {
+  const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * __expf(-0.5f * z * z);
+  return cdf + z * pdf;
+}
+
+// TMEM columns to allocate for BN accumulator columns (power of two >= 32).
+__host__ __device__ constexpr uint32_t tmem_cols(int bn) {
+  return bn <= 32 ? 32u : bn <= 64 ? 64u : bn <= 128 ? 128u : 256u;
+}
+
+template <int BN>
+struct smem_layout {
+  static constexpr int kABytes = kBM * kBK * 2;  // 16 KB
+  static constexpr int kBBytes = BN * kBK * 2;
+  static constexpr int kStageBytes = kABytes + kBBytes;
+  // stages (1024-aligned), then barriers
+  static constexpr int kBarOffset = kStages * kStageBytes;
+  static constexpr int kBytes = kBarOffset + (2 * kStages + 1) * 8 + 16;
+  static constexpr int kAlloc = kBytes + 1024;  // slack for 1024-byte alignment
+};
+
+template <int BN, int EPI>
+__global__ void __launch_bounds__(kThreads, 1)
+    umma_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                     const __grid_constant__ gemm_args a) {
+  static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "UMMA N for M=128");
+  using L = smem_layout<BN>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem =
+      (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + L::kBarOffset);
+  uint64_t* empty = full + kStages;
+  uint64_t* done = empty + kStages;
+  uint32_t* tmem_slot = (uint32_t*)(done + 1);
+  __shared__ int abort_flag;
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
+  const int nk = (a.K + kBK - 1) / kBK;
+
+  if (threadIdx.x == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < kStages; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(tmem_cols(BN)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // TMA producer
+    for (int kt = 0; kt < nk; kt++) {
+      const int s = kt % kStages;
+      if (kt >= kStages && !mbar_wait(&empty[s], ((kt / kStages) - 1) & 1)) {
+        atomicExch(&abort_flag, 1);
+        break;
+      }
+      if (abort_flag) break;
+      unsigned char* st = smem + s * L::kStageBytes;
+      mbar_expect_tx(&full[s], L::kStageBytes);
+      tma_load_2d(st, &tmA, &full[s], kt * kBK, m0);
+      tma_load_2d(st + L::kABytes, &tmB, &full[s], kt * kBK, n0);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    constexpr uint32_t idesc = instr_desc_bf16(kBM, BN);
+    bool ok = true;
+    for (int kt = 0; kt < nk && ok; kt++) {
+      const int s = kt % kStages;
+      if (!mbar_wait(&full[s], (kt / kStages) & 1)) {
+        atomicExch(&abort_flag, 1);
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sa = smem_u32(smem + s * L::kStageBytes);
+      const uint32_t sb = sa + L::kABytes;
+#pragma unroll
+      for (int k = 0; k < kBK / 16; k++) {
+        // advance K by 16 bf16 = 32 bytes inside the 128-byte swizzle row
+        mma_bf16(tmem, smem_desc(sa + k * 32), smem_desc(sb + k * 32), idesc,
+                 (kt > 0 || k > 0) ? 1u : 0u);
+      }
+      mma_commit(&empty[s]);
+    }
+    if (ok) mma_commit(done);
+  }
+
+  // Epilogue: every warp waits for the accumulator.
+  bool ready = mbar_wait(done, 0);
+  __syncwarp();
+  // tcgen05.ld is warp-collective: the whole warp reads or none of it does
+  ready = __all_sync(0xFFFFFFFFu, ready);
+  if (!ready) atomicExch(&abort_flag, 1);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ready) {
+    const int row = m0 + warp * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      float v[32];
+      tmem_ld32(lane_base + (uint32_t)c0, v);
+      if (row < a.M) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+          const int col = n0 + c0 + j;
+          if (col >= a.N) continue;
+          const size_t o = (size_t)row * a.ld_out + col;
+          if (EPI == EPI_F32) {
+            a.out_f32[o] = v[j];
+          } else if (EPI == EPI_BIAS_F32) {
+            a.out_f32[o] = v[j] + a.bias[col];
+          } else if (EPI == EPI_BIAS_GELU) {
+            const float z = v[j] + a.bias[col];
+            const __nv_bfloat16 zb = __float2bfloat16(z);
+            const __nv_bfloat16 g = __float2bfloat16(gelu(__bfloat162float(zb)));
+            a.aux_bf16[o] = zb;
+            a.out_bf16[o] = g;
+            if (a.out_t) a.out_t[(size_t)col * a.ld_t + row] = g;
+          } else {  // EPI_DGELU
+            const float z = __bfloat162float(a.aux_bf16[o]);
+            const __nv_bfloat16 d = __float2bfloat16(v[j] * gelu_grad(z));
+            a.out_bf16[o] = d;
+            if (a.out_t) a.out_t[(size_t)col * a.ld_t + row] = d;
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (abort_flag && threadIdx.x == 0 && a.err) atomicExch(a.err, kErrTimeout);
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(tmem_cols(BN)));
+  }
+}
+
+}  // namespace cdm_mma
