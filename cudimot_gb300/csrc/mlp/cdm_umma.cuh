@@ -16,9 +16,9 @@
 //   * all four warps - epilogue: warp w owns TMEM lanes 32w..32w+31 (= tile
 //     rows), reads 32 columns at a time with tcgen05.ld, applies the fused
 //     epilogue and stores to global memory.
-// Every mbarrier wait is bounded (%globaltimer, 2 s): on expiry the thread
-// raises CDM_DEVERR_MMA_TIMEOUT in the error word and the CTA skips to the
-// TMEM release, so no wait can hang the GPU.
+// Every mbarrier wait is bounded (%globaltimer, 2 s): on expiry the CTA
+// writes kErrTimeout to the error word and skips to the TMEM release, so no
+// wait can hang the GPU.
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int j = 0; j < 32; j++) {
           const int col = n0 + c0 + j;
-          if (col >= a.N) continue;
+          if (c0 + j >= BN || col >= a.N) continue;  // BN need not be a multiple of 32
           const size_t o = (size_t)row * a.ld_out + col;
           if (EPI == EPI_F32) {
             a.out_f32[o] = v[j];
