@@ -211,6 +211,12 @@ def _declare(lib):
         "cdm_fit": [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "cdm_fit_host": [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, i, i64],
         "cdm_fit_reserve": [_vp, i, i],
+        "cdm_mcmc_seeded": [_vp, i, i, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+        "cdm_synth_signals": [_vp, i, i, _vp, _vp, _vp, C.c_double, C.c_double, C.c_uint64, i,
+                              _vp, _vp, _vp, i, _vp],
+        "cdm_mlp_head_info": [C.POINTER(i), C.POINTER(i), _vp],
+        "cdm_mlp_targets": [_vp, i, _vp, _vp, _vp],
+        "cdm_mlp_decode": [_vp, i, _vp, i, _vp, _vp, _vp],
         "cdm_fit_enqueue": [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "cdm_synchronize": [_vp, _vp, i64],
         "cdm_get_stats": [_vp, C.POINTER(Stats)],
@@ -229,7 +235,9 @@ EXPORTED = ("cdm_get_model_info", "cdm_default_cfg", "cdm_status_string", "cdm_l
             "cdm_parse_priors", "cdm_parse_grid", "cdm_parse_fixed", "cdm_read_cfp_list",
             "cdm_create", "cdm_destroy", "cdm_gridsearch", "cdm_levmar", "cdm_mcmc",
             "cdm_bic_aic", "cdm_predicted_signal", "cdm_fit", "cdm_fit_host",
-            "cdm_fit_reserve", "cdm_fit_enqueue", "cdm_synchronize", "cdm_get_stats")
+            "cdm_fit_reserve", "cdm_fit_enqueue", "cdm_synchronize", "cdm_get_stats",
+            "cdm_mcmc_seeded", "cdm_synth_signals", "cdm_mlp_head_info", "cdm_mlp_targets",
+            "cdm_mlp_decode")
 
 
 def lib_path(model: str) -> str:
@@ -345,6 +353,41 @@ class Cudimot:
         _check(self.lib, self.lib.cdm_fit_host(self.ctx, nv, nm, p(meas), p(params), p(cfp), p(fixp),
                                                p(samples), p(tau), p(pred), p(bic), p(aic),
                                                part_size, timeout_ms), "fit_host")
+
+    def mcmc_seeded(self, meas, params, cfp, fixp, samples, prop_sd, tau=None):
+        nv, nm, ct, ft = self._sizes(meas)
+        _check(self.lib, self.lib.cdm_mcmc_seeded(self.ctx, nv, nm, ct, ft, _dptr(meas), _dptr(params),
+                                                  _dptr(cfp), _dptr(fixp), _dptr(samples), _dptr(tau),
+                                                  _dptr(prop_sd), self._stream()), "mcmc_seeded")
+
+    def synth(self, cfp, params, fixp, snr=(20.0, 20.0), seed=1, b_col=3, meas=None, s0=None,
+              x=None):
+        """Synthetic noisy signals from the plugin (see cdm_synth_signals);
+        x is a bf16 CUDA tensor [nvox][x_ld]."""
+        nv = params.shape[0]
+        nm = cfp.shape[0]
+        xp = None if x is None else C.c_void_p(x.data_ptr())
+        _check(self.lib, self.lib.cdm_synth_signals(
+            self.ctx, nv, nm, _dptr(cfp), _dptr(params), _dptr(fixp), float(snr[0]), float(snr[1]),
+            int(seed), b_col, _dptr(meas), _dptr(s0), xp, 0 if x is None else x.shape[1],
+            self._stream()), "synth_signals")
+
+    def mlp_head(self):
+        n_mu, n_sig = C.c_int(), C.c_int()
+        g = (C.c_int * 16)()
+        _check(self.lib, self.lib.cdm_mlp_head_info(C.byref(n_mu), C.byref(n_sig),
+                                                    C.cast(g, C.c_void_p)), "mlp_head_info")
+        return n_mu.value, n_sig.value, list(g)[:n_mu.value]
+
+    def mlp_targets(self, params, targets):
+        _check(self.lib, self.lib.cdm_mlp_targets(self.ctx, params.shape[0], _dptr(params),
+                                                  C.c_void_p(targets.data_ptr()), self._stream()),
+               "mlp_targets")
+
+    def mlp_decode(self, out, params, prop_sd=None):
+        _check(self.lib, self.lib.cdm_mlp_decode(self.ctx, out.shape[0], C.c_void_p(out.data_ptr()),
+                                                 out.shape[1], _dptr(params), _dptr(prop_sd),
+                                                 self._stream()), "mlp_decode")
 
     def fit_enqueue(self, meas, params, cfp, fixp, samples, tau=None, pred=None, bic=None, aic=None):
         """The stage sequence as plain launches on the current stream."""

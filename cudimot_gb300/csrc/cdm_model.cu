@@ -16,6 +16,7 @@
 #include "cdm_levmar.cuh"
 #include "cdm_mcmc.cuh"
 #include "cdm_postfit.cuh"
+#include "cdm_synth.cuh"
 
 #include "cdm_host.h"
 #include "cudimot_gb300.h"
@@ -96,6 +97,7 @@ struct cdm_ctx {
   size_t gs_best_cap = 0;
   int* err = nullptr;
   unsigned long long* counters = nullptr;  // [0] lm passes [1] lm successes [2] gs rechecks
+  const double* prop_sd = nullptr;          // initial MCMC proposal widths of the next run_mcmc
   // host-buffer path
   double* h_meas = nullptr; size_t h_meas_cap = 0;
   double* h_params = nullptr; size_t h_params_cap = 0;
@@ -333,6 +335,7 @@ cdm_status launch_mcmc(cdm_ctx* c, int nvox, int nmeas, double* params, const do
   a.seed = c->cfg.seed;
   a.stream = (uint32_t)c->cfg.id_part;
   a.voxel_offset = voxel_offset;
+  a.prop_sd = c->prop_sd;
   const size_t sm = proto_bytes(c->nmeas_pad);
   CDM_TRY(set_smem(cdm_mcmc_kernel<G, RICIAN>, sm));
   cdm_mcmc_kernel<G, RICIAN><<<blocks_for(nvox, G), CDM_NT, sm, st>>>(a);
@@ -581,6 +584,100 @@ cdm_status cdm_mcmc(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_size
   CDM_TRY(check_common(c, nvox, nmeas, CFP_size, FixP_size));
   return run_mcmc(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau_samples, 0,
                   (cudaStream_t)stream);
+}
+
+cdm_status cdm_mcmc_seeded(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_size,
+                           const double* meas, double* params, const double* CFP,
+                           const double* FixP, double* samples, double* tau_samples,
+                           const double* prop_sd, void* stream) {
+  CDM_TRY(check_common(c, nvox, nmeas, CFP_size, FixP_size));
+  c->prop_sd = prop_sd;
+  const cdm_status s = run_mcmc(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau_samples, 0,
+                                (cudaStream_t)stream);
+  c->prop_sd = nullptr;
+  return s;
+}
+
+cdm_status cdm_synth_signals(cdm_ctx* c, int nvox, int nmeas, const double* CFP,
+                             const double* params, const double* FixP, double snr_lo,
+                             double snr_hi, uint64_t seed, int b_col, double* meas,
+                             double* s0_est, void* x, int x_ld, void* stream) {
+  CDM_TRY(check_common(c, nvox, nmeas, CDM_CFP_TSIZE, CDM_FIXP_TSIZE));
+  if (!CFP || !params || (CDM_FIXP_TSIZE > 0 && !FixP)) return cdm_fail(CDM_BAD_ARG, "null array");
+  if (b_col >= kNCOLS) return cdm_fail(CDM_BAD_ARG, "b_col beyond the protocol columns");
+  if (x && x_ld < nmeas) return cdm_fail(CDM_BAD_ARG, "x_ld < nmeas");
+  if (!(snr_lo > 0.0) || snr_hi < snr_lo) return cdm_fail(CDM_BAD_ARG, "bad SNR range");
+  cudaStream_t st = (cudaStream_t)stream;
+  CDM_TRY(reserve_fit(c, std::max(nvox, 1), nmeas));
+  CDM_TRY(prep_protocol(c, nmeas, CFP, st));
+  if (nvox == 0) return CDM_OK;
+  cdm_synth_args a;
+  a.nvox = nvox;
+  a.nmeas = nmeas;
+  a.nmeas_pad = c->nmeas_pad;
+  a.fixp_tsize = CDM_FIXP_TSIZE;
+  a.b_col = b_col;
+  a.x_ld = x_ld;
+  a.proto_bytes = (uint32_t)proto_bytes(c->nmeas_pad);
+  a.proto = c->proto32;
+  a.params = params;
+  a.fixp = FixP;
+  a.snr_lo = (float)snr_lo;
+  a.snr_hi = (float)snr_hi;
+  a.seed = seed;
+  a.meas = meas;
+  a.s0_est = s0_est;
+  a.x = (__nv_bfloat16*)x;
+  a.err = c->err;
+  const size_t sm = proto_bytes(c->nmeas_pad);
+  CDM_TRY(set_smem(cdm_synth_kernel, sm));
+  cdm_synth_kernel<<<(nvox + CDM_NT / 32 - 1) / (CDM_NT / 32), CDM_NT, sm, st>>>(a);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+cdm_status cdm_mlp_head_info(int* n_mu, int* n_sig, int* group) {
+#ifdef CDM_MLP_HEAD
+  const int g[CDM_MLP_NMU] = CDM_MLP_GROUPS;
+  if (n_mu) *n_mu = CDM_MLP_NMU;
+  if (n_sig) *n_sig = CDM_MLP_NSIG;
+  if (group)
+    for (int j = 0; j < CDM_MLP_NMU; j++) group[j] = g[j];
+  return CDM_OK;
+#else
+  (void)n_mu; (void)n_sig; (void)group;
+  return cdm_fail(CDM_NOT_SUPPORTED, "this plugin defines no learned-initialiser head");
+#endif
+}
+
+cdm_status cdm_mlp_targets(cdm_ctx* c, int n, const double* params, float* targets, void* stream) {
+#ifdef CDM_MLP_HEAD
+  if (!c || n < 0 || !params || !targets) return cdm_fail(CDM_BAD_ARG, "bad argument");
+  if (n == 0) return CDM_OK;
+  cdm_mlp_encode_kernel<<<std::min((n + 255) / 256, 152 * 8), 256, 0, (cudaStream_t)stream>>>(
+      params, n, targets);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+#else
+  (void)c; (void)n; (void)params; (void)targets; (void)stream;
+  return cdm_fail(CDM_NOT_SUPPORTED, "this plugin defines no learned-initialiser head");
+#endif
+}
+
+cdm_status cdm_mlp_decode(cdm_ctx* c, int n, const float* out, int ld, double* params,
+                          double* prop_sd, void* stream) {
+#ifdef CDM_MLP_HEAD
+  if (!c || n < 0 || !out || !params || ld < CDM_MLP_NMU + CDM_MLP_NSIG)
+    return cdm_fail(CDM_BAD_ARG, "bad argument");
+  if (n == 0) return CDM_OK;
+  cdm_mlp_decode_kernel<<<std::min((n + 255) / 256, 152 * 8), 256, 0, (cudaStream_t)stream>>>(
+      out, ld, n, params, prop_sd);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+#else
+  (void)c; (void)n; (void)out; (void)ld; (void)params; (void)prop_sd; (void)stream;
+  return cdm_fail(CDM_NOT_SUPPORTED, "this plugin defines no learned-initialiser head");
+#endif
 }
 
 cdm_status cdm_bic_aic(cdm_ctx* c, int nvox, int nmeas, int nsamples, int CFP_size, int FixP_size,

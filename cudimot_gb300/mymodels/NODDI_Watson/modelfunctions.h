@@ -383,3 +383,62 @@ MACRO void Partial_Derivatives(int npar, T* P, T* CFP, T* FixP, T* derivatives) 
 MACRO void FixConstraintsLM(int npar, T* P) {}
 
 MACRO T custom_priors(int id_p, T* P, int nmeas, T* CFP, T* FixP) { return (T)0.0; }
+
+// ---------------------------------------------------------------------------
+// Optional hooks of the learned initialiser (no counterpart in CUDIMOT).
+// Network head: 8 means = (fiso, fintra, log kappa, and the five independent
+// entries vx^2, vy^2, vx vy, vx vz, vy vz of the fibre dyad v v^T, which is
+// sign-free: v and -v are the same fibre), 4 log-stds: one per scalar and
+// one shared by the dyad entries.
+#define CDM_MLP_HEAD 1
+#define CDM_MLP_NMU 8
+#define CDM_MLP_NSIG 4
+#define CDM_MLP_GROUPS {0, 1, 2, 3, 3, 3, 3, 3}
+
+template <typename T>
+__host__ __device__ inline void MLP_Encode(const T* P, float* t) {
+  const double st = sin((double)P[3]), ct = cos((double)P[3]);
+  const double vx = st * cos((double)P[4]), vy = st * sin((double)P[4]), vz = ct;
+  t[0] = (float)P[0];
+  t[1] = (float)P[1];
+  t[2] = (float)log(fmax((double)P[2], 1e-3));
+  t[3] = (float)(vx * vx);
+  t[4] = (float)(vy * vy);
+  t[5] = (float)(vx * vy);
+  t[6] = (float)(vx * vz);
+  t[7] = (float)(vy * vz);
+}
+
+// Parameters inside the bounds and MCMC proposal widths from the network's
+// outputs. The fibre is the principal eigenvector of the predicted dyad
+// (power iteration on dyad + I, which keeps the top eigenvalue on top even
+// when the prediction is slightly indefinite).
+template <typename T>
+__host__ __device__ inline void MLP_Decode(const float* mu, const float* ls, T* P, T* sd) {
+  const double lo = 1e-3, hi = 1.0 - 1e-3;
+  P[0] = (T)fmin(fmax((double)mu[0], lo), hi);
+  P[1] = (T)fmin(fmax((double)mu[1], lo), hi);
+  const double kappa = fmin(fmax(exp((double)mu[2]), 0.05), 63.0);
+  P[2] = (T)kappa;
+  const double a = mu[3], b = mu[4], c = mu[5], d = mu[6], e = mu[7];
+  const double M[3][3] = {{a + 1.0, c, d}, {c, b + 1.0, e}, {d, e, 2.0 - a - b}};
+  double v[3] = {0.0, 0.0, 0.0};
+  const double dg[3] = {a, b, 1.0 - a - b};
+  v[dg[0] >= dg[1] && dg[0] >= dg[2] ? 0 : (dg[1] >= dg[2] ? 1 : 2)] = 1.0;
+  for (int it = 0; it < 32; it++) {
+    double w[3];
+    for (int i = 0; i < 3; i++) w[i] = M[i][0] * v[0] + M[i][1] * v[1] + M[i][2] * v[2];
+    const double n = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    if (!(n > 0.0)) break;
+    for (int i = 0; i < 3; i++) v[i] = w[i] / n;
+  }
+  const double th = acos(fmin(fmax(v[2], -1.0), 1.0));
+  P[3] = (T)th;
+  P[4] = (T)atan2(v[1], v[0]);
+  const double sang = fmin(fmax(exp((double)ls[3]), 1e-3), 0.5);
+  sd[0] = (T)fmin(fmax(exp((double)ls[0]), 1e-4), 0.5);
+  sd[1] = (T)fmin(fmax(exp((double)ls[1]), 1e-4), 0.5);
+  sd[2] = (T)fmin(fmax(kappa * exp((double)ls[2]), 1e-3), 16.0);
+  sd[3] = (T)sang;
+  sd[4] = (T)fmin(sang / fmax(sin(th), 0.1), 1.0);
+}

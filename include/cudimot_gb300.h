@@ -208,6 +208,38 @@ cdm_status cdm_fit_enqueue(cdm_ctx* ctx, int nvox, int nmeas, const double* meas
                            double* samples, double* tau, double* pred, double* BIC,
                            double* AIC, void* stream);
 
+/* As cdm_mcmc, with each voxel's initial proposal widths prop_sd
+ * [nvox][NPARAMS] (CUDIMOT starts from |P|/10, MCMC.cu:474-476; null gives
+ * that). Used by the learned initialiser to seed the proposal scales. */
+cdm_status cdm_mcmc_seeded(cdm_ctx* ctx, int nvox, int nmeas, int CFP_size, int FixP_size,
+                           const double* meas, double* params, const double* CFP,
+                           const double* FixP, double* samples, double* tau_samples,
+                           const double* prop_sd, void* stream);
+
+/* Synthetic acquisitions from the model itself (training data of the
+ * learned initialiser; no CUDIMOT counterpart): for each voxel the
+ * plugin's Predicted_Signal at params [nvox][NPARAMS] / FixP (true values),
+ * Rician noise with sigma = mean clean b = 0 signal / SNR, SNR uniform in
+ * [snr_lo, snr_hi] per voxel, Philox-keyed by (seed, voxel, measurement).
+ * b_col: the CFP column holding b (-1: none; then sigma uses the largest
+ * clean signal). Outputs (each optional): meas [nvox][nmeas], s0_est [nvox]
+ * = mean noisy b = 0 signal, x bf16 [nvox][x_ld] = meas / s0_est. */
+cdm_status cdm_synth_signals(cdm_ctx* ctx, int nvox, int nmeas, const double* CFP,
+                             const double* params, const double* FixP, double snr_lo,
+                             double snr_hi, uint64_t seed, int b_col, double* meas,
+                             double* s0_est, void* x, int x_ld, void* stream);
+
+/* The plugin's learned-initialiser head (optional hooks MLP_Encode /
+ * MLP_Decode; CDM_NOT_SUPPORTED without them): number of means, of
+ * log-stds, and the log-std group of each mean; network targets (float
+ * [n][n_mu]) from parameters; parameters and MCMC proposal widths
+ * [n][NPARAMS] from network outputs (float [n][ld], means then log-stds). */
+cdm_status cdm_mlp_head_info(int* n_mu, int* n_sig, int* group);
+cdm_status cdm_mlp_targets(cdm_ctx* ctx, int n, const double* params, float* targets,
+                           void* stream);
+cdm_status cdm_mlp_decode(cdm_ctx* ctx, int n, const float* out, int ld, double* params,
+                          double* prop_sd, void* stream);
+
 /* Wait for all work of the context on `stream`, polling at most timeout_ms
  * (< 0 = no limit); CDM_TIMEOUT if it did not finish. */
 cdm_status cdm_synchronize(cdm_ctx* ctx, void* stream, int64_t timeout_ms);
