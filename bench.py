@@ -52,6 +52,16 @@ def parse():
                     help="run the preceding stages, then one launch of this stage (for ncu)")
     ap.add_argument("--nburn", type=int, default=NBURN)
     ap.add_argument("--njumps", type=int, default=NJUMPS)
+    ap.add_argument("--workload", default="noddi_watson",
+                    choices=["noddi_watson", "ball_1_stick_lm", "heterogeneous", "learned_init"],
+                    help="noddi_watson: the headline (200k voxels GS->LM->MCMC); "
+                         "ball_1_stick_lm: 10k voxels plain LM; heterogeneous: DiffusionTensor "
+                         "400k + Ball_2_Sticks 300k + NODDI_Watson 500k LM+MCMC in one graph; "
+                         "learned_init: network-initialised vs grid-initialised NODDI_Watson")
+    ap.add_argument("--train-signals", type=int, default=20_000_000)
+    ap.add_argument("--lm-targets", type=int, default=1_000_000)
+    ap.add_argument("--epochs", type=int, default=2)
+    ap.add_argument("--eval-voxels", type=int, default=1_000_000)
     return ap.parse_args()
 
 
@@ -69,7 +79,7 @@ def workload_cfg(grid=True):
     return cfg
 
 
-def make_workload(nvox, seed, dev):
+def make_workload(nvox, seed, dev, snr=20.0):
     """Synthetic C1 inputs; the clean signal comes from the library itself."""
     import torch
     from cudimot_gb300 import capi, synth
@@ -84,7 +94,7 @@ def make_workload(nvox, seed, dev):
     torch.cuda.synchronize()
     clean = clean.cpu().numpy()
     lib.close()
-    meas = synth.rician(clean, S0 / 20.0, r_noise)
+    meas = synth.rician(clean, S0 / snr, r_noise)
     b0 = cfp[:, 3] == 0
     fixp = meas[:, b0].mean(axis=1, keepdims=True)
     _, _, _, th, ph = synth.dti_init(meas, cfp)
@@ -254,11 +264,249 @@ def profiled_traffic():
     return None
 
 
+def timed_events(fn, steps, flush=None):
+    """CUDA-event time (ms) of each call of fn on the current stream; flush
+    (untimed) before each call when given."""
+    import torch
+    st = torch.cuda.current_stream()
+    out = []
+    for _ in range(steps):
+        if flush is not None:
+            flush()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        out.append(e0.elapsed_time(e1))
+    return out
+
+
+def base_line(metric, value, unit, a, ms, config, clocks, dtype="f32 model / f64 sums", **kw):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": a.steps,
+         "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+         "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": config,
+         "clocks": clocks}
+    d.update(kw)
+    return d
+
+
+def bench_b1s_lm(a, dev):
+    """Ball & 1 Stick plain LM, 10,000 voxels x 134 measurements, LM <= 200
+    iterations from a log-linear tensor fit. Inputs (5 MB) fit in L2, so a
+    256 MB buffer is written before every timed step."""
+    import torch
+    from cudimot_gb300 import capi, synth
+    n = 10_000 if a.nvox == NVOX else a.nvox
+    wl = synth.ball_1_stick(n)
+    cfg = capi.model_cfg("Ball_1_Stick", iter_levmar=200)
+    lib = capi.Cudimot("Ball_1_Stick", cfg)
+    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
+    m, c, f, p0 = t(wl.meas), t(wl.cfp), t(wl.fixp), t(wl.init)
+    p = p0.clone()
+    s = torch.zeros(n, 5, 1, dtype=torch.float64, device=dev)
+    junk = torch.empty(64 << 20, dtype=torch.float32, device=dev)
+
+    def flush():
+        junk.fill_(1.0)
+        p.copy_(p0)
+
+    def step():
+        lib.fit(m, p, c, f, s)
+
+    timed_events(step, a.warmup, flush)
+    with ClockSampler(dev.index or 0) as clk:
+        ms = timed_events(step, max(a.steps, 10), flush)
+    ms_step = statistics.median(ms)
+    st = lib.stats()
+    # e2e: host arrays through cdm_fit_host
+    hm, hc, hf = wl.meas.copy(), wl.cfp.copy(), wl.fixp.copy()
+    hs = np.zeros((n, 5, 1))
+    e2e = []
+    for _ in range(3):
+        hp = wl.init.copy()
+        t0 = time.perf_counter()
+        lib.fit_host(hm, hp, hc, hf, hs)
+        e2e.append(time.perf_counter() - t0)
+    line = base_line("voxels/s fitted (plain LM)", n / (ms_step / 1e3), "voxels/s", a, ms_step,
+                     {"workload": "ball_1_stick_lm", "model": "Ball_1_Stick", "nvox": n, "nmeas": 134,
+                      "iter_levmar": 200, "l2": "256 MB written before each step (inputs fit in L2)"},
+                     clk.summary(), lm_iterations_per_voxel=st.lm_iterations / n,
+                     gpu_launches=3 * max(a.steps, 10),
+                     e2e={"value": n / statistics.median(e2e), "unit": "voxels/s",
+                          "h2d_bytes_per_step": int(hm.nbytes + hc.nbytes + wl.init.nbytes),
+                          "d2h_bytes_per_step": int(wl.init.nbytes + hs.nbytes)})
+    print(json.dumps(line))
+
+
+def bench_heterogeneous(a, dev):
+    """Three volumes, three models, three protocols - DiffusionTensor 400k x
+    71, Ball_2_Sticks 300k x 134, NODDI_Watson 500k x 288 (SNR 25), LM +
+    MCMC (1250 + 1250, every 25th) - recorded as branches of one CUDA graph
+    (cdm_batch) and launched once per step; the same fits run one model
+    after another are timed too."""
+    import torch
+    from cudimot_gb300 import capi, synth
+    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
+    scale = a.nvox / NVOX if a.nvox != NVOX else 1.0
+    vols = []
+    wdt = synth.diffusion_tensor(int(400_000 * scale), snr=25.0)
+    wb2 = synth.ball_2_sticks(int(300_000 * scale), snr=25.0)
+    cfp, meas, fixp, init, _ = make_workload(int(500_000 * scale), 8219, dev, snr=25.0)
+    for model, m, c, f, i in (("DiffusionTensor", wdt.meas, wdt.cfp, wdt.fixp, wdt.init),
+                              ("Ball_2_Sticks", wb2.meas, wb2.cfp, wb2.fixp, wb2.init),
+                              ("NODDI_Watson", meas, cfp, fixp, init)):
+        cfg = capi.model_cfg(model, run_mcmc=1, nburn=NBURN, njumps=NJUMPS, sampleevery=SE)
+        npar = i.shape[1]
+        d = dict(model=model, lib=capi.Cudimot(model, cfg), meas=t(m), cfp=t(c), fixp=t(f),
+                 init=t(i), params=t(i),
+                 samples=torch.zeros(m.shape[0], npar, NJUMPS // SE, dtype=torch.float64, device=dev))
+        vols.append(d)
+    total = sum(v["meas"].shape[0] for v in vols)
+    batch = capi.Batch()
+    for v in vols:
+        batch.add(v["lib"], v["meas"], v["params"], v["cfp"], v["fixp"], v["samples"],
+                  work=float(v["meas"].numel()) * v["init"].shape[1])
+
+    def reset():
+        for v in vols:
+            v["params"].copy_(v["init"])
+
+    def run_batch():
+        batch.run()
+
+    def run_seq():
+        for v in vols:
+            v["lib"].fit(v["meas"], v["params"], v["cfp"], v["fixp"], v["samples"])
+
+    timed_events(run_batch, a.warmup, reset)
+    timed_events(run_seq, 1, reset)
+    with ClockSampler(dev.index or 0) as clk:
+        ms = timed_events(run_batch, a.steps, reset)
+    ms_seq = timed_events(run_seq, a.steps, reset)
+    ms_b, ms_s = statistics.median(ms), statistics.median(ms_seq)
+    line = base_line("voxels/s fitted (LM+MCMC), heterogeneous batch", total / (ms_b / 1e3),
+                     "voxels/s", a, ms_b,
+                     {"workload": "heterogeneous_lm_mcmc",
+                      "volumes": [{"model": v["model"], "nvox": int(v["meas"].shape[0]),
+                                   "nmeas": int(v["meas"].shape[1])} for v in vols],
+                      "nburn": NBURN, "njumps": NJUMPS, "sampleevery": SE,
+                      "l2": "inputs larger than L2 (no flush)",
+                      "launch": "one CUDA graph, one branch per volume"},
+                     clk.summary(), sequential={"value": total / (ms_s / 1e3), "ms_per_step": ms_s},
+                     gpu_launches=sum(9 for _ in vols) * a.steps)
+    print(json.dumps(line))
+
+
+def bench_learned(a, dev):
+    """Network-initialised vs grid-initialised NODDI-Watson fits on the same
+    GPU. The network (288 -> 256 -> 256 -> 256 -> 12, BF16 tensor cores) is
+    trained first on --train-signals synthetic signals (SNR U(10,50)) plus
+    --lm-targets grid-search+LM fits; then --eval-voxels voxels at SNR 20 are
+    fitted both ways, each LM -> MCMC (1250 + 1250, every 25th). Voxels
+    whose surrogate-path LM cost exceeds the plain path's by > 1 % are
+    refit by grid search + LM (counted in the surrogate time)."""
+    import torch
+    from cudimot_gb300 import capi, synth
+    from cudimot_gb300.learned import LearnedInit
+    rng = np.random.default_rng(8219)
+    cfp = synth.protocol(18, [(90, 1000.0), (90, 2000.0), (90, 3000.0)], rng)
+    li = LearnedInit(MODEL, cfp, grid=synth.WATSON_GRID, seed=8219, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x, tg = li.make_training_set(a.train_signals, a.lm_targets)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    li.train(x, tg, epochs=a.epochs, batch=4096)
+    n_train = x.shape[0]
+    del x, tg
+    steps = a.epochs * (n_train // 4096)
+    flop_sample = 2 * sum(d0 * d1 for d0, d1 in zip(li.net.dims()[:-1], li.net.dims()[1:]))
+    n = a.eval_voxels
+    d = li.synth(n, seed=4242, snr=(20.0, 20.0), meas=True)
+    meas, s0, truth = d["meas"], d["s0"], d["params"].cpu().numpy()
+    _, _, _, th, ph = synth.dti_init(meas.cpu().numpy(), cfp)
+    init = li._default_init(n)
+    init[:, 3] = torch.as_tensor(th, device=dev)
+    init[:, 4] = torch.as_tensor(ph, device=dev)
+    fit_cfg = capi.model_cfg(MODEL, run_mcmc=1, nburn=NBURN, njumps=NJUMPS, sampleevery=SE)
+    gs_cfg = capi.model_cfg(MODEL, grid=synth.WATSON_GRID, run_mcmc=1, nburn=NBURN, njumps=NJUMPS,
+                            sampleevery=SE)
+    plain = capi.Cudimot(MODEL, gs_cfg)
+    ns = NJUMPS // SE
+    sp = torch.zeros(n, 5, ns, dtype=torch.float64, device=dev)
+    ss = torch.zeros_like(sp)
+    st = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    # scratch buffers and the network's inference buffers before timing
+    plain.fit_reserve(n, 288)
+    ctx = li.contexts(fit_cfg, n)
+    li.predict(meas, s0)
+    torch.cuda.synchronize()
+    # grid-initialised path: GS -> LM | judge cost | MCMC
+    with ClockSampler(dev.index or 0) as clk:
+        p = init.clone()
+        e = [ev() for _ in range(4)]
+        e[0].record(st)
+        plain.gridsearch(meas, p, li.cfp, s0)
+        plain.levmar(meas, p, li.cfp, s0)
+        e[1].record(st)
+        judge = li.cost(meas, p, s0)
+        e[2].record(st)
+        plain.mcmc(meas, p, li.cfp, s0, sp)
+        e[3].record(st)
+        torch.cuda.synchronize()
+        t_plain = e[0].elapsed_time(e[1]) + e[2].elapsed_time(e[3])
+        # network-initialised path: network -> LM -> refit -> MCMC
+        q = None
+        f0, f1 = ev(), ev()
+        f0.record(st)
+        q, info = li.fit(meas, s0, fit_cfg, ss, judge_cost=judge, margin=0.01, ctx=ctx)
+        f1.record(st)
+        torch.cuda.synchronize()
+        t_sur = f0.elapsed_time(f1)
+    gp, gs_ = sp.cpu().numpy().mean(2), ss.cpu().numpy().mean(2)
+
+    def err(m):
+        ang = np.degrees(np.arccos(np.clip(np.abs(
+            np.sin(m[:, 3]) * np.sin(truth[:, 3]) * np.cos(m[:, 4] - truth[:, 4]) +
+            np.cos(m[:, 3]) * np.cos(truth[:, 3])), 0, 1)))
+        return {"fiso_rmse": float(np.sqrt(np.mean((m[:, 0] - truth[:, 0]) ** 2))),
+                "fintra_rmse": float(np.sqrt(np.mean((m[:, 1] - truth[:, 1]) ** 2))),
+                "log_kappa_rmse": float(np.sqrt(np.mean((np.log(np.maximum(m[:, 2], 1e-3)) -
+                                                          np.log(truth[:, 2])) ** 2))),
+                "orientation_median_deg": float(np.median(ang))}
+
+    line = base_line(METRIC, n / (t_sur / 1e3), "voxels/s", a, t_sur,
+                     {"workload": "learned_init_noddi_watson", "model": MODEL, "nvox": n,
+                      "nmeas": 288, "nburn": NBURN, "njumps": NJUMPS, "sampleevery": SE,
+                      "refit_margin": 0.01, "network": "288-256-256-256-12 GELU, bf16",
+                      "l2": "inputs larger than L2 (no flush)"},
+                     clk.summary(),
+                     grid_init={"value": n / (t_plain / 1e3), "ms": t_plain,
+                                "param_error": err(gp)},
+                     surrogate_init={"value": n / (t_sur / 1e3), "ms": t_sur,
+                                     "param_error": err(gs_), "refit_voxels": info["refit"]},
+                     training={"signals": int(n_train), "epochs": a.epochs, "steps": int(steps),
+                               "seconds": li.train_seconds, "data_seconds": t_data,
+                               "tflops": 3 * flop_sample * steps * 4096 / li.train_seconds / 1e12,
+                               "loss_first": li.history[0][1], "loss_last": li.history[-1][1]})
+    print(json.dumps(line))
+
+
 def main():
     a = parse()
     rank, world, local = dist_env()
     if a.profile_stage:
         profile_stage(a)
+        return
+    if a.impl == "ours" and a.workload != "noddi_watson":
+        import torch
+        torch.cuda.set_device(local)
+        dev = torch.device("cuda", local)
+        {"ball_1_stick_lm": bench_b1s_lm, "heterogeneous": bench_heterogeneous,
+         "learned_init": bench_learned}[a.workload](a, dev)
         return
     if a.impl == "reference":
         if world > 1:

@@ -389,6 +389,10 @@ class Cudimot:
                                                  out.shape[1], _dptr(params), _dptr(prop_sd),
                                                  self._stream()), "mlp_decode")
 
+    def fit_reserve(self, nvox, nmeas):
+        """Allocate the scratch buffers of a fit of this shape now."""
+        _check(self.lib, self.lib.cdm_fit_reserve(self.ctx, nvox, nmeas), "fit_reserve")
+
     def fit_enqueue(self, meas, params, cfp, fixp, samples, tau=None, pred=None, bic=None, aic=None):
         """The stage sequence as plain launches on the current stream."""
         nv, nm = meas.shape

@@ -192,13 +192,22 @@ class LearnedInit:
         self.lib.predicted_signal(params.unsqueeze(2).contiguous(), self.cfp, s0, pred)
         return ((pred - meas) ** 2).sum(1)
 
-    def fit(self, meas, s0, fit_cfg, samples, judge_cost=None, margin=0.01):
+    def contexts(self, fit_cfg, nvox):
+        """Fitting contexts of `fit` (LM/MCMC, and grid search + LM for the
+        refit) with their scratch buffers reserved for nvox voxels."""
+        lib = capi.Cudimot(self.model, fit_cfg)
+        g = capi.Cudimot(self.model, capi.model_cfg(self.model, grid=self.grid))
+        lib.fit_reserve(nvox, self.nmeas)
+        g.fit_reserve(nvox, self.nmeas)
+        return lib, g
+
+    def fit(self, meas, s0, fit_cfg, samples, judge_cost=None, margin=0.01, ctx=None):
         """Surrogate-initialised fit: network -> LM -> (refit by grid search +
         LM where the LM cost exceeds judge_cost by more than margin) -> MCMC
         with network-seeded proposal widths. Returns (params, info)."""
         torch = self.torch
         n = meas.shape[0]
-        lib = capi.Cudimot(self.model, fit_cfg)
+        lib, g = ctx or self.contexts(fit_cfg, n)
         P, sd = self.predict(meas, s0)
         lib.levmar(meas, P, self.cfp, s0)
         info = {"refit": 0}
@@ -211,8 +220,6 @@ class LearnedInit:
                 sub_s0 = s0.index_select(0, bad).contiguous()
                 sub_p = self._default_init(bad.numel())
                 sub_p[:, 3:5] = P.index_select(0, bad)[:, 3:5]
-                gcfg = capi.model_cfg(self.model, grid=self.grid)
-                g = capi.Cudimot(self.model, gcfg)
                 g.gridsearch(sub_m, sub_p, self.cfp, sub_s0)
                 g.levmar(sub_m, sub_p, self.cfp, sub_s0)
                 P.index_copy_(0, bad, sub_p)
