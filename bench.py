@@ -439,17 +439,30 @@ def bench_learned(a, dev):
     st = torch.cuda.current_stream()
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
 
-    # scratch buffers and the network's inference buffers before timing
+    # scratch buffers, the network's inference buffers and every kernel of
+    # both paths loaded before timing (a short run of each on 4096 voxels)
     plain.fit_reserve(n, 288)
     ctx = li.contexts(fit_cfg, n)
     li.predict(meas, s0)
+    w = min(n, 4096)
+    wcfg = capi.model_cfg(MODEL, grid=synth.WATSON_GRID, run_mcmc=1, nburn=25, njumps=25,
+                          sampleevery=25)
+    wp = init[:w].clone()
+    wl = capi.Cudimot(MODEL, wcfg)
+    wl.gridsearch(meas[:w], wp, li.cfp, s0[:w])
+    wl.levmar(meas[:w], wp, li.cfp, s0[:w])
+    wsamp = torch.zeros(w, 5, 1, dtype=torch.float64, device=dev)
+    wl.mcmc(meas[:w], wp, li.cfp, s0[:w], wsamp)
+    li.fit(meas[:w].contiguous(), s0[:w].contiguous(), wcfg, wsamp,
+           judge_cost=torch.zeros(w, dtype=torch.float64, device=dev), margin=0.0)
     torch.cuda.synchronize()
     # grid-initialised path: GS -> LM | judge cost | MCMC
     with ClockSampler(dev.index or 0) as clk:
         p = init.clone()
-        e = [ev() for _ in range(4)]
+        e = [ev() for _ in range(6)]
         e[0].record(st)
         plain.gridsearch(meas, p, li.cfp, s0)
+        e[4].record(st)
         plain.levmar(meas, p, li.cfp, s0)
         e[1].record(st)
         judge = li.cost(meas, p, s0)
@@ -458,6 +471,9 @@ def bench_learned(a, dev):
         e[3].record(st)
         torch.cuda.synchronize()
         t_plain = e[0].elapsed_time(e[1]) + e[2].elapsed_time(e[3])
+        plain_ms = {"gridsearch": e[0].elapsed_time(e[4]), "levmar": e[4].elapsed_time(e[1]),
+                    "mcmc": e[2].elapsed_time(e[3])}
+        lm_it_plain = plain.stats().lm_iterations / n
         # network-initialised path: network -> LM -> refit -> MCMC
         q = None
         f0, f1 = ev(), ev()
@@ -484,9 +500,11 @@ def bench_learned(a, dev):
                       "refit_margin": 0.01, "network": "288-256-256-256-12 GELU, bf16",
                       "l2": "inputs larger than L2 (no flush)"},
                      clk.summary(),
-                     grid_init={"value": n / (t_plain / 1e3), "ms": t_plain,
-                                "param_error": err(gp)},
+                     grid_init={"value": n / (t_plain / 1e3), "ms": t_plain, "stages_ms": plain_ms,
+                                "lm_iterations_per_voxel": lm_it_plain, "param_error": err(gp)},
                      surrogate_init={"value": n / (t_sur / 1e3), "ms": t_sur,
+                                     "stages_ms": info["ms"],
+                                     "lm_iterations_per_voxel": ctx[0].stats().lm_iterations / n,
                                      "param_error": err(gs_), "refit_voxels": info["refit"]},
                      training={"signals": int(n_train), "epochs": a.epochs, "steps": int(steps),
                                "seconds": li.train_seconds, "data_seconds": t_data,

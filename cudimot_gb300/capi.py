@@ -215,6 +215,9 @@ def _declare(lib):
         "cdm_synth_signals": [_vp, i, i, _vp, _vp, _vp, C.c_double, C.c_double, C.c_uint64, i,
                               _vp, _vp, _vp, i, _vp],
         "cdm_mlp_head_info": [C.POINTER(i), C.POINTER(i), _vp],
+        "cdm_cost": [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp],
+        "cdm_select_worse": [i, _vp, _vp, C.c_double, _vp, _vp, _vp],
+        "cdm_rows": [i, _vp, i, _vp, _vp, i, C.c_double, _vp],
         "cdm_mlp_targets": [_vp, i, _vp, _vp, _vp],
         "cdm_mlp_decode": [_vp, i, _vp, i, _vp, _vp, _vp],
         "cdm_fit_enqueue": [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
@@ -237,7 +240,7 @@ EXPORTED = ("cdm_get_model_info", "cdm_default_cfg", "cdm_status_string", "cdm_l
             "cdm_bic_aic", "cdm_predicted_signal", "cdm_fit", "cdm_fit_host",
             "cdm_fit_reserve", "cdm_fit_enqueue", "cdm_synchronize", "cdm_get_stats",
             "cdm_mcmc_seeded", "cdm_synth_signals", "cdm_mlp_head_info", "cdm_mlp_targets",
-            "cdm_mlp_decode")
+            "cdm_mlp_decode", "cdm_cost", "cdm_select_worse", "cdm_rows")
 
 
 def lib_path(model: str) -> str:
@@ -371,6 +374,23 @@ class Cudimot:
             self.ctx, nv, nm, _dptr(cfp), _dptr(params), _dptr(fixp), float(snr[0]), float(snr[1]),
             int(seed), b_col, _dptr(meas), _dptr(s0), xp, 0 if x is None else x.shape[1],
             self._stream()), "synth_signals")
+
+    def cost(self, meas, params, cfp, fixp, out):
+        nv, nm = meas.shape
+        _check(self.lib, self.lib.cdm_cost(self.ctx, nv, nm, _dptr(meas), _dptr(params), _dptr(cfp),
+                                           _dptr(fixp), _dptr(out), self._stream()), "cost")
+
+    def select_worse(self, cost, ref, margin, idx, count):
+        """idx, count: int32 CUDA tensors ([n], [1])."""
+        _check(self.lib, self.lib.cdm_select_worse(cost.shape[0], _dptr(cost), _dptr(ref), float(margin),
+                                                   C.c_void_p(idx.data_ptr()),
+                                                   C.c_void_p(count.data_ptr()), self._stream()),
+               "select_worse")
+
+    def rows(self, nsel, idx, src, dst, mode, value=0.0):
+        ncols = dst.shape[1]
+        _check(self.lib, self.lib.cdm_rows(nsel, C.c_void_p(idx.data_ptr()), ncols, _dptr(src),
+                                           _dptr(dst), mode, float(value), self._stream()), "rows")
 
     def mlp_head(self):
         n_mu, n_sig = C.c_int(), C.c_int()

@@ -636,6 +636,58 @@ cdm_status cdm_synth_signals(cdm_ctx* c, int nvox, int nmeas, const double* CFP,
   return CDM_OK;
 }
 
+cdm_status cdm_cost(cdm_ctx* c, int nvox, int nmeas, const double* meas, const double* params,
+                    const double* CFP, const double* FixP, double* cost, void* stream) {
+  CDM_TRY(check_common(c, nvox, nmeas, CDM_CFP_TSIZE, CDM_FIXP_TSIZE));
+  if (!meas || !params || !CFP || !cost || (CDM_FIXP_TSIZE > 0 && !FixP))
+    return cdm_fail(CDM_BAD_ARG, "null array");
+  cudaStream_t st = (cudaStream_t)stream;
+  CDM_TRY(prep_protocol(c, nmeas, CFP, st));
+  if (nvox == 0) return CDM_OK;
+  cdm_post_args a;
+  std::memset(&a, 0, sizeof(a));
+  a.nvox = nvox;
+  a.nmeas = nmeas;
+  a.nmeas_pad = c->nmeas_pad;
+  a.nsamples = 1;
+  a.fixp_tsize = CDM_FIXP_TSIZE;
+  a.proto_bytes = (uint32_t)proto_bytes(c->nmeas_pad);
+  a.proto = c->proto32;
+  a.meas = meas;
+  a.fixp = FixP;
+  a.err = c->err;
+  const size_t sm = proto_bytes(c->nmeas_pad);
+  CDM_TRY(set_smem(cdm_cost_kernel, sm));
+  cdm_cost_kernel<<<blocks_for(nvox, 32), CDM_NT, sm, st>>>(a, params, cost);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+cdm_status cdm_select_worse(int n, const double* cost, const double* ref, double margin, int* idx,
+                            int* count, void* stream) {
+  if (n < 0 || !cost || !ref || !idx || !count) return cdm_fail(CDM_BAD_ARG, "bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  CDM_CUDA(cudaMemsetAsync(count, 0, sizeof(int), st));
+  if (n == 0) return CDM_OK;
+  cdm_select_worse_kernel<<<std::min((n + 255) / 256, 152 * 8), 256, 0, st>>>(n, cost, ref, margin,
+                                                                             idx, count);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+cdm_status cdm_rows(int nsel, const int* idx, int ncols, const double* src, double* dst, int mode,
+                    double value, void* stream) {
+  if (nsel < 0 || ncols <= 0 || !idx || !dst || mode < 0 || mode > 2 || (mode < 2 && !src))
+    return cdm_fail(CDM_BAD_ARG, "bad argument");
+  if (nsel == 0) return CDM_OK;
+  const size_t total = (size_t)nsel * ncols;
+  cdm_rows_kernel<<<(int)std::min<size_t>((total + 255) / 256, 152 * 8), 256, 0,
+                    (cudaStream_t)stream>>>(nsel, idx, ncols, mode == 2 ? nullptr : src, dst,
+                                            mode == 1, value);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
 cdm_status cdm_mlp_head_info(int* n_mu, int* n_sig, int* group) {
 #ifdef CDM_MLP_HEAD
   const int g[CDM_MLP_NMU] = CDM_MLP_GROUPS;

@@ -37,7 +37,7 @@ struct cdm_mcmc_args {
   uint64_t seed;
   uint32_t stream;
   uint32_t voxel_offset;
-  const double* prop_sd;  // [nvox][NPARAMS] initial proposal widths, or null: |P|/10 as CUDIMOT
+  const double* prop_sd;  // [nvox][NPARAMS] initial proposal widths; null or <= 0: P/10 as CUDIMOT
   int* err;
   cdm_limits lim;
 };
@@ -137,7 +137,9 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
   int acc[kNP], rej[kNP];
 #pragma unroll
   for (int p = 0; p < kNP; p++)
-    propSD[p] = a.prop_sd ? (float)a.prop_sd[(size_t)v * kNP + p] : (float)P[p] / 10.0f;
+    propSD[p] = (a.prop_sd && a.prop_sd[(size_t)v * kNP + p] > 0.0)
+                    ? (float)a.prop_sd[(size_t)v * kNP + p]
+                    : (float)P[p] / 10.0f;
   float tau = 0.0f, tauSD = 0.0f;
   int tacc = 0, trej = 0;
   const uint32_t vid = a.voxel_offset + (uint32_t)v;

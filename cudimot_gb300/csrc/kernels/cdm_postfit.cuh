@@ -97,6 +97,59 @@ __global__ void __launch_bounds__(CDM_NT) cdm_bic_aic_kernel(const __grid_consta
   a.bic[v] = -2.0 * b + np * log(n);
 }
 
+// Cost of given parameters, as the LM and grid search score them: sum of
+// squared residuals (FP32 model, FP64 warp sum); a warp per voxel.
+__global__ void __launch_bounds__(CDM_NT) cdm_cost_kernel(const __grid_constant__ cdm_post_args a,
+                                                          const double* __restrict__ params,
+                                                          double* __restrict__ cost) {
+  extern __shared__ __align__(16) float sproto[];
+  if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
+  const int v = blockIdx.x * (CDM_NT / 32) + (int)threadIdx.x / 32;
+  if (v >= a.nvox) return;
+  const int lane = threadIdx.x & 31;
+  fp32 P[kNPS], FixP[kNFIX];
+  cdm_load_params(params + (size_t)v * kNP, P);
+  cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
+  cdm_update_derived(P, FixP);
+  float acc = 0.0f;
+  for (int m = lane; m < a.nmeas; m += 32) {
+    fp32 cf[kNCOLS];
+    cdm_load_cfp(sproto, a.nmeas_pad, m, cf);
+    const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - (float)a.meas[(size_t)v * a.nmeas + m];
+    acc = fmaf(r, r, acc);
+  }
+  const double tot = cdm_group_sum<32>((double)acc, 0xFFFFFFFFu);
+  if (lane == 0) cost[v] = tot;
+}
+
+// Row helpers of the learned initialiser's fallback (voxels whose cost
+// exceeds a reference cost by more than a margin are refit).
+__global__ void cdm_select_worse_kernel(int n, const double* __restrict__ cost,
+                                        const double* __restrict__ ref, double margin,
+                                        int* __restrict__ idx, int* __restrict__ count) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    if (cost[v] > ref[v] * (1.0 + margin)) idx[atomicAdd(count, 1)] = v;
+}
+
+// dst[k][:] = src[idx[k]][:] (gather) or dst[idx[k]][:] = src[k][:] (scatter),
+// or dst[idx[k]][:] = value (src null).
+__global__ void cdm_rows_kernel(int nsel, const int* __restrict__ idx, int ncols,
+                                const double* __restrict__ src, double* __restrict__ dst,
+                                int scatter, double value) {
+  const size_t total = (size_t)nsel * ncols;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i / ncols), c = (int)(i % ncols);
+    const size_t r = (size_t)idx[k];
+    if (!src)
+      dst[r * ncols + c] = value;
+    else if (scatter)
+      dst[r * ncols + c] = src[(size_t)k * ncols + c];
+    else
+      dst[(size_t)k * ncols + c] = src[r * ncols + c];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Layout kernels.
 // Protocol: CUDIMOT's CFP [nmeas][CFP_Tsize] (double) plus the plugin's

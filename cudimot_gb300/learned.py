@@ -185,21 +185,29 @@ class LearnedInit:
         self.lib.mlp_decode(out, P, sd)
         return P, sd
 
-    def cost(self, meas, params, s0):
-        """Per-voxel sum of squared residuals (the LM cost) on the GPU."""
+    def cost(self, meas, params, s0, out=None):
+        """Per-voxel sum of squared residuals (the LM cost), on the GPU."""
         torch = self.torch
-        pred = torch.empty_like(meas)
-        self.lib.predicted_signal(params.unsqueeze(2).contiguous(), self.cfp, s0, pred)
-        return ((pred - meas) ** 2).sum(1)
+        if out is None:
+            out = torch.empty(meas.shape[0], dtype=torch.float64, device=self.dev)
+        self.lib.cost(meas, params, self.cfp, s0, out)
+        return out
 
-    def contexts(self, fit_cfg, nvox):
-        """Fitting contexts of `fit` (LM/MCMC, and grid search + LM for the
-        refit) with their scratch buffers reserved for nvox voxels."""
+    def contexts(self, fit_cfg, nvox, refit_cap=None):
+        """Fitting contexts and buffers of `fit` (LM/MCMC; grid search + LM
+        for the refit, in chunks of refit_cap voxels), allocated now."""
+        torch = self.torch
         lib = capi.Cudimot(self.model, fit_cfg)
         g = capi.Cudimot(self.model, capi.model_cfg(self.model, grid=self.grid))
+        cap = max(1, min(nvox, refit_cap or max(4096, nvox // 16)))
         lib.fit_reserve(nvox, self.nmeas)
-        g.fit_reserve(nvox, self.nmeas)
-        return lib, g
+        g.fit_reserve(cap, self.nmeas)
+        npar = self.lib.nparams
+        f = lambda *shape: torch.empty(*shape, dtype=torch.float64, device=self.dev)  # noqa: E731
+        buf = dict(cost=f(nvox), idx=torch.empty(nvox, dtype=torch.int32, device=self.dev),
+                   count=torch.zeros(1, dtype=torch.int32, device=self.dev),
+                   m=f(cap, self.nmeas), s0=f(cap, 1), p=f(cap, npar), cap=cap)
+        return lib, g, buf
 
     def fit(self, meas, s0, fit_cfg, samples, judge_cost=None, margin=0.01, ctx=None):
         """Surrogate-initialised fit: network -> LM -> (refit by grid search +
@@ -207,23 +215,43 @@ class LearnedInit:
         with network-seeded proposal widths. Returns (params, info)."""
         torch = self.torch
         n = meas.shape[0]
-        lib, g = ctx or self.contexts(fit_cfg, n)
+        lib, g, buf = ctx or self.contexts(fit_cfg, n)
+        ev = []
+
+        def mark():
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(torch.cuda.current_stream())
+            ev.append(e)
+
+        mark()
         P, sd = self.predict(meas, s0)
+        mark()
         lib.levmar(meas, P, self.cfp, s0)
+        mark()
         info = {"refit": 0}
         if judge_cost is not None:
-            c = self.cost(meas, P, s0)
-            bad = torch.nonzero(c > judge_cost * (1.0 + margin)).flatten()
-            info["refit"] = int(bad.numel())
-            if bad.numel():
-                sub_m = meas.index_select(0, bad).contiguous()
-                sub_s0 = s0.index_select(0, bad).contiguous()
-                sub_p = self._default_init(bad.numel())
-                sub_p[:, 3:5] = P.index_select(0, bad)[:, 3:5]
-                g.gridsearch(sub_m, sub_p, self.cfp, sub_s0)
-                g.levmar(sub_m, sub_p, self.cfp, sub_s0)
-                P.index_copy_(0, bad, sub_p)
-                sd.index_copy_(0, bad, (sub_p.abs() / 10.0))
+            self.cost(meas, P, s0, out=buf["cost"])
+            lib.select_worse(buf["cost"], judge_cost, margin, buf["idx"], buf["count"])
+            nbad = int(buf["count"].item())
+            info["refit"] = nbad
+            cap = buf["cap"]
+            for k0 in range(0, nbad, cap):
+                k = min(cap, nbad - k0)
+                idx = buf["idx"][k0:k0 + k]
+                sm, ss, sp = buf["m"][:k], buf["s0"][:k], buf["p"][:k]
+                lib.rows(k, idx, meas, sm, 0)
+                lib.rows(k, idx, s0, ss, 0)
+                lib.rows(k, idx, P, sp, 0)
+                # the grid search replaces the grid parameters, keeps the rest
+                g.gridsearch(sm, sp, self.cfp, ss)
+                g.levmar(sm, sp, self.cfp, ss)
+                lib.rows(k, idx, sp, P, 1)
+                lib.rows(k, idx, None, sd, 2, 0.0)  # MCMC starts these from P/10
+        mark()
         if fit_cfg.run_mcmc:
             lib.mcmc_seeded(meas, P, self.cfp, s0, samples, sd)
+        mark()
+        torch.cuda.synchronize()
+        info["ms"] = {k: ev[i].elapsed_time(ev[i + 1])
+                      for i, k in enumerate(("network", "levmar", "refit", "mcmc"))}
         return P, info

@@ -209,8 +209,9 @@ cdm_status cdm_fit_enqueue(cdm_ctx* ctx, int nvox, int nmeas, const double* meas
                            double* AIC, void* stream);
 
 /* As cdm_mcmc, with each voxel's initial proposal widths prop_sd
- * [nvox][NPARAMS] (CUDIMOT starts from |P|/10, MCMC.cu:474-476; null gives
- * that). Used by the learned initialiser to seed the proposal scales. */
+ * [nvox][NPARAMS] (CUDIMOT starts from P/10, MCMC.cu:474-476; a null array
+ * or an entry <= 0 gives that). Used by the learned initialiser to seed
+ * the proposal scales. */
 cdm_status cdm_mcmc_seeded(cdm_ctx* ctx, int nvox, int nmeas, int CFP_size, int FixP_size,
                            const double* meas, double* params, const double* CFP,
                            const double* FixP, double* samples, double* tau_samples,
@@ -228,6 +229,21 @@ cdm_status cdm_synth_signals(cdm_ctx* ctx, int nvox, int nmeas, const double* CF
                              const double* params, const double* FixP, double snr_lo,
                              double snr_hi, uint64_t seed, int b_col, double* meas,
                              double* s0_est, void* x, int x_ld, void* stream);
+
+/* Per-voxel cost (sum of squared residuals, the LM/grid-search score,
+ * GridSearch.cu:25-73) of params [nvox][NPARAMS] -> cost [nvox]. */
+cdm_status cdm_cost(cdm_ctx* ctx, int nvox, int nmeas, const double* meas, const double* params,
+                    const double* CFP, const double* FixP, double* cost, void* stream);
+
+/* Row helpers of the learned initialiser's fallback (no CUDIMOT
+ * counterpart). cdm_select_worse: idx[0 .. *count) = the voxels with
+ * cost > ref * (1 + margin), in no particular order (count is a device int).
+ * cdm_rows, mode 0: dst[k] = src[idx[k]]; mode 1: dst[idx[k]] = src[k];
+ * mode 2: dst[idx[k]] = value; rows of ncols doubles. */
+cdm_status cdm_select_worse(int n, const double* cost, const double* ref, double margin, int* idx,
+                            int* count, void* stream);
+cdm_status cdm_rows(int nsel, const int* idx, int ncols, const double* src, double* dst, int mode,
+                    double value, void* stream);
 
 /* The plugin's learned-initialiser head (optional hooks MLP_Encode /
  * MLP_Decode; CDM_NOT_SUPPORTED without them): number of means, of

@@ -133,3 +133,35 @@ def test_seeded_mcmc_samples_the_same_posterior(trained, cuda):
         z = (g[:, p].mean(1) - r[:, p].mean(1)) / np.sqrt(se(g[:, p]) ** 2 + se(r[:, p]) ** 2 + 1e-30)
         assert abs(np.median(z)) < 0.5, (p, np.median(z))
         assert np.mean(np.abs(z) < 4) > 0.9, (p, np.mean(np.abs(z) < 4))
+
+
+def test_cost_select_and_rows(built, cuda):
+    cfp = protocol()
+    o = oracle("NODDI_Watson")
+    rng = np.random.default_rng(5)
+    P, S0 = synth.watson_truth(2000, rng)
+    meas = synth.rician(o.signal(P, cfp, S0[:, None]), S0[:, None] / 20.0, rng)
+    lib = capi.Cudimot("NODDI_Watson", capi.model_cfg("NODDI_Watson"))
+    c = torch.zeros(2000, dtype=torch.float64, device=cuda)
+    lib.cost(T(meas, cuda), T(P, cuda), T(cfp, cuda), T(S0[:, None], cuda), c)
+    torch.cuda.synchronize()
+    ref = o.cost(meas, P, cfp, S0[:, None])
+    np.testing.assert_allclose(c.cpu().numpy(), ref, rtol=1e-5)
+    refc = torch.full_like(c, float(np.median(ref)))
+    idx = torch.zeros(2000, dtype=torch.int32, device=cuda)
+    cnt = torch.zeros(1, dtype=torch.int32, device=cuda)
+    lib.select_worse(c, refc, 0.01, idx, cnt)
+    k = int(cnt.item())
+    sel = np.sort(idx[:k].cpu().numpy())
+    assert np.array_equal(sel, np.nonzero(c.cpu().numpy() > np.median(ref) * 1.01)[0])
+    src = T(P, cuda)
+    sub = torch.zeros(k, 5, dtype=torch.float64, device=cuda)
+    lib.rows(k, idx, src, sub, 0)
+    dst = torch.zeros_like(src)
+    lib.rows(k, idx, sub, dst, 1)
+    lib.rows(k, idx, None, src, 2, -1.0)
+    torch.cuda.synchronize()
+    ii = idx[:k].long()
+    assert torch.equal(sub, T(P, cuda)[ii])
+    assert torch.equal(dst[ii], T(P, cuda)[ii])
+    assert torch.all(src[ii] == -1.0)
