@@ -48,8 +48,10 @@ def parse():
     ap.add_argument("--nvox", type=int, default=NVOX)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="voxels for the CPU baseline")
-    ap.add_argument("--profile-stage", choices=["gridsearch", "levmar", "mcmc"], default=None,
-                    help="run the preceding stages, then one launch of this stage (for ncu)")
+    ap.add_argument("--profile-stage", choices=["gridsearch", "levmar", "mcmc", "mlp_forward"],
+                    default=None,
+                    help="run the preceding stages, then one launch of this stage (for ncu); "
+                         "mlp_forward: two inference passes of the network on --nvox voxels")
     ap.add_argument("--nburn", type=int, default=NBURN)
     ap.add_argument("--njumps", type=int, default=NJUMPS)
     ap.add_argument("--workload", default="noddi_watson",
@@ -222,11 +224,33 @@ def run_reference(a, rank, world):
     print(json.dumps(line))
 
 
+def profile_mlp_forward(a, dev):
+    import torch
+    from cudimot_gb300 import synth
+    from cudimot_gb300.learned import LearnedInit
+    rng = np.random.default_rng(8219)
+    cfp = synth.protocol(18, [(90, 1000.0), (90, 2000.0), (90, 3000.0)], rng)
+    li = LearnedInit(MODEL, cfp, grid=synth.WATSON_GRID, seed=8219, device=dev)
+    d = li.synth(a.nvox, seed=4242, snr=(20.0, 20.0), meas=True)
+    li.predict(d["meas"], d["s0"])  # warm-up: 4 GEMM launches
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    li.predict(d["meas"], d["s0"])
+    e1.record()
+    torch.cuda.synchronize()
+    li.net.check()
+    print(json.dumps({"stage": "mlp_forward", "nvox": a.nvox, "ms": e0.elapsed_time(e1)}))
+
+
 def profile_stage(a):
     """One launch of one stage on a small case, for ncu captures."""
     import torch
     from cudimot_gb300 import capi, synth
     dev = torch.device("cuda:0")
+    if a.profile_stage == "mlp_forward":
+        profile_mlp_forward(a, dev)
+        return
     cfp, meas, fixp, init, _ = make_workload(a.nvox, 8219, dev)
     cfg = capi.model_cfg(MODEL, grid=synth.WATSON_GRID, run_mcmc=1, nburn=a.nburn,
                          njumps=a.njumps, sampleevery=SE)
