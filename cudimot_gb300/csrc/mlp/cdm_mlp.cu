@@ -145,6 +145,16 @@ cdm_status make_gemm(gemm* g, const void* A, int lda, const void* B, int ldb, in
 }
 
 cdm_status run_gemm(const gemm& g, cudaStream_t st) {
+  if (g.epi == EPI_BIAS_GELU || g.epi == EPI_DGELU) {
+    // the staged epilogue writes 16-byte row pieces
+    const void* ptrs[3] = {g.a.out_bf16, g.a.aux_bf16, nullptr};
+    for (const void* p : ptrs)
+      if (p && ((uintptr_t)p & 15)) return fail(CDM_BAD_ARG, "bf16 GEMM outputs must be 16-byte aligned");
+    if (g.a.ld_out % 8 || g.a.N % 8 || (g.epi == EPI_DGELU && !g.a.aux_bf16) || !g.a.out_bf16)
+      return fail(CDM_BAD_ARG, "bf16 GEMM outputs need ld_out and N multiples of 8");
+    if (g.bn < 256 && g.a.N > g.bn && (g.a.N % g.bn) % 8)
+      return fail(CDM_BAD_ARG, "bf16 GEMM tile remainder must be a multiple of 8");
+  }
   switch (g.epi) {
     case EPI_F32: return launch_epi<EPI_F32>(g.bn, g.ta, g.tb, g.a, st);
     case EPI_BIAS_F32: return launch_epi<EPI_BIAS_F32>(g.bn, g.ta, g.tb, g.a, st);
@@ -385,7 +395,7 @@ cdm_status forward(cdm_mlp* m, const __nv_bfloat16* x, int n, float* out, bool t
       g.a.out_t = m->actT[l];
       g.a.ld_t = n;
     } else {
-      g.a.aux_bf16 = m->iz;
+      g.a.aux_bf16 = nullptr;  // the pre-activation is only needed for training
       g.a.out_bf16 = m->ia[l & 1];
     }
     MLP_TRY(run_gemm(g, st));

@@ -6,7 +6,7 @@
 // One CTA computes a 128 x BN tile (BN <= 256, a multiple of 16) with 128
 // threads:
 //   * warp 0, lane 0 - TMA producer: 128x64 (A) and BNx64 (B) bf16 boxes of
-//     the tensor maps, 128-byte swizzle, into a ring of kStages shared-memory
+//     the tensor maps, 128-byte swizzle, into a ring of shared-memory
 //     stages, each completing a "full" mbarrier with its transaction bytes;
 //   * warp 1, lane 0 - MMA issuer: per stage four tcgen05.mma
 //     (kind::f16, M=128, N=BN, K=16) reading both operands through shared
@@ -28,7 +28,9 @@ namespace cdm_mma {
 
 constexpr int kBM = 128;     // tile rows (TMEM lanes)
 constexpr int kBK = 64;      // bf16 elements per 128-byte swizzle row
-constexpr int kStages = 4;
+// Ring depth: two stages for 256-wide tiles (two CTAs fit on an SM, so one
+// CTA's epilogue overlaps the other's loads and MMAs), more for narrower.
+__host__ __device__ constexpr int stages_for(int bn) { return bn >= 256 ? 2 : bn >= 144 ? 3 : 4; }
 constexpr int kThreads = 128;
 constexpr int kErrTimeout = 0x4D4D41;  // "MMA"
 constexpr unsigned long long kWaitNs = 2000000000ull;
@@ -175,13 +177,17 @@ __host__ __device__ constexpr uint32_t tmem_cols(int bn) {
 
 template <int BN>
 struct smem_layout {
+  static constexpr int kStages = stages_for(BN);
   static constexpr int kABytes = kBM * kBK * 2;  // 16 KB
   static constexpr int kBBytes = BN * kBK * 2;
   static constexpr int kStageBytes = kABytes + kBBytes;
-  // stages (1024-aligned), then barriers
+  // stages (1024-aligned), then barriers; the bf16 output tile of the
+  // epilogue ([128][BN + 8], padded rows) reuses the stage memory
+  static constexpr int kOutLd = BN + 8;
   static constexpr int kBarOffset = kStages * kStageBytes;
   static constexpr int kBytes = kBarOffset + (2 * kStages + 1) * 8 + 16;
   static constexpr int kAlloc = kBytes + 1024;  // slack for 1024-byte alignment
+  static_assert(kBM * kOutLd * 2 <= kBarOffset, "output tile must fit in the stage memory");
 };
 
 template <int BN, int EPI>
@@ -190,6 +196,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                      const __grid_constant__ gemm_args a) {
   static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "UMMA N for M=128");
   using L = smem_layout<BN>;
+  constexpr int kStages = L::kStages;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
       (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -264,44 +271,104 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (ok) mma_commit(done);
   }
 
-  // Epilogue: every warp waits for the accumulator.
+  // Epilogue: every thread waits for the accumulator; the decision to read
+  // it is made for the whole CTA (the staged path below has CTA barriers).
   bool ready = mbar_wait(done, 0);
-  __syncwarp();
-  // tcgen05.ld is warp-collective: the whole warp reads or none of it does
-  ready = __all_sync(0xFFFFFFFFu, ready);
-  if (!ready) atomicExch(&abort_flag, 1);
+  ready = __syncthreads_and(ready) != 0;
+  if (!ready && threadIdx.x == 0) atomicExch(&abort_flag, 1);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ready) {
-    const int row = m0 + warp * 32 + lane;
+    const int rloc = warp * 32 + lane;  // tile row (TMEM lane) of this thread
+    const int row = m0 + rloc;
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    if constexpr (EPI == EPI_F32 || EPI == EPI_BIAS_F32) {
+      // fp32 rows straight from registers (128 contiguous bytes per chunk)
+      const bool vec = (a.ld_out % 4) == 0;
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 32) {
-      float v[32];
-      tmem_ld32(lane_base + (uint32_t)c0, v);
-      if (row < a.M) {
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        float v[32];
+        tmem_ld32(lane_base + (uint32_t)c0, v);
+        if (row >= a.M) continue;
+        float* dst = a.out_f32 + (size_t)row * a.ld_out + n0 + c0;
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
+        for (int j = 0; j < 32; j += 4) {
           const int col = n0 + c0 + j;
-          if (c0 + j >= BN || col >= a.N) continue;  // BN need not be a multiple of 32
-          const size_t o = (size_t)row * a.ld_out + col;
-          if (EPI == EPI_F32) {
-            a.out_f32[o] = v[j];
-          } else if (EPI == EPI_BIAS_F32) {
-            a.out_f32[o] = v[j] + a.bias[col];
-          } else if (EPI == EPI_BIAS_GELU) {
-            const float z = v[j] + a.bias[col];
-            const __nv_bfloat16 zb = __float2bfloat16(z);
-            const __nv_bfloat16 g = __float2bfloat16(gelu(__bfloat162float(zb)));
-            a.aux_bf16[o] = zb;
-            a.out_bf16[o] = g;
-            if (a.out_t) a.out_t[(size_t)col * a.ld_t + row] = g;
-          } else {  // EPI_DGELU
-            const float z = __bfloat162float(a.aux_bf16[o]);
-            const __nv_bfloat16 d = __float2bfloat16(v[j] * gelu_grad(z));
-            a.out_bf16[o] = d;
-            if (a.out_t) a.out_t[(size_t)col * a.ld_t + row] = d;
+          float4 q;
+          q.x = v[j] + (EPI == EPI_BIAS_F32 && col + 0 < a.N ? a.bias[col + 0] : 0.0f);
+          q.y = v[j + 1] + (EPI == EPI_BIAS_F32 && col + 1 < a.N ? a.bias[col + 1] : 0.0f);
+          q.z = v[j + 2] + (EPI == EPI_BIAS_F32 && col + 2 < a.N ? a.bias[col + 2] : 0.0f);
+          q.w = v[j + 3] + (EPI == EPI_BIAS_F32 && col + 3 < a.N ? a.bias[col + 3] : 0.0f);
+          if (vec && c0 + j + 3 < BN && col + 3 < a.N) {
+            *reinterpret_cast<float4*>(dst + j) = q;
+          } else {
+            const float e[4] = {q.x, q.y, q.z, q.w};
+            for (int t = 0; t < 4; t++)
+              if (c0 + j + t < BN && col + t < a.N) dst[j + t] = e[t];
           }
         }
+      }
+    } else {
+      // bf16 outputs: each thread converts its row into a padded shared
+      // tile, then the CTA writes whole rows with coalesced 16-byte stores.
+      // BIAS_GELU with an aux output takes a second pass for z.
+      constexpr int LD = L::kOutLd;
+      __nv_bfloat16* stile = reinterpret_cast<__nv_bfloat16*>(smem);
+      const int ncols = min(BN, a.N - n0);  // valid columns of this tile (a multiple of 8)
+      const int passes = (EPI == EPI_BIAS_GELU && a.aux_bf16) ? 2 : 1;
+      for (int pass = 0; pass < passes; pass++) {
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 32) {
+          float v[32];
+          tmem_ld32(lane_base + (uint32_t)c0, v);
+          float zin[32];
+          if constexpr (EPI == EPI_DGELU) {
+#pragma unroll
+            for (int j = 0; j < 32; j++) zin[j] = 0.0f;
+            if (row < a.M && c0 < ncols) {
+              const __nv_bfloat16* zr = a.aux_bf16 + (size_t)row * a.ld_out + n0 + c0;
+#pragma unroll
+              for (int q = 0; q < 4; q++)
+                if (c0 + 8 * q < ncols) {
+                  const uint4 raw = *reinterpret_cast<const uint4*>(zr + 8 * q);
+                  const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&raw);
+#pragma unroll
+                  for (int t = 0; t < 8; t++) zin[8 * q + t] = __bfloat162float(h[t]);
+                }
+            }
+          }
+          __align__(16) __nv_bfloat16 o[32];
+#pragma unroll
+          for (int j = 0; j < 32; j++) {
+            const int col = n0 + c0 + j;
+            const bool ok = c0 + j < ncols;
+            float val;
+            if constexpr (EPI == EPI_BIAS_GELU) {
+              const float z = __bfloat162float(__float2bfloat16(v[j] + (ok ? a.bias[col] : 0.0f)));
+              val = pass == 0 ? gelu(z) : z;
+            } else {
+              val = v[j] * gelu_grad(zin[j]);
+            }
+            o[j] = __float2bfloat16(val);
+            if (pass == 0 && a.out_t && ok && row < a.M) a.out_t[(size_t)col * a.ld_t + row] = o[j];
+          }
+          if (c0 < BN) {
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+              if (c0 + 8 * q < BN)
+                *reinterpret_cast<uint4*>(stile + rloc * LD + c0 + 8 * q) =
+                    *reinterpret_cast<const uint4*>(o + 8 * q);
+          }
+        }
+        __syncthreads();
+        __nv_bfloat16* gout = pass == 0 ? a.out_bf16 : a.aux_bf16;
+        const int vpr = ncols / 8;  // 16-byte vectors per row
+        for (int i = threadIdx.x; i < kBM * vpr; i += kThreads) {
+          const int r = i / vpr, q = i % vpr;
+          if (m0 + r < a.M)
+            *reinterpret_cast<uint4*>(gout + (size_t)(m0 + r) * a.ld_out + n0 + 8 * q) =
+                *reinterpret_cast<const uint4*>(stile + r * LD + 8 * q);
+        }
+        __syncthreads();
       }
     }
   }
