@@ -621,7 +621,7 @@ def main():
         roofline = {"bound": "fp32", "kernel": "cdm_mcmc_kernel", "achieved": achieved,
                     "peak": fp32_peak["tflops"], "unit": "TFLOP/s", "frac": achieved / fp32_peak["tflops"],
                     "peak_source": fp32_peak["source"], "traffic": profiled_traffic(),
-                    "traffic_source": "profiles/mcmc_kernel_noddi_watson.md (small-case ncu capture scaled by voxels)",
+                    "traffic_source": "profiles/mcmc_kernel_noddi_watson.md (full-length 100k-voxel ncu capture scaled by voxels)",
                     "flop_per_voxel": per_voxel_mcmc, "launch_ms": mcmc_ms}
     line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
