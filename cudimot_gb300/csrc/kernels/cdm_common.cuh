@@ -149,6 +149,32 @@ __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const fl
   const int full = io.nmeas / G;
   const float* row = sproto + (size_t)io.lane * kNCOLS4;
   const float* sig = io.sig;
+#ifdef CDM_SIGNAL_PAIR
+  // two chunks per step on the paired FP32 instructions (plugin hook
+  // Predicted_Signal_Pair); two interleaved partial sums
+  float2 acc2 = make_float2(0.0f, 0.0f);
+  int c = 0;
+#pragma unroll 1
+  for (; c + 1 < full; c += 2) {
+    fp32 ca[kNCOLS], cb[kNCOLS];
+    cdm_load_cfp(row, 0, 0, ca);
+    cdm_load_cfp(row + G * kNCOLS4, 0, 0, cb);
+    const float2 s2 = Predicted_Signal_Pair(P, ca, cb, FixP);
+    const float2 r = __fadd2_rn(s2, make_float2(-sig[0], -sig[io.chunk_stride]));
+    acc2 = __ffma2_rn(r, r, acc2);
+    row += 2 * G * kNCOLS4;
+    sig += 2 * io.chunk_stride;
+  }
+  acc = acc2.x + acc2.y;
+  if (c < full) {
+    fp32 cf[kNCOLS];
+    cdm_load_cfp(row, 0, 0, cf);
+    const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - *sig;
+    acc = fmaf(r, r, acc);
+    row += G * kNCOLS4;
+    sig += io.chunk_stride;
+  }
+#else
 #pragma unroll kSseUnroll
   for (int c = 0; c < full; c++) {
     fp32 cf[kNCOLS];
@@ -158,6 +184,7 @@ __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const fl
     row += G * kNCOLS4;
     sig += io.chunk_stride;
   }
+#endif
   if (full < io.nchunk) {
     const bool valid = full * G + io.lane < io.nmeas;
     fp32 cf[kNCOLS];
