@@ -29,6 +29,10 @@
 #endif
 
 constexpr int kSseUnroll = CDM_SSE_UNROLL;
+#ifndef CDM_PAIR_UNROLL
+#define CDM_PAIR_UNROLL 2  // unroll of the paired (two-measurement) cost loop
+#endif
+constexpr int kPairUnroll = CDM_PAIR_UNROLL;
 constexpr int kNP = NPARAMS;
 constexpr int kNPS = CDM_PSTORE;
 constexpr int kNCOLS = CDM_CFP_TSIZE + CDM_NDCFP;
@@ -154,7 +158,7 @@ __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const fl
   // Predicted_Signal_Pair); two interleaved partial sums
   float2 acc2 = make_float2(0.0f, 0.0f);
   int c = 0;
-#pragma unroll 1
+#pragma unroll kPairUnroll
   for (; c + 1 < full; c += 2) {
     fp32 ca[kNCOLS], cb[kNCOLS];
     cdm_load_cfp(row, 0, 0, ca);

@@ -344,7 +344,7 @@ __device__ __forceinline__ float2 Predicted_Signal_Pair(const fp32* P, const fp3
   xv = __ffma2_rn(make_float2(A[2].v, B[2].v), watson_bc(P[7].v), xv);
   const float2 q = __ffma2_rn(__fmul2_rn(watson_bc(P[9].v), xv), xv, watson_bc(P[8].v));
   const float2 z = __fmul2_rn(make_float2(-A[3].v, -B[3].v), q);
-  const float2 extra = make_float2(expf(z.x), expf(z.y));
+  const float2 extra = make_float2((float)exp_gpu(fp32(z.x)), (float)exp_gpu(fp32(z.y)));
   const float2 x = make_float2(fminf(fmaxf(xv.x, -1.0f), 1.0f), fminf(fmaxf(xv.y, -1.0f), 1.0f));
   const float2 y = __fmul2_rn(x, x);
   float2 pm = make_float2(0.0f, 0.0f), pc = make_float2(1.0f, 1.0f);
