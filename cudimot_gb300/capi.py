@@ -171,6 +171,11 @@ MODEL_LIMITS = {
                                   3: (-100.0, 100.0), 4: (-100.0, 100.0), 5: (0.0, 1.0),
                                   6: (-100.0, 100.0), 7: (-100.0, 100.0)},
                           priors={3: (SINPRIOR,), 5: (ARDPRIOR, 1.0), 6: (SINPRIOR,)}),
+    # CUDIMOT's modelpriors writes "priors[4]=sin()", which its parser ignores
+    "NODDI_Bingham": dict(bounds={0: (0.0, 1.0), 1: (0.0, 1.0), 2: (0.1, 64.0), 3: (0.01, 32.0),
+                                  4: (-10000.0, 10000.0), 5: (-10000.0, 10000.0),
+                                  6: (-100.0, 100.0)},
+                          priors={}),
 }
 
 

@@ -275,3 +275,53 @@ def ball_2_sticks(nvox=300_000, seed=DEFAULT_SEED, snr=25.0) -> Workload:
     init = np.stack([np.clip(s0i, 1.0, 9000.0), np.clip(w[:, 0], 1e-5, 9e-3), fa, th1, ph1,
                      fa / 4.0, th2, ph2], axis=1)
     return Workload("ball_2_sticks", "Ball_2_Sticks", cfp, meas, truth, init, np.zeros((nvox, 0)))
+
+
+# Grid of CUDIMOT's NODDI-Bingham pipeline (fiso, fintra, kappa, beta):
+# 5 x 10 x 17 x 13 = 11,050 combinations.
+BINGHAM_GRID = {0: np.array([0.0, 0.05, 0.1, 0.2, 0.3]),
+                1: np.array([0.3, 0.5, 0.6, 0.7, 0.75, 0.8, 0.85, 0.9, 0.95, 1.0]),
+                2: np.array([0.5, 1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 15, 20, 25, 30, 40, 50], float),
+                3: np.array([0.2, 0.5, 1.0, 1.5, 2.0, 2.5, 3.0, 4.5, 6.5, 9, 12, 16, 20])}
+
+
+def bingham_truth(nvox, rng):
+    """NODDI-Watson parameters as noddi_watson draws them, plus
+    beta = U(0, 0.9) kappa and psi ~ U(0, pi)."""
+    P, S0 = watson_truth(nvox, rng)
+    beta = rng.uniform(0.0, 0.9, nvox) * P[:, 2]
+    psi = rng.uniform(0.0, np.pi, nvox)
+    return np.stack([P[:, 0], P[:, 1], P[:, 2], beta, P[:, 3], P[:, 4], psi], axis=1), S0
+
+
+def dti_psi(V, th, ph):
+    """Fanning angle psi from the second tensor eigenvector, as
+    utils/initialise_Psi.cc in CUDIMOT does: the angle of V2 in the plane
+    orthogonal to the fibre, measured from the fanning direction at psi = 0."""
+    v2 = V[:, :, 1]
+    f0 = np.stack([-np.sin(ph), np.cos(ph), np.zeros_like(ph)], axis=1)       # psi = 0
+    h0 = np.stack([np.cos(th) * np.cos(ph), np.cos(th) * np.sin(ph), -np.sin(th)], axis=1)
+    return np.arctan2(-np.sum(v2 * h0, axis=1), np.sum(v2 * f0, axis=1))
+
+
+def noddi_bingham(nvox=1_000_000, seed=DEFAULT_SEED, signal_fn=None, snr=20.0) -> Workload:
+    """NODDI-Bingham precision study: the NODDI-Watson protocol (288
+    measurements) and parameters plus beta = U(0,0.9) kappa and psi ~
+    U(0, pi); Rician noise at SNR 20; S0 = mean noisy b=0 signal; theta,
+    phi from a DTI fit and psi from its second eigenvector; grid of
+    CUDIMOT's Bingham pipeline (11,050 combinations)."""
+    r_proto, r_par, r_noise = _streams(seed, 3)
+    cfp = protocol(18, [(90, 1000.0), (90, 2000.0), (90, 3000.0)], r_proto)
+    truth, S0 = bingham_truth(nvox, r_par)
+    if signal_fn is None:
+        raise ValueError("noddi_bingham needs signal_fn (the model's Predicted_Signal)")
+    meas = rician(signal_fn(truth, cfp, S0), S0 / snr, r_noise)
+    b0 = cfp[:, 3] == 0
+    s0_est = meas[:, b0].mean(axis=1)
+    _, _, w, V = dti_fit(meas, cfp)
+    thi, phi = _angles(V[:, :, 0])
+    psi = dti_psi(V, thi, phi)
+    init = np.stack([np.full(nvox, 0.2), np.full(nvox, 0.7), np.full(nvox, 5.0), np.full(nvox, 2.0),
+                     thi, phi, psi], axis=1)
+    return Workload("noddi_bingham_gs_lm_mcmc", "NODDI_Bingham", cfp, meas, truth, init,
+                    s0_est[:, None].copy(), grid=BINGHAM_GRID)

@@ -34,7 +34,7 @@ def nvcc():
     raise FileNotFoundError("nvcc")
 
 
-MODELS = ("Ball_1_Stick", "NODDI_Watson", "DiffusionTensor", "Ball_2_Sticks")
+MODELS = ("Ball_1_Stick", "NODDI_Watson", "DiffusionTensor", "Ball_2_Sticks", "NODDI_Bingham")
 
 
 def build_cubins(reference, models=MODELS, jobs=8):

@@ -14,7 +14,7 @@ needed to run them):
   fit_<Model>.npz     grid search (Watson) and LM results of the oracle's
                       fitting loops driven by the reference plugin on
                       48 synthetic voxels.
-Models: Ball_1_Stick, NODDI_Watson, DiffusionTensor, Ball_2_Sticks.
+Models: Ball_1_Stick, NODDI_Watson, DiffusionTensor, Ball_2_Sticks, NODDI_Bingham.
 """
 import os
 import sys
@@ -50,6 +50,12 @@ def plugin_inputs(model, rng):
                       rng.uniform(-3, 3, n), rng.uniform(-3, 3, n), rng.uniform(0, 1, n) * (1 - f1),
                       rng.uniform(-3, 3, n), rng.uniform(-3, 3, n)], 1)
         F = np.zeros((n, 0))
+    elif model == "NODDI_Bingham":
+        k = np.exp(rng.uniform(np.log(0.3), np.log(64), n))
+        P = np.stack([rng.uniform(0, 0.6, n), rng.uniform(0.05, 1, n), k,
+                      rng.uniform(0, 1.1, n) * k, rng.uniform(-3, 3, n), rng.uniform(-3, 3, n),
+                      rng.uniform(-3, 3, n)], 1)
+        F = rng.uniform(500, 1500, (n, 1))
     else:
         k = np.concatenate([np.exp(rng.uniform(np.log(1e-3), np.log(64), n - 6)),
                             [0.0, 0.2, 2.0, 5.0, 12.0, 40.0]])
@@ -171,6 +177,21 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"fit_{model}.npz"), cfp=wl.cfp, meas=wl.meas,
                             init=wl.init, fixp=wl.fixp, lm=lm, lm_iters=it, lm_cost=co)
         print(model, "done")
+    rng = np.random.default_rng(20240603)
+    model = "NODDI_Bingham"
+    ref = Oracle(model, reference=True)
+    P, cfp, F = plugin_inputs(model, rng)
+    S, J = ref.signal(P, cfp, F, jac=True)
+    np.savez_compressed(os.path.join(HERE, f"plugin_{model}.npz"), params=P, cfp=cfp, fixp=F,
+                        signal=S, jacobian=J)
+    wl = synth.noddi_bingham(48, seed=77, signal_fn=lambda t, c, s0: ref.signal(t, c, s0[:, None]))
+    cfg = capi.model_cfg(model, grid=wl.grid)
+    gs, best, bc = ref.gridsearch(cfg, wl.meas, wl.init, wl.cfp, wl.fixp)
+    lm, it, su, co = ref.levmar(cfg, wl.meas, gs, wl.cfp, wl.fixp)
+    np.savez_compressed(os.path.join(HERE, f"fit_{model}.npz"), cfp=wl.cfp, meas=wl.meas,
+                        init=wl.init, fixp=wl.fixp, gs=gs, gs_best=best, gs_cost=bc, lm=lm,
+                        lm_iters=it, lm_cost=co)
+    print(model, "done")
 
 
 if __name__ == "__main__":

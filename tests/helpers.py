@@ -31,6 +31,12 @@ def b2s(nvox, seed=8219):
     return synth.ball_2_sticks(nvox, seed=seed)
 
 
+def bingham(nvox, seed=8219, snr=20.0):
+    o = oracle("NODDI_Bingham")
+    return synth.noddi_bingham(nvox, seed=seed, snr=snr,
+                               signal_fn=lambda t, cfp, s0: o.signal(t, cfp, s0[:, None]))
+
+
 def angle_deg(th1, ph1, th2, ph2):
     """Angle between two axes (sign-insensitive), degrees."""
     v1 = np.stack([np.sin(th1) * np.cos(ph1), np.sin(th1) * np.sin(ph1), np.cos(th1)], -1)

@@ -18,7 +18,7 @@ def declared():
     return sorted(set(re.findall(r"\b(cdm_[a-z_0-9]+)\s*\(", text)))
 
 
-MODELS = ["Ball_1_Stick", "NODDI_Watson", "DiffusionTensor", "Ball_2_Sticks"]
+MODELS = ["Ball_1_Stick", "NODDI_Watson", "DiffusionTensor", "Ball_2_Sticks", "NODDI_Bingham"]
 
 
 @pytest.mark.parametrize("model", MODELS)

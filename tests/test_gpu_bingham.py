@@ -1,0 +1,90 @@
+"""GPU parity for NODDI-Bingham (single-precision restatement) against the
+FP64 CPU oracle, with the tolerances of the other parity tests:
+  * predicted signal |dS| <= 2e-5 |S| + 2e-6 S0;
+  * grid search (CUDIMOT's 11,050-combination Bingham grid): the winning
+    combination is identical (FP32 ranking, FP64 re-check of near ties);
+  * LM from the grid-search result: final cost within 1e-4 relative and
+    fibre orientation within 0.5 degrees (>= 98 % of voxels);
+  * MCMC: posterior means within Monte Carlo error (batch-means z-scores,
+    |z| < 4 on >= 90 % of voxels, median |z| < 0.5) and SDs within 25 %;
+    the constraint kappa - 0.05 >= beta holds in every sample."""
+import numpy as np
+import pytest
+import torch
+
+from cudimot_gb300 import capi, synth
+from tests.helpers import angle_deg, bingham, oracle
+
+pytestmark = pytest.mark.gpu
+MODEL = "NODDI_Bingham"
+
+
+def T(x, dev):
+    return torch.as_tensor(np.ascontiguousarray(x, dtype=np.float64), device=dev)
+
+
+def test_predicted_signal(built, cuda):
+    wl = bingham(3000, seed=2)
+    lib = capi.Cudimot(MODEL, capi.model_cfg(MODEL))
+    pred = torch.zeros(wl.nvox, wl.nmeas, dtype=torch.float64, device=cuda)
+    lib.predicted_signal(T(wl.truth[:, :, None], cuda), T(wl.cfp, cuda), T(wl.fixp, cuda), pred)
+    torch.cuda.synchronize()
+    ref = oracle(MODEL).signal(wl.truth, wl.cfp, wl.fixp)
+    got = pred.cpu().numpy()
+    err = np.abs(got - ref)
+    assert np.all(err <= 2e-5 * np.abs(ref) + 2e-6 * wl.fixp), np.max(err / wl.fixp)
+
+
+def test_gridsearch_argmin_bit_exact(built, cuda):
+    wl = bingham(192, seed=3)
+    cfg = capi.model_cfg(MODEL, grid=wl.grid)
+    lib = capi.Cudimot(MODEL, cfg)
+    params = T(wl.init, cuda)
+    lib.gridsearch(T(wl.meas, cuda), params, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    torch.cuda.synchronize()
+    ref_p, _, _ = oracle(MODEL).gridsearch(cfg, wl.meas, wl.init, wl.cfp, wl.fixp)
+    assert np.array_equal(params.cpu().numpy(), ref_p)
+
+
+def test_levmar_after_gridsearch(built, cuda):
+    wl = bingham(512, seed=5)
+    o = oracle(MODEL)
+    cfg = capi.model_cfg(MODEL, grid=wl.grid)
+    gs_p, _, _ = o.gridsearch(cfg, wl.meas, wl.init, wl.cfp, wl.fixp)
+    lib = capi.Cudimot(MODEL, cfg)
+    params = T(gs_p, cuda)
+    lib.levmar(T(wl.meas, cuda), params, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    torch.cuda.synchronize()
+    got = params.cpu().numpy()
+    ref, _, _, _ = o.levmar(cfg, wl.meas, gs_p, wl.cfp, wl.fixp)
+    c_got = o.cost(wl.meas, got, wl.cfp, wl.fixp)
+    c_ref = o.cost(wl.meas, ref, wl.cfp, wl.fixp)
+    rel = (c_got - c_ref) / c_ref
+    ang = angle_deg(got[:, 4], got[:, 5], ref[:, 4], ref[:, 5])
+    assert np.mean(rel <= 1e-4) >= 0.98, np.quantile(rel, [0.5, 0.98, 1.0])
+    assert np.mean(ang <= 0.5) >= 0.98, np.quantile(ang, [0.5, 0.98, 1.0])
+
+
+def test_mcmc_posterior_matches_oracle(built, cuda):
+    wl = bingham(128, seed=21)
+    o = oracle(MODEL)
+    cfg = capi.model_cfg(MODEL, grid=wl.grid, run_mcmc=1, nburn=500, njumps=2000, sampleevery=10)
+    gs_p, _, _ = o.gridsearch(cfg, wl.meas, wl.init, wl.cfp, wl.fixp)
+    start, _, _, _ = o.levmar(cfg, wl.meas, gs_p, wl.cfp, wl.fixp)
+    lib = capi.Cudimot(MODEL, cfg)
+    samples = torch.zeros(wl.nvox, 7, 200, dtype=torch.float64, device=cuda)
+    lib.mcmc(T(wl.meas, cuda), T(start, cuda), T(wl.cfp, cuda), T(wl.fixp, cuda), samples)
+    torch.cuda.synchronize()
+    g = samples.cpu().numpy()
+    assert np.all(g[:, 2] - 0.05 >= g[:, 3] - 1e-6)
+    cfg2 = capi.model_cfg(MODEL, run_mcmc=1, nburn=500, njumps=2000, sampleevery=10, seed=12345)
+    _, r, _ = o.mcmc(cfg2, wl.meas, start, wl.cfp, wl.fixp)
+    for p in (0, 1, 2):
+        def se(x):
+            bm = x.reshape(x.shape[0], 10, -1).mean(2)
+            return bm.std(1, ddof=1) / np.sqrt(10)
+        z = (g[:, p].mean(1) - r[:, p].mean(1)) / np.sqrt(se(g[:, p]) ** 2 + se(r[:, p]) ** 2 + 1e-30)
+        assert abs(np.median(z)) < 0.5, (p, np.median(z))
+        assert np.mean(np.abs(z) < 4) > 0.9, (p, np.mean(np.abs(z) < 4))
+        ratio = np.median(g[:, p].std(1) / np.maximum(r[:, p].std(1), 1e-30))
+        assert 0.75 < ratio < 1.33, (p, ratio)

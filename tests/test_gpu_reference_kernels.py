@@ -173,3 +173,31 @@ def test_b2s_mcmc_vs_reference_kernels(built, cuda):
         assert np.mean(np.abs(z) < 4) > 0.85, (p, np.mean(np.abs(z) < 4))
         ratio = np.median(g[:, p].std(1) / np.maximum(r[:, p].std(1), 1e-30))
         assert 0.8 < ratio < 1.25, (p, ratio)
+
+
+def test_bingham_gridsearch_and_levmar_vs_reference_kernels(built, cuda):
+    need("NODDI_Bingham")
+    from tests.helpers import bingham
+    wl = bingham(256, seed=13)
+    cfg = capi.model_cfg("NODDI_Bingham", grid=synth.BINGHAM_GRID)
+    ref = rk.RefKernels("NODDI_Bingham", 7)
+    ours = capi.Cudimot("NODDI_Bingham", cfg)
+    grid = T(cfg.grid_array, cuda)
+    pr, po = T(wl.init, cuda), T(wl.init, cuda)
+    ref.gridsearch(cfg, T(wl.meas, cuda), pr, T(wl.cfp, cuda), T(wl.fixp, cuda), grid)
+    ours.gridsearch(T(wl.meas, cuda), po, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    torch.cuda.synchronize()
+    r, g = pr.cpu().numpy(), po.cpu().numpy()
+    same = np.all(r == g, axis=1)
+    assert same.mean() >= 0.98, same.mean()
+    o = oracle("NODDI_Bingham")
+    cr, cg = o.cost(wl.meas, r, wl.cfp, wl.fixp), o.cost(wl.meas, g, wl.cfp, wl.fixp)
+    assert np.all(cg[~same] <= cr[~same] * (1 + 1e-4))
+    pr2, po2 = T(r, cuda), T(r, cuda)
+    ref.levmar(cfg, T(wl.meas, cuda), pr2, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    ours.levmar(T(wl.meas, cuda), po2, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    torch.cuda.synchronize()
+    r2, g2 = pr2.cpu().numpy(), po2.cpu().numpy()
+    cr2, cg2 = o.cost(wl.meas, r2, wl.cfp, wl.fixp), o.cost(wl.meas, g2, wl.cfp, wl.fixp)
+    rel = (cg2 - cr2) / cr2
+    assert np.mean(rel <= 1e-4) >= 0.95, np.quantile(rel, [0.5, 0.95, 1])

@@ -3,6 +3,9 @@ fixtures produced by CUDIMOT's own plugins (tests/golden/make_golden.py).
 
 Ball_1_Stick: the restated plugin is CUDIMOT's formula for formula, so the
 signal matches exactly and the LM fit to rounding.
+NODDI_Bingham: restated for single precision (shifted saddlepoint, analytic
+d log H); in FP64 it equals CUDIMOT's plugin to 1e-9 S0 and picks the same
+grid-search winners.
 DiffusionTensor, Ball_2_Sticks: restated with CUDIMOT's operation order
 (and its quirks), so signal, Jacobian and the LM fit match bit for bit.
 NODDI_Watson: CUDIMOT's FP64 plugin loses precision in two places (its
@@ -96,3 +99,28 @@ def test_signal_jacobian_and_levmar_bit_exact_with_reference_plugin(built, model
                                         f["fixp"])
     assert np.array_equal(p, f["lm"])
     assert np.array_equal(it, f["lm_iters"])
+
+
+def test_bingham_matches_reference_plugin(built):
+    from cudimot_gb300 import synth
+    g = load("plugin_NODDI_Bingham.npz")
+    o = oracle("NODDI_Bingham")
+    S, J = o.signal(g["params"], g["cfp"], g["fixp"], jac=True)
+    assert np.max(np.abs(S - g["signal"]) / g["fixp"]) < 1e-9
+    for p in (0, 1, 4, 5, 6):  # analytic columns, and angles by central differences
+        d = np.abs(J[..., p] - g["jacobian"][..., p]).max() / np.abs(g["jacobian"][..., p]).max()
+        assert d < 1e-6, (p, d)
+    f = load("fit_NODDI_Bingham.npz")
+    cfg = capi.model_cfg("NODDI_Bingham", grid=synth.BINGHAM_GRID)
+    _, best, _ = o.gridsearch(cfg, f["meas"], f["init"], f["cfp"], f["fixp"])
+    assert np.mean(best == f["gs_best"]) >= 0.95
+    _, _, _, co = o.levmar(cfg, f["meas"], f["gs"], f["cfp"], f["fixp"])
+    assert np.median(np.abs(co - f["lm_cost"]) / f["lm_cost"]) < 1e-6
+
+
+def test_bingham_single_precision_signal(built):
+    g = load("plugin_NODDI_Bingham.npz")
+    o = oracle("NODDI_Bingham")
+    S64 = o.signal(g["params"], g["cfp"], g["fixp"])
+    S32 = o.signal(g["params"], g["cfp"], g["fixp"], prec=1)
+    assert np.max(np.abs(S32 - S64) / g["fixp"]) < 2e-6
