@@ -55,11 +55,13 @@ def parse():
     ap.add_argument("--nburn", type=int, default=NBURN)
     ap.add_argument("--njumps", type=int, default=NJUMPS)
     ap.add_argument("--workload", default="noddi_watson",
-                    choices=["noddi_watson", "ball_1_stick_lm", "heterogeneous", "learned_init"],
+                    choices=["noddi_watson", "ball_1_stick_lm", "heterogeneous", "learned_init",
+                             "noddi_bingham"],
                     help="noddi_watson: the headline (200k voxels GS->LM->MCMC); "
                          "ball_1_stick_lm: 10k voxels plain LM; heterogeneous: DiffusionTensor "
                          "400k + Ball_2_Sticks 300k + NODDI_Watson 500k LM+MCMC in one graph; "
-                         "learned_init: network-initialised vs grid-initialised NODDI_Watson")
+                         "learned_init: network-initialised vs grid-initialised NODDI_Watson; "
+                         "noddi_bingham: 1M voxels GS (11,050) -> LM -> MCMC, precision study")
     ap.add_argument("--train-signals", type=int, default=20_000_000)
     ap.add_argument("--lm-targets", type=int, default=1_000_000)
     ap.add_argument("--epochs", type=int, default=2)
@@ -537,6 +539,98 @@ def bench_learned(a, dev):
     print(json.dumps(line))
 
 
+def bench_bingham(a, dev):
+    """NODDI-Bingham precision study: --nvox voxels (default 1,000,000) of
+    the NODDI-Watson protocol and parameters plus beta = U(0,0.9) kappa and
+    psi ~ U(0,pi), SNR 20; grid search over CUDIMOT's 11,050-combination
+    Bingham grid -> LM -> MCMC (1250 + 1250, every 25th), FP32 model. The
+    per-parameter error of the GPU fit against the FP64 CPU oracle's fit of
+    the same voxels (LM from the same grid-search start, 256 voxels) and
+    the posterior-mean error against the truth are reported."""
+    import torch
+    from cudimot_gb300 import capi, synth
+    model = "NODDI_Bingham"
+    n = 1_000_000 if a.nvox == NVOX else a.nvox
+    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
+    lib0 = capi.Cudimot(model, capi.model_cfg(model))
+
+    def signal(truth, cfp, S0):
+        out = np.empty((truth.shape[0], cfp.shape[0]))
+        for r0 in range(0, truth.shape[0], 1 << 18):
+            tr = truth[r0:r0 + (1 << 18)]
+            clean = torch.zeros(tr.shape[0], cfp.shape[0], dtype=torch.float64, device=dev)
+            lib0.predicted_signal(t(tr[:, :, None]), t(cfp), t(S0[r0:r0 + tr.shape[0], None]), clean)
+            out[r0:r0 + tr.shape[0]] = clean.cpu().numpy()
+        return out
+
+    wl = synth.noddi_bingham(n, signal_fn=signal)
+    cfg = capi.model_cfg(model, grid=synth.BINGHAM_GRID, run_mcmc=1, nburn=NBURN, njumps=NJUMPS,
+                         sampleevery=SE)
+    lib = capi.Cudimot(model, cfg)
+    m, c, f, p0 = t(wl.meas), t(wl.cfp), t(wl.fixp), t(wl.init)
+    p = p0.clone()
+    samples = torch.zeros(n, 7, NJUMPS // SE, dtype=torch.float64, device=dev)
+    st = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    with ClockSampler(dev.index or 0) as clk:
+        torch.cuda.synchronize()
+        ev[0].record(st)
+        lib.gridsearch(m, p, c, f)
+        ev[1].record(st)
+        lib.levmar(m, p, c, f)
+        ev[2].record(st)
+        gs_lm = p.clone()
+        lib.mcmc(m, p, c, f, samples)
+        ev[3].record(st)
+        torch.cuda.synchronize()
+    ms = {"gridsearch": ev[0].elapsed_time(ev[1]), "levmar": ev[1].elapsed_time(ev[2]),
+          "mcmc": ev[2].elapsed_time(ev[3])}
+    total = sum(ms.values())
+    # precision study on a subset: LM in FP32 (GPU) vs FP64 (oracle) from the same start
+    from oracle.oracle import Oracle
+    o = Oracle(model)
+    k = 256
+    gs_only = p0[:k].clone()
+    lib.gridsearch(m[:k].contiguous(), gs_only, c, f[:k].contiguous())
+    torch.cuda.synchronize()
+    start = gs_only.cpu().numpy()
+    gpu_lm = start.copy()
+    q = t(start)
+    lib.levmar(m[:k].contiguous(), q, c, f[:k].contiguous())
+    torch.cuda.synchronize()
+    gpu_lm = q.cpu().numpy()
+    ref_lm, _, _, _ = o.levmar(cfg, wl.meas[:k], start, wl.cfp, wl.fixp[:k])
+    names = ["fiso", "fintra", "kappa", "beta"]
+    vs_oracle = {nm: float(np.median(np.abs(gpu_lm[:, i] - ref_lm[:, i]) /
+                                     np.maximum(np.abs(ref_lm[:, i]), 1e-3)))
+                 for i, nm in enumerate(names)}
+    nf = lambda th, ph: np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], 1)  # noqa
+    ang = np.degrees(np.arccos(np.clip(np.abs(np.sum(nf(gpu_lm[:, 4], gpu_lm[:, 5]) *
+                                                      nf(ref_lm[:, 4], ref_lm[:, 5]), 1)), 0, 1)))
+    vs_oracle["orientation_deg_median"] = float(np.median(ang))
+    c_gpu = o.cost(wl.meas[:k], gpu_lm, wl.cfp, wl.fixp[:k])
+    c_ref = o.cost(wl.meas[:k], ref_lm, wl.cfp, wl.fixp[:k])
+    vs_oracle["cost_rel_median"] = float(np.median((c_gpu - c_ref) / c_ref))
+    pm = samples.mean(2).cpu().numpy()
+    truth = wl.truth
+    vs_truth = {nm: float(np.sqrt(np.mean((pm[:, i] - truth[:, i]) ** 2))) for i, nm in
+                enumerate(names[:2])}
+    vs_truth["log_kappa_rmse"] = float(np.sqrt(np.mean((np.log(np.maximum(pm[:, 2], 1e-3)) -
+                                                        np.log(truth[:, 2])) ** 2)))
+    vs_truth["beta_over_kappa_rmse"] = float(np.sqrt(np.mean((pm[:, 3] / pm[:, 2] -
+                                                               truth[:, 3] / truth[:, 2]) ** 2)))
+    line = base_line("voxels/s fitted (GS+LM+MCMC), NODDI-Bingham", n / (total / 1e3), "voxels/s",
+                     a, total,
+                     {"workload": "noddi_bingham_gs_lm_mcmc", "model": model, "nvox": n, "nmeas": 288,
+                      "grid_combs": 11050, "nburn": NBURN, "njumps": NJUMPS, "sampleevery": SE,
+                      "l2": "inputs larger than L2 (no flush)"},
+                     clk.summary(), stages_ms=ms,
+                     lm_iterations_per_voxel=lib.stats().lm_iterations / (n + k),
+                     fp32_vs_fp64_oracle_lm=vs_oracle, posterior_mean_vs_truth=vs_truth,
+                     gpu_launches=9)
+    print(json.dumps(line))
+
+
 def main():
     a = parse()
     rank, world, local = dist_env()
@@ -548,7 +642,7 @@ def main():
         torch.cuda.set_device(local)
         dev = torch.device("cuda", local)
         {"ball_1_stick_lm": bench_b1s_lm, "heterogeneous": bench_heterogeneous,
-         "learned_init": bench_learned}[a.workload](a, dev)
+         "learned_init": bench_learned, "noddi_bingham": bench_bingham}[a.workload](a, dev)
         return
     if a.impl == "reference":
         if world > 1:
