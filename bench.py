@@ -45,7 +45,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--nvox", type=int, default=NVOX)
+    ap.add_argument("--nvox", type=int, default=None,
+                    help="voxels (default: the workload's own size)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="voxels for the CPU baseline")
     ap.add_argument("--profile-stage", choices=["gridsearch", "levmar", "mcmc", "mlp_forward"],
@@ -233,6 +234,7 @@ def profile_mlp_forward(a, dev):
     rng = np.random.default_rng(8219)
     cfp = synth.protocol(18, [(90, 1000.0), (90, 2000.0), (90, 3000.0)], rng)
     li = LearnedInit(MODEL, cfp, grid=synth.WATSON_GRID, seed=8219, device=dev)
+    a.nvox = a.nvox or 262144
     d = li.synth(a.nvox, seed=4242, snr=(20.0, 20.0), meas=True)
     li.predict(d["meas"], d["s0"])  # warm-up: 4 GEMM launches
     torch.cuda.synchronize()
@@ -253,6 +255,7 @@ def profile_stage(a):
     if a.profile_stage == "mlp_forward":
         profile_mlp_forward(a, dev)
         return
+    a.nvox = a.nvox or 20000
     cfp, meas, fixp, init, _ = make_workload(a.nvox, 8219, dev)
     cfg = capi.model_cfg(MODEL, grid=synth.WATSON_GRID, run_mcmc=1, nburn=a.nburn,
                          njumps=a.njumps, sampleevery=SE)
@@ -323,7 +326,7 @@ def bench_b1s_lm(a, dev):
     256 MB buffer is written before every timed step."""
     import torch
     from cudimot_gb300 import capi, synth
-    n = 10_000 if a.nvox == NVOX else a.nvox
+    n = a.nvox or 10_000
     wl = synth.ball_1_stick(n)
     cfg = capi.model_cfg("Ball_1_Stick", iter_levmar=200)
     lib = capi.Cudimot("Ball_1_Stick", cfg)
@@ -374,7 +377,7 @@ def bench_heterogeneous(a, dev):
     import torch
     from cudimot_gb300 import capi, synth
     t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
-    scale = a.nvox / NVOX if a.nvox != NVOX else 1.0
+    scale = a.nvox / 1_200_000 if a.nvox else 1.0
     vols = []
     wdt = synth.diffusion_tensor(int(400_000 * scale), snr=25.0)
     wb2 = synth.ball_2_sticks(int(300_000 * scale), snr=25.0)
@@ -550,7 +553,7 @@ def bench_bingham(a, dev):
     import torch
     from cudimot_gb300 import capi, synth
     model = "NODDI_Bingham"
-    n = 1_000_000 if a.nvox == NVOX else a.nvox
+    n = a.nvox or 1_000_000
     t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
     lib0 = capi.Cudimot(model, capi.model_cfg(model))
 
@@ -619,6 +622,28 @@ def bench_bingham(a, dev):
                                                         np.log(truth[:, 2])) ** 2)))
     vs_truth["beta_over_kappa_rmse"] = float(np.sqrt(np.mean((pm[:, 3] / pm[:, 2] -
                                                                truth[:, 3] / truth[:, 2]) ** 2)))
+    # CUDIMOT's own kernels (double, as shipped) on the first 512 voxels
+    refk = None
+    if os.environ.get("CDM_BENCH_REFK", "1") != "0":
+        try:
+            import time as _time
+            from oracle.refkernels.refkernels import RefKernels, available
+            if available(model):
+                rk = RefKernels(model, 7)
+                r = 512
+                pr = p0[:r].clone()
+                sr = torch.zeros(r, 7, NJUMPS // SE, dtype=torch.float64, device=dev)
+                torch.cuda.synchronize()
+                t0 = _time.perf_counter()
+                rk.gridsearch(cfg, m[:r].contiguous(), pr, c, f[:r].contiguous(), t(cfg.grid_array))
+                rk.levmar(cfg, m[:r].contiguous(), pr, c, f[:r].contiguous())
+                rk.mcmc(cfg, m[:r].contiguous(), pr, c, f[:r].contiguous(), sr)
+                torch.cuda.synchronize()
+                dt = _time.perf_counter() - t0
+                refk = {"value": r / dt, "unit": "voxels/s", "seconds": dt,
+                        "sample": f"first {r} voxels, grid search -> LM -> MCMC, CUDIMOT kernels"}
+        except Exception as e:  # noqa: BLE001
+            refk = {"unavailable": f"{type(e).__name__}: {e}"}
     line = base_line("voxels/s fitted (GS+LM+MCMC), NODDI-Bingham", n / (total / 1e3), "voxels/s",
                      a, total,
                      {"workload": "noddi_bingham_gs_lm_mcmc", "model": model, "nvox": n, "nmeas": 288,
@@ -627,7 +652,7 @@ def bench_bingham(a, dev):
                      clk.summary(), stages_ms=ms,
                      lm_iterations_per_voxel=lib.stats().lm_iterations / (n + k),
                      fp32_vs_fp64_oracle_lm=vs_oracle, posterior_mean_vs_truth=vs_truth,
-                     gpu_launches=9)
+                     reference_kernels=refk, gpu_launches=9)
     print(json.dumps(line))
 
 
@@ -657,7 +682,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     from cudimot_gb300 import capi
-    nvox = a.nvox
+    nvox = a.nvox or NVOX
     cfp, meas, fixp, init, truth = make_workload(nvox, 8219 + rank, dev)
     cfg = workload_cfg()
     lib = capi.Cudimot(MODEL, cfg)

@@ -53,6 +53,7 @@ CNT_MUFU(log_gpu, std::log) CNT_MUFU(exp_gpu, std::exp) CNT_MUFU(sin_gpu, std::s
 CNT_MUFU(cos_gpu, std::cos) CNT_MUFU(atan_gpu, std::atan) CNT_MUFU(tan_gpu, std::tan)
 CNT_MUFU(sqrt_gpu, std::sqrt) CNT_MUFU(acos_gpu, std::acos)
 inline cnt fabs_gpu(cnt x) { return cnt(std::fabs(x.v)); }
+inline cnt rcp_gpu(cnt x) { g_mufu++; return cnt(1.0 / x.v); }
 template <> struct cdm_bin<cnt> {
   static cnt mn(cnt a, cnt b) { return cnt(std::fmin(a.v, b.v)); }
   static cnt mx(cnt a, cnt b) { return cnt(std::fmax(a.v, b.v)); }

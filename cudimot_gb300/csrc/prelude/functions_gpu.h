@@ -54,6 +54,18 @@ CDM_UNARY(sqrt_gpu, sqrtf, sqrt)
 CDM_UNARY(acos_gpu, acosf, acos)
 #undef CDM_UNARY
 
+// rcp_gpu(x) = 1/x for the inner steps of iterative solvers in plugins: in
+// single precision the hardware reciprocal approximation (__fdividef, 2 ulp)
+// instead of the IEEE-rounded division sequence; exact 1/x in double.
+#if defined(__CUDA_ARCH__)
+FUNC float rcp_gpu(float x) { return __fdividef(1.0f, x); }
+FUNC fp32 rcp_gpu(fp32 x) { return fp32(__fdividef(1.0f, x.v)); }
+#else
+FUNC float rcp_gpu(float x) { return 1.0f / x; }
+FUNC fp32 rcp_gpu(fp32 x) { return fp32(1.0f / x.v); }
+#endif
+FUNC double rcp_gpu(double x) { return 1.0 / x; }
+
 // Integer arguments (e.g. sqrt_gpu(3)) follow C's promotion to double.
 template <class I, class = typename std::enable_if<std::is_integral<I>::value>::type>
 FUNC double sqrt_gpu(I x) { return sqrt((double)x); }

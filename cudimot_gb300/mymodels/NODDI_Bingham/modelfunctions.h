@@ -43,26 +43,37 @@ __host__ __device__ inline void Derived_CFP(const T* cfp, T* d) {
   d[1] = (T)(-b * BINGHAM_DPAR);
 }
 
+// Convergence test of the Newton iterations: a step below the working
+// precision of the iterate (relative 1e-7 in single, 1e-15 in double).
+MACRO bool bingham_done(T step, T x) {
+  return fabs_gpu(step) <= (T)(sizeof(T) == sizeof(double) ? 1e-15 : 1e-7) * fabs_gpu(x);
+}
+
+// Saddle point s in [1/2, 3/2]: root of h(s) = 1/(2s) + (A + 2s) / (2 q) - 1,
+// q = B + A s + s^2 (u1 + u2 = A + 2s, u1 u2 = q). h decreases and is
+// convex, so Newton from s = 1/2 rises monotonically onto the root.
+MACRO T bingham_saddle(T A, T B) {
+  T s = (T)0.5;
+#pragma unroll 1
+  for (int it = 0; it < 12; it++) {
+    const T q = B + A * s + s * s;
+    const T ps = A + (T)2.0 * s;
+    const T is = rcp_gpu(s), iq = rcp_gpu(q);
+    const T h = (T)0.5 * is + (T)0.5 * ps * iq - (T)1.0;
+    const T dh = -(T)0.5 * is * is + (T)0.5 * ((T)2.0 * q - ps * ps) * iq * iq;
+    const T step = h * rcp_gpu(dh);
+    s = min_gpu(max_gpu(s - step, (T)0.5), (T)1.5);
+    if (bingham_done(step, s)) break;
+  }
+  return s;
+}
+
 // Saddlepoint terms for eigenvalues x_max (gap 0) and two more with gap sum
 // A = e1 + e2 >= 0 and gap product B = e1 e2 >= 0:
 // returns F = s - log K2 / 2 - (log u_0 + log u_1 + log u_2) / 2 + T2,
 // so that log H = const + x_max + F.
 MACRO T bingham_F(T A, T B) {
-  // s: root of 1/(2s) + (A + 2s) / (2 (B + A s + s^2)) = 1 on [1/2, 3/2];
-  // the left side decreases and is convex, so Newton from s = 1/2 rises
-  // monotonically to the root.
-  T s = (T)0.5;
-#pragma unroll
-  for (int it = 0; it < 8; it++) {
-    const T q = B + A * s + s * s;     // u1 u2
-    const T ps = A + (T)2.0 * s;       // u1 + u2
-    const T h = (T)0.5 / s + (T)0.5 * ps / q - (T)1.0;
-    // d/ds [ps/q] = (2 q - ps^2) / q^2
-    const T dh = -(T)0.5 / (s * s) + (T)0.5 * ((T)2.0 * q - ps * ps) / (q * q);
-    const T step = h / dh;
-    s = s - step;
-    s = min_gpu(max_gpu(s, (T)0.5), (T)1.5);
-  }
+  const T s = bingham_saddle(A, B);
   const T q = B + A * s + s * s;
   const T ps = A + (T)2.0 * s;
   const T iq = (T)1.0 / q, is = (T)1.0 / s;
@@ -74,8 +85,9 @@ MACRO T bingham_F(T A, T B) {
   const T K2 = (T)0.5 * (is * is + s2);
   const T K3 = is * is * is + s3;
   const T K4 = (T)3.0 * (is * is * is * is + s4);
-  const T T2 = K4 / ((T)8.0 * K2 * K2) - (T)5.0 * K3 * K3 / ((T)24.0 * K2 * K2 * K2);
-  return s - (T)0.5 * log_gpu(K2) - (T)0.5 * (log_gpu(s) + log_gpu(q)) + T2;
+  const T iK2 = (T)1.0 / K2;
+  const T T2 = (T)0.125 * K4 * iK2 * iK2 - (T)(5.0 / 24.0) * K3 * K3 * iK2 * iK2 * iK2;
+  return s - (T)0.5 * log_gpu(K2) - (T)0.5 * log_gpu(s * q) + T2;
 }
 
 // Largest eigenvalue of D + c w w^T with D = diag(d) <= 0 (max 0) and
@@ -85,18 +97,26 @@ MACRO T bingham_F(T A, T B) {
 // x = 0 descends monotonically onto it (stopping when a step no longer
 // moves it). Also returns p'(root) = product of the two gaps below it.
 MACRO T bingham_top_eig(const T* d, const T* w2, T c, T& dp_root) {
-  T x = (T)0.0, dp = (T)1.0;
+  // start: the lowest Gershgorin upper bound that is still >= the root
+  // (the rows' centre + radius; never above 0)
+  const T aw0 = sqrt_gpu(w2[0]), aw1 = sqrt_gpu(w2[1]), aw2 = sqrt_gpu(w2[2]);
+  const T g0 = d[0] + c * w2[0] - c * aw0 * (aw1 + aw2);
+  const T g1 = d[1] + c * w2[1] - c * aw1 * (aw0 + aw2);
+  const T g2 = d[2] + c * w2[2] - c * aw2 * (aw0 + aw1);
+  T x = min_gpu(max_gpu(max_gpu(g0, g1), g2), (T)0.0), dp = (T)1.0;
 #pragma unroll 1
   for (int it = 0; it < 24; it++) {
     const T l0 = x - d[0], l1 = x - d[1], l2 = x - d[2];
     const T p = l0 * l1 * l2 - c * (w2[0] * l1 * l2 + w2[1] * l0 * l2 + w2[2] * l0 * l1);
     dp = l1 * l2 + l0 * l2 + l0 * l1 - c * (w2[0] * (l1 + l2) + w2[1] * (l0 + l2) + w2[2] * (l0 + l1));
     if (!(dp > (T)0.0)) break;
-    const T nx = x - p / dp;
-    if (!(nx < x)) break;
-    x = nx;
+    const T step = p * rcp_gpu(dp);
+    if (!(step > (T)0.0)) break;
+    x = x - step;
+    if (bingham_done(step, fabs_gpu(x) + fabs_gpu(c))) break;
   }
-  dp_root = dp;
+  const T l0 = x - d[0], l1 = x - d[1], l2 = x - d[2];
+  dp_root = l1 * l2 + l0 * l2 + l0 * l1 - c * (w2[0] * (l1 + l2) + w2[1] * (l0 + l2) + w2[2] * (l0 + l1));
   return x;
 }
 
@@ -128,16 +148,7 @@ MACRO void bingham_denominator(T beta, T kappa, T& L, T& dk, T& db) {
   const T A = e0 + e1 + e2;
   const T B = e0 * e1 + e0 * e2 + e1 * e2;
   L = bingham_F(A, B);  // log H - const - max(0, beta, kappa)
-  // the saddle point s again (as in bingham_F) for the u_i
-  T s = (T)0.5;
-#pragma unroll
-  for (int it = 0; it < 8; it++) {
-    const T q = B + A * s + s * s;
-    const T ps = A + (T)2.0 * s;
-    const T h = (T)0.5 / s + (T)0.5 * ps / q - (T)1.0;
-    const T dh = -(T)0.5 / (s * s) + (T)0.5 * ((T)2.0 * q - ps * ps) / (q * q);
-    s = min_gpu(max_gpu(s - h / dh, (T)0.5), (T)1.5);
-  }
+  const T s = bingham_saddle(A, B);
   const T u[3] = {e0 + s, e1 + s, e2 + s};
   T K2 = (T)0.0, K3 = (T)0.0, K4 = (T)0.0;
 #pragma unroll
