@@ -382,13 +382,20 @@ def bench_heterogeneous(a, dev):
     wdt = synth.diffusion_tensor(int(400_000 * scale), snr=25.0)
     wb2 = synth.ball_2_sticks(int(300_000 * scale), snr=25.0)
     cfp, meas, fixp, init, _ = make_workload(int(500_000 * scale), 8219, dev, snr=25.0)
+    from cudimot_gb300 import autotune
+    tuned = {}
     for model, m, c, f, i in (("DiffusionTensor", wdt.meas, wdt.cfp, wdt.fixp, wdt.init),
                               ("Ball_2_Sticks", wb2.meas, wb2.cfp, wb2.fixp, wb2.init),
                               ("NODDI_Watson", meas, cfp, fixp, init)):
-        cfg = capi.model_cfg(model, run_mcmc=1, nburn=NBURN, njumps=NJUMPS, sampleevery=SE)
+        dm, dc, df, di = t(m), t(c), t(f), t(i)
+        # lane counts per stage from the autotuner, timed on this volume's data
+        choice = autotune.tune(model, dm, di, dc, df, stages=("levmar", "mcmc"), reps=1)
+        tuned[model] = choice
+        cfg = capi.model_cfg(model, run_mcmc=1, nburn=NBURN, njumps=NJUMPS, sampleevery=SE,
+                             **autotune.lanes_kwargs(choice))
         npar = i.shape[1]
-        d = dict(model=model, lib=capi.Cudimot(model, cfg), meas=t(m), cfp=t(c), fixp=t(f),
-                 init=t(i), params=t(i),
+        d = dict(model=model, lib=capi.Cudimot(model, cfg), meas=dm, cfp=dc, fixp=df,
+                 init=di, params=di.clone(),
                  samples=torch.zeros(m.shape[0], npar, NJUMPS // SE, dtype=torch.float64, device=dev))
         vols.append(d)
     total = sum(v["meas"].shape[0] for v in vols)
@@ -421,7 +428,8 @@ def bench_heterogeneous(a, dev):
                                    "nmeas": int(v["meas"].shape[1])} for v in vols],
                       "nburn": NBURN, "njumps": NJUMPS, "sampleevery": SE,
                       "l2": "inputs larger than L2 (no flush)",
-                      "launch": "one CUDA graph, one branch per volume"},
+                      "launch": "one CUDA graph, one branch per volume",
+                      "lanes_from_autotuner": tuned},
                      clk.summary(), sequential={"value": total / (ms_s / 1e3), "ms_per_step": ms_s},
                      gpu_launches=sum(9 for _ in vols) * a.steps)
     print(json.dumps(line))
