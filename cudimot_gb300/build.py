@@ -183,6 +183,24 @@ def build_mlp(force=False):
     return out, None
 
 
+def build_utils(force=False):
+    """DTI initialiser, post-processing and part files (include/cdm_utils.h)."""
+    src = os.path.join(CSRC, "utils", "cdm_utils.cu")
+    hdr = os.path.join(ROOT, "include", "cdm_utils.h")
+    out = os.path.join(LIBDIR, "libcdm_utils.so")
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(src),
+                                                                          os.path.getmtime(hdr)):
+        return out, None
+    os.makedirs(LIBDIR, exist_ok=True)
+    cmd = [nvcc_path(), "-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-shared",
+           "-I", os.path.join(ROOT, "include"), src, "-o", out + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return out, (r.stdout + r.stderr)[-4000:]
+    os.replace(out + ".tmp", out)
+    return out, None
+
+
 def build_all(models=None, model_dirs=(), jobs=None, verbose=False, force=False):
     todo = [(os.path.join(MODELS, m), m) for m in (models or shipped_models())]
     todo += [(d, None) for d in model_dirs]
@@ -193,6 +211,7 @@ def build_all(models=None, model_dirs=(), jobs=None, verbose=False, force=False)
         futs[ex.submit(build_peak, force)] = ("peak", None)
         futs[ex.submit(build_batch, force)] = ("batch", None)
         futs[ex.submit(build_mlp, force)] = ("mlp", None)
+        futs[ex.submit(build_utils, force)] = ("utils", None)
         for f in cf.as_completed(futs):
             out, err = f.result()
             if err:
