@@ -226,6 +226,22 @@ cdm_status cdm_dti_fit(int nvox, int nmeas, const double* meas, const double* bv
     return fail(CDM_BAD_ARG, "bad argument (the tensor fit needs at least 7 measurements)");
   if (nmeas > kDtiMaxMeas)
     return fail(CDM_BAD_ARG, "cdm_dti_fit supports at most 512 measurements");
+  // the gradient table may be in host or device memory; the design matrix
+  // is formed on the host
+  std::vector<double> hg((size_t)nmeas * 3), hb((size_t)nmeas);
+  for (int k = 0; k < 2; k++) {
+    const void* src = k == 0 ? (const void*)bvecs : (const void*)bvals;
+    void* dst = k == 0 ? (void*)hg.data() : (void*)hb.data();
+    const size_t bytes = (k == 0 ? 3 : 1) * (size_t)nmeas * sizeof(double);
+    cudaPointerAttributes attr;
+    const cudaError_t e = cudaPointerGetAttributes(&attr, src);
+    if (e == cudaSuccess && attr.type == cudaMemoryTypeDevice) {
+      U_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    } else {
+      cudaGetLastError();  // an unregistered host pointer is not an error here
+      std::memcpy(dst, src, bytes);
+    }
+  }
   dti_args* a = new dti_args();
   a->nvox = nvox;
   a->nmeas = nmeas;
@@ -233,7 +249,7 @@ cdm_status cdm_dti_fit(int nvox, int nmeas, const double* meas, const double* bv
   a->out = out;
   std::vector<double> X((size_t)nmeas * 7);
   for (int m = 0; m < nmeas; m++) {
-    const double gx = bvecs[3 * m], gy = bvecs[3 * m + 1], gz = bvecs[3 * m + 2], b = bvals[m];
+    const double gx = hg[3 * m], gy = hg[3 * m + 1], gz = hg[3 * m + 2], b = hb[m];
     const double r[7] = {1.0, -b * gx * gx, -b * gy * gy, -b * gz * gz, -2 * b * gx * gy,
                          -2 * b * gx * gz, -2 * b * gy * gz};
     for (int j = 0; j < 7; j++) X[(size_t)m * 7 + j] = r[j];

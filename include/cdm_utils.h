@@ -39,8 +39,9 @@ enum {
  * decomposition of the tensor (descending eigenvalues); theta/phi of V1
  * and V2 (cart2spherical); psi = angle of V2 in the plane orthogonal to
  * V1 from the fanning direction at psi = 0 (NODDI-Bingham's
- * parameterisation, as initialise_Psi.cc). meas [nvox][nmeas],
- * bvecs [nmeas][3], bvals [nmeas], out [nvox][CDM_DTI_NOUT]. */
+ * parameterisation, as initialise_Psi.cc). meas [nvox][nmeas] and
+ * out [nvox][CDM_DTI_NOUT] on the device; bvecs [nmeas][3] and bvals
+ * [nmeas] in host or device memory (at most 512 measurements). */
 cdm_status cdm_dti_fit(int nvox, int nmeas, const double* meas, const double* bvecs,
                        const double* bvals, double* out, void* stream);
 
