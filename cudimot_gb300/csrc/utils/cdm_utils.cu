@@ -182,6 +182,27 @@ __global__ void od_kernel(int n, const double* __restrict__ k, int stride, doubl
     od[v] = 0.63661977236758134 * atan(1.0 / k[(size_t)v * stride]);
 }
 
+__global__ void mean_cols_kernel(int nvox, int nmeas, const double* __restrict__ meas,
+                                 const int* __restrict__ idx, int nidx, double* __restrict__ out,
+                                 int out_ld) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nvox; v += gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int k = 0; k < nidx; k++) acc += meas[(size_t)v * nmeas + idx[k]];
+    out[(size_t)v * out_ld] = acc / nidx;
+  }
+}
+
+__global__ void copy_cols_kernel(int nvox, const double* __restrict__ src, int src_ld, int src_col,
+                                 double* __restrict__ dst, int dst_ld, int dst_col, int ncols,
+                                 double scale, int fill, double value) {
+  const size_t n = (size_t)nvox * ncols;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t v = i / ncols, c = i % ncols;
+    dst[v * dst_ld + dst_col + c] = fill ? value : scale * src[v * src_ld + src_col + c];
+  }
+}
+
 int grid_for(size_t n, int t = 256) { return (int)std::min<size_t>((n + t - 1) / t, 152 * 8); }
 
 // 7x7 Gauss-Jordan inverse with partial pivoting (host, double).
@@ -307,6 +328,30 @@ cdm_status cdm_od_from_kappa(int nvox, const double* src, int stride, double* od
   if (nvox < 0 || !src || !od || stride <= 0) return fail(CDM_BAD_ARG, "bad argument");
   if (nvox == 0) return CDM_OK;
   od_kernel<<<grid_for(nvox), 256, 0, (cudaStream_t)stream>>>(nvox, src, stride, od);
+  U_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+cdm_status cdm_mean_columns(int nvox, int nmeas, const double* meas, const int* idx, int nidx,
+                            double* out, int out_ld, void* stream) {
+  if (nvox < 0 || nmeas <= 0 || !meas || !idx || nidx <= 0 || !out || out_ld <= 0)
+    return fail(CDM_BAD_ARG, "bad argument");
+  if (nvox == 0) return CDM_OK;
+  mean_cols_kernel<<<grid_for(nvox), 256, 0, (cudaStream_t)stream>>>(nvox, nmeas, meas, idx, nidx,
+                                                                     out, out_ld);
+  U_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
+cdm_status cdm_copy_columns(int nvox, const double* src, int src_ld, int src_col, double* dst,
+                            int dst_ld, int dst_col, int ncols, double scale, void* stream) {
+  if (nvox < 0 || !dst || ncols <= 0 || dst_ld < dst_col + ncols || dst_col < 0 ||
+      (src && (src_ld < src_col + ncols || src_col < 0)))
+    return fail(CDM_BAD_ARG, "bad argument");
+  if (nvox == 0) return CDM_OK;
+  copy_cols_kernel<<<grid_for((size_t)nvox * ncols), 256, 0, (cudaStream_t)stream>>>(
+      nvox, src, src_ld, src_col, dst, dst_ld, dst_col, ncols, src ? scale : 0.0, src ? 0 : 1,
+      scale);
   U_CUDA(cudaGetLastError());
   return CDM_OK;
 }

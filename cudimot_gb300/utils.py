@@ -25,6 +25,8 @@ def lib():
             "cdm_sample_stats": [i, i, i, vp, vp, vp, vp],
             "cdm_dyads": [i, i, i, vp, i, i, vp, vp],
             "cdm_od_from_kappa": [i, vp, i, vp, vp],
+            "cdm_mean_columns": [i, i, vp, vp, i, vp, i, vp],
+            "cdm_copy_columns": [i, vp, i, i, vp, i, i, i, C.c_double, vp],
             "cdm_part_path": [cp, i, cp, C.c_char_p, i],
             "cdm_part_write": [cp, i, i, vp],
             "cdm_part_read": [cp, C.POINTER(i), C.POINTER(i), vp, i64],
@@ -55,14 +57,25 @@ def _stream():
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
-def dti_fit(meas, bvecs, bvals):
-    """meas [n][nmeas], bvecs [nmeas][3], bvals [nmeas] (CUDA float64) ->
-    [n][17] (columns DTI_COLS)."""
+def _hd(x):
+    """Pointer of a CUDA tensor or a numpy array (host)."""
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data_as(C.c_void_p)
+    return C.c_void_p(x.contiguous().data_ptr())
+
+
+def dti_fit(meas, bvecs, bvals, out=None):
+    """meas [n][nmeas] (CUDA float64), bvecs [nmeas][3], bvals [nmeas]
+    (numpy or CUDA) -> [n][17] (columns DTI_COLS)."""
     import torch
     n, nm = meas.shape
-    out = torch.empty(n, len(DTI_COLS), dtype=torch.float64, device=meas.device)
-    _check(lib().cdm_dti_fit(n, nm, _d(meas), _d(bvecs.contiguous()), _d(bvals.contiguous()),
-                             _d(out), _stream()), "dti_fit")
+    if out is None:
+        out = torch.empty(n, len(DTI_COLS), dtype=torch.float64, device=meas.device)
+    keep = (bvecs, bvals)
+    bv = np.ascontiguousarray(bvecs, dtype=np.float64) if isinstance(bvecs, np.ndarray) else bvecs.contiguous()
+    bb = np.ascontiguousarray(bvals, dtype=np.float64) if isinstance(bvals, np.ndarray) else bvals.contiguous()
+    _check(lib().cdm_dti_fit(n, nm, _d(meas), _hd(bv), _hd(bb), _d(out), _stream()), "dti_fit")
+    del keep
     return out
 
 
@@ -71,25 +84,52 @@ def sample_stats(samples):
     n, p, s = samples.shape
     mean = torch.empty(n, p, dtype=torch.float64, device=samples.device)
     sd = torch.empty_like(mean)
-    _check(lib().cdm_sample_stats(n, p, s, _d(samples), _d(mean), _d(sd), _stream()), "sample_stats")
+    sample_stats_into(samples, mean, sd)
     return mean, sd
+
+
+def sample_stats_into(samples, mean, sd=None):
+    n, p, s = samples.shape
+    _check(lib().cdm_sample_stats(n, p, s, _d(samples), _d(mean), _d(sd), _stream()), "sample_stats")
 
 
 def dyads(samples, ith, iph):
     import torch
-    n, p, s = samples.shape
-    out = torch.empty(n, 4, dtype=torch.float64, device=samples.device)
-    _check(lib().cdm_dyads(n, p, s, _d(samples), ith, iph, _d(out), _stream()), "dyads")
+    out = torch.empty(samples.shape[0], 4, dtype=torch.float64, device=samples.device)
+    dyads_into(samples, ith, iph, out)
     return out
 
 
-def od_from_kappa(kappa_col):
+def dyads_into(samples, ith, iph, out):
+    n, p, s = samples.shape
+    _check(lib().cdm_dyads(n, p, s, _d(samples), ith, iph, _d(out), _stream()), "dyads")
+
+
+def od_from_kappa(kappa_col, out=None):
     """kappa_col: CUDA float64 tensor [n] or a column view (any stride)."""
     import torch
     n = kappa_col.shape[0]
-    out = torch.empty(n, dtype=torch.float64, device=kappa_col.device)
-    _check(lib().cdm_od_from_kappa(n, _d(kappa_col), kappa_col.stride(0), _d(out), _stream()), "od")
+    if out is None:
+        out = torch.empty(n, dtype=torch.float64, device=kappa_col.device)
+    _check(lib().cdm_od_from_kappa(n, C.c_void_p(kappa_col.data_ptr()), kappa_col.stride(0), _d(out),
+                                   _stream()), "od")
     return out
+
+
+def mean_columns(meas, idx, out, out_ld=None):
+    """out[v * out_ld] = mean(meas[v, idx]); idx an int32 CUDA tensor."""
+    n, nm = meas.shape
+    _check(lib().cdm_mean_columns(n, nm, _d(meas), C.c_void_p(idx.data_ptr()), idx.shape[0], _d(out),
+                                  out_ld or out.stride(0), _stream()), "mean_columns")
+
+
+def copy_columns(src, src_col, dst, dst_col, ncols, scale=1.0):
+    """dst[:, dst_col:dst_col+ncols] = scale * src[:, src_col:...] (src None:
+    fill with scale)."""
+    n = dst.shape[0]
+    _check(lib().cdm_copy_columns(n, _d(src), 0 if src is None else src.stride(0), src_col, _d(dst),
+                                  dst.stride(0), dst_col, ncols, float(scale), _stream()),
+           "copy_columns")
 
 
 def part_path(partsdir, id_part, name):

@@ -60,6 +60,16 @@ cdm_status cdm_dyads(int nvox, int nparams, int nsamples, const double* samples,
 /* OD = 2/pi atan(1/kappa) for kappa = src[v * stride] -> od [nvox]. */
 cdm_status cdm_od_from_kappa(int nvox, const double* src, int stride, double* od, void* stream);
 
+/* out[v * out_ld] = mean of meas[v][idx[k]], k < nidx (idx on the device):
+ * the S0 of the pipelines (mean of the b <= 50 volumes,
+ * Pipeline_NODDI_Watson.sh:155-170). */
+cdm_status cdm_mean_columns(int nvox, int nmeas, const double* meas, const int* idx, int nidx,
+                            double* out, int out_ld, void* stream);
+/* dst[v][dst_col + c] = scale * src[v][src_col + c] for c < ncols, or
+ * = scale when src is null: parameter columns between pipeline steps. */
+cdm_status cdm_copy_columns(int nvox, const double* src, int src_ld, int src_col, double* dst,
+                            int dst_ld, int dst_col, int ncols, double scale, void* stream);
+
 /* "<partsdir>/part_<id_part>/<name>" into buf (CDM_BAD_ARG if too long). */
 cdm_status cdm_part_path(const char* partsdir, int id_part, const char* name, char* buf,
                          int buflen);

@@ -1,0 +1,94 @@
+"""Pipelines restating CUDIMOT's Pipeline_<Model>.sh on the GPU:
+  * NODDI-Watson (S0 from the b=0 volumes, tensor fit, grid search with the
+    orientation fixed, fractions with kappa and orientation fixed, full
+    fit, finish) replayed from one captured CUDA graph equals the same
+    steps run eagerly, bit for bit, and twice in a row;
+  * the steps do what the scripts do: the grid search leaves theta/phi at
+    the tensor fit's V1, FitFractions leaves kappa at the grid value, and
+    the final fit's cost is no worse than the grid search's;
+  * Ball_1_Stick's one-step pipeline from the tensor fit matches LM from
+    the same initial values."""
+import numpy as np
+import pytest
+import torch
+
+from cudimot_gb300 import capi
+from cudimot_gb300.pipeline import Pipeline
+from tests.helpers import b1s, oracle, watson
+
+pytestmark = pytest.mark.gpu
+
+
+def T(x, dev):
+    return torch.as_tensor(np.ascontiguousarray(x, dtype=np.float64), device=dev)
+
+
+def test_watson_pipeline_graph_equals_eager(built, cuda):
+    wl = watson(2048, seed=31)
+    m = T(wl.meas, cuda)
+    eager = Pipeline("NODDI_Watson", m, wl.cfp[:, :3], wl.cfp[:, 3], run_mcmc=True, nburn=100,
+                     njumps=100, sampleevery=10)
+    eager.run(graph=False)
+    torch.cuda.synchronize()
+    g = Pipeline("NODDI_Watson", m, wl.cfp[:, :3], wl.cfp[:, 3], run_mcmc=True, nburn=100,
+                 njumps=100, sampleevery=10)
+    g.run()
+    torch.cuda.synchronize()
+    first = g.samples.clone()
+    g.run()
+    torch.cuda.synchronize()
+    assert torch.equal(g.samples, first)
+    assert torch.equal(g.samples, eager.samples)
+    assert torch.equal(g.fixp, eager.fixp)
+    assert torch.equal(g.od, eager.od) and torch.equal(g.dyads, eager.dyads)
+    s0 = wl.meas[:, wl.cfp[:, 3] <= 50].mean(1)
+    np.testing.assert_allclose(g.fixp.cpu().numpy()[:, 0], s0, rtol=1e-12)
+
+
+def test_watson_pipeline_steps(built, cuda):
+    wl = watson(1024, seed=32)
+    m = T(wl.meas, cuda)
+    pl = Pipeline("NODDI_Watson", m, wl.cfp[:, :3], wl.cfp[:, 3])
+    # step by step, inspecting the shared parameter array
+    from cudimot_gb300 import utils
+    utils.mean_columns(m, pl.b0, pl.fixp)
+    utils.dti_fit(m, pl.bvecs, pl.bvals, out=pl.dti)
+    for p, col, scale in pl.spec["init"]:
+        if col is None:
+            utils.copy_columns(None, 0, pl.params, p, 1, scale)
+        else:
+            utils.copy_columns(pl.dti, utils.DTI_COLS.index(col), pl.params, p, 1, scale)
+    st, lib, samples = pl.ctx[0]
+    lib.fit_enqueue(m, pl.params, pl.cfp, pl.fixp, samples)
+    torch.cuda.synchronize()
+    after_gs = pl.params.cpu().numpy().copy()
+    np.testing.assert_array_equal(after_gs[:, 3:5], pl.dti.cpu().numpy()[:, 12:14])
+    st, lib, samples = pl.ctx[1]
+    lib.fit_enqueue(m, pl.params, pl.cfp, pl.fixp, samples)
+    torch.cuda.synchronize()
+    after_ff = pl.params.cpu().numpy().copy()
+    np.testing.assert_array_equal(after_ff[:, 2:5], after_gs[:, 2:5])
+    st, lib, samples = pl.ctx[2]
+    lib.fit_enqueue(m, pl.params, pl.cfp, pl.fixp, samples)
+    torch.cuda.synchronize()
+    final = pl.params.cpu().numpy()
+    o = oracle("NODDI_Watson")
+    f = pl.fixp.cpu().numpy()
+    c_gs = o.cost(wl.meas, after_gs, wl.cfp, f)
+    c_fin = o.cost(wl.meas, final, wl.cfp, f)
+    assert np.mean(c_fin <= c_gs * (1 + 1e-6)) >= 0.99
+
+
+def test_ball_1_stick_pipeline(built, cuda):
+    wl = b1s(2048, seed=33)
+    m = T(wl.meas, cuda)
+    pl = Pipeline("Ball_1_Stick", m, wl.cfp[:, :3], wl.cfp[:, 3])
+    pl.run()
+    torch.cuda.synchronize()
+    d = pl.dti.cpu().numpy()
+    init = np.stack([d[:, 0], d[:, 1], d[:, 10], d[:, 12], d[:, 13]], 1)
+    lib = capi.Cudimot("Ball_1_Stick", capi.model_cfg("Ball_1_Stick"))
+    q = T(init, cuda)
+    lib.levmar(m, q, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    torch.cuda.synchronize()
+    assert torch.equal(pl.params, q)
