@@ -56,6 +56,10 @@ __device__ __forceinline__ void cdm_lm_inv_transform(const cdm_limits& L, fp32* 
   for (int p = 0; p < kNP; p++) {
     const float lo = L.bmin[p], hi = L.bmax[p];
     float x = (float)P[p];
+    if (L.fixed[p]) {  // a fixed parameter never moves: no round trip through the transform
+      Pt[p] = x;
+      continue;
+    }
     if (L.btype[p] == BMIN) {
       Pt[p] = logf(x - lo);
     } else if (L.btype[p] == BMAX) {
@@ -76,6 +80,7 @@ __device__ __forceinline__ void cdm_lm_transform(const cdm_limits& L, fp32* P, f
 #pragma unroll
   for (int p = 0; p < kNP; p++) {
     const float lo = L.bmin[p], hi = L.bmax[p];
+    if (L.fixed[p]) continue;
     if (L.btype[p] == BMIN) {
       P[p] = fp32(expf(Pt[p]) + lo);
     } else if (L.btype[p] == BMAX) {
@@ -285,7 +290,13 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
   FixConstraintsLM(NPARAMS, P);
   if (lane == 0) {
 #pragma unroll
-    for (int p = 0; p < kNP; p++) a.params[(size_t)v * kNP + p] = (double)(float)P[p];
+    for (int p = 0; p < kNP; p++) {
+      // a fixed parameter that FixConstraintsLM left alone keeps its input
+      // value in full double precision
+      const double in = a.params[(size_t)v * kNP + p];
+      a.params[(size_t)v * kNP + p] =
+          (L.fixed[p] && (float)P[p] == (float)in) ? in : (double)(float)P[p];
+    }
     if (a.iter_count) atomicAdd(a.iter_count, (unsigned long long)passes);
     if (a.succ_count) atomicAdd(a.succ_count, (unsigned long long)nsucc);
   }

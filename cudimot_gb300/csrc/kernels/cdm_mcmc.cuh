@@ -264,7 +264,9 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
         if (s < a.nsamples && lane == 0) {
           double* dst = a.samples + (size_t)v * kNP * a.nsamples + s;
 #pragma unroll
-          for (int p = 0; p < kNP; p++) dst[(size_t)p * a.nsamples] = (double)(float)P[p];
+          for (int p = 0; p < kNP; p++)  // fixed parameters: their input value, in double
+            dst[(size_t)p * a.nsamples] =
+                L.fixed[p] ? a.params[(size_t)v * kNP + p] : (double)(float)P[p];
           if (RICIAN && a.tau_samples) a.tau_samples[(size_t)v * a.nsamples + s] = (double)tau;
         }
       }
@@ -287,6 +289,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
   }
   if (lane == 0) {
 #pragma unroll
-    for (int p = 0; p < kNP; p++) a.params[(size_t)v * kNP + p] = (double)(float)P[p];
+    for (int p = 0; p < kNP; p++)
+      if (!L.fixed[p]) a.params[(size_t)v * kNP + p] = (double)(float)P[p];
   }
 }
