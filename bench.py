@@ -775,33 +775,50 @@ def main():
     print(json.dumps(line))
 
 
-def reference_kernels_leg(cfp, meas, fixp, init, cfg, dev, n=2048):
+def reference_kernels_leg(cfp, meas, fixp, init, cfg, dev, n=2048, n_float=8192):
     """CUDIMOT's own GridSearch/LM/MCMC kernels (unmodified sources compiled
-    for sm_103a, T = double as shipped) on the first n voxels of this
-    workload, same GPU; wall time of the three stages."""
+    for sm_103a) on the first voxels of this workload, same GPU; wall time of
+    the three stages. T = double as the plugins ship (n voxels), and CUDIMOT's
+    float instantiation of the same kernels (n_float voxels)."""
     import time
     import torch
     try:
         from oracle.refkernels.refkernels import RefKernels, available
         if not available(MODEL):
             return {"unavailable": "CUDIMOT kernels were not compiled (source tree absent at build time)"}
-        ref = RefKernels(MODEL, 5)
+        RefKernels(MODEL, 5)
     except Exception as e:  # noqa: BLE001
         return {"unavailable": f"{type(e).__name__}: {e}"}
-    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
-    m, c, f, p = t(meas[:n]), t(cfp), t(fixp[:n]), t(init[:n])
-    s = torch.zeros(n, 5, NJUMPS // SE, dtype=torch.float64, device=dev)
-    grid = t(cfg.grid_array)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    ref.gridsearch(cfg, m, p, c, f, grid)
-    ref.levmar(cfg, m, p, c, f)
-    ref.mcmc(cfg, m, p, c, f, s)
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
-    return {"value": n / dt, "unit": "voxels/s", "seconds": dt,
-            "sample": f"first {n} voxels of this workload, grid search -> LM -> MCMC, "
-                      "one warp per voxel as CUDIMOT launches them"}
+
+    def run(k, real):
+        ref = RefKernels(MODEL, 5, real=real)
+        t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=real, device=dev)  # noqa
+        m, c, f, p = t(meas[:k]), t(cfp), t(fixp[:k]), t(init[:k])
+        s = torch.zeros(k, 5, NJUMPS // SE, dtype=real, device=dev)
+        grid = t(cfg.grid_array)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ref.gridsearch(cfg, m, p, c, f, grid)
+        ref.levmar(cfg, m, p, c, f)
+        ref.mcmc(cfg, m, p, c, f, s)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, s
+
+    dt, _ = run(n, torch.float64)
+    out = {"value": n / dt, "unit": "voxels/s", "seconds": dt,
+           "sample": f"first {n} voxels of this workload, grid search -> LM -> MCMC, "
+                     "one warp per voxel as CUDIMOT launches them, T = double"}
+    try:
+        k = min(n_float, len(meas))
+        dtf, sf = run(k, torch.float32)
+        means = sf.mean(2)
+        out["float"] = {"value": k / dtf, "unit": "voxels/s", "seconds": dtf,
+                        "sample": f"first {k} voxels, CUDIMOT's float instantiation "
+                                  "(MyType = float) of the same kernels",
+                        "finite_posterior_means": float(torch.isfinite(means).all(1).float().mean())}
+    except Exception as e:  # noqa: BLE001
+        out["float"] = {"unavailable": f"{type(e).__name__}: {e}"}
+    return out
 
 
 def gpu_launches_per_step(cfg):

@@ -7,8 +7,10 @@
 // BIC_AIC.cu and getPredictedSignal.cu for sm_103a. The CUDIMOT host classes
 // need FSL, so this file does what their constructors and run() methods do
 // (same __constant__ uploads, launch shapes and dynamic shared memory),
-// through the CUDA driver API, for T = double (the MyType of the plugins).
-// Line references are to those files.
+// through the CUDA driver API, for T = double (the MyType of the plugins)
+// or T = float (CUDIMOT instantiates every method for both, e.g.
+// GridSearch.cu:320-321; ref_set_real selects which). Line references are
+// to those files.
 //
 // The reference kernels process whole blocks of voxels without a bounds
 // check (VOXELS_BLOCK = 8 for GridSearch/MCMC/BIC/predicted signal, 2 for
@@ -29,6 +31,9 @@ CUmodule g_mod[5] = {};
 enum { M_GS = 0, M_LM, M_MCMC, M_BIC, M_PRED };
 const char* kFiles[5] = {"GridSearch", "Levenberg_Marquardt", "MCMC", "BIC_AIC", "getPredictedSignal"};
 char g_err[512];
+// T of the launched kernels: 'd' (double) or 'f' (float), its size in bytes
+char g_t = 'd';
+size_t g_ts = sizeof(double);
 
 int fail(const char* what, CUresult r) {
   const char* s = nullptr;
@@ -74,6 +79,16 @@ extern "C" {
 
 const char* ref_last_error() { return g_err; }
 
+// Select T for the following calls: bytes 8 = double, 4 = float. Every
+// array argument (meas, params, CFP, FixP, grid, samples, tau, outputs) is
+// then a T array.
+int ref_set_real(int bytes) {
+  if (bytes != 4 && bytes != 8) return -1;
+  g_t = bytes == 4 ? 'f' : 'd';
+  g_ts = (size_t)bytes;
+  return 0;
+}
+
 // Load the five cubins of one model from dir/<File>.cubin into the primary
 // context of device 0 (the context the CUDA runtime uses too).
 int ref_load(const char* dir) {
@@ -104,9 +119,10 @@ int ref_gridsearch(int nparams, int nvox, int nmeas, int cfp_size, int fixp_size
       set_const(M_GS, "_ZN7Cudimot12GSbounds_maxE", bmax, nparams * sizeof(float)))
     return -1;
   CUfunction f;
-  if (get_fn(M_GS, "_ZN7Cudimot17gridSearch_kernelIdLb0EEEviiiiiPT_S2_S2_S2_S2_i", &f)) return -1;
-  const size_t smem = 2 * 8 * sizeof(double) + (size_t)nmeas * cfp_size * sizeof(double) +
-                      2 * (size_t)nparams * 8 * sizeof(double) + 8 * sizeof(int);  // :298-303
+  if (get_fn(M_GS, std::string("_ZN7Cudimot17gridSearch_kernelI") + g_t + "Lb0EEEviiiiiPT_S2_S2_S2_S2_i", &f))
+    return -1;
+  const size_t smem = 2 * 8 * sizeof(double) + (size_t)nmeas * cfp_size * g_ts +
+                      2 * (size_t)nparams * 8 * g_ts + 8 * sizeof(int);  // :298-303
   int dbg = -1;
   void* args[] = {&ngp, &combs, &nmeas, &cfp_size, &fixp_size, &meas, &grid, &params, &cfp, &fixp, &dbg};
   return launch(f, nvox / 8, 8 * 32, smem, args);
@@ -123,13 +139,13 @@ int ref_levmar(int nparams, int nvox, int nmeas, int cfp_size, int fixp_size, CU
       set_const(M_LM, "_ZN7Cudimot7LMfixedE", fixed, nparams * sizeof(int)))
     return -1;
   CUfunction f;
-  std::string name = std::string("_ZN7Cudimot16levenberg_kernelIdLb") + b(marquardt) +
+  std::string name = std::string("_ZN7Cudimot16levenberg_kernelI") + g_t + "Lb" + b(marquardt) +
                      "ELb0EEEviiiPT_S2_S2_S2_ii";
   if (get_fn(M_LM, name, &f)) return -1;
   const size_t np = nparams;
-  const size_t smem = 4 * 2 * sizeof(double) + (size_t)nmeas * cfp_size * sizeof(double) +
-                      3 * np * 2 * sizeof(double) + np * np * 2 * sizeof(double) +
-                      2 * 2 * sizeof(int) + np * 2 * sizeof(double);  // :674-682
+  const size_t smem = 4 * 2 * sizeof(double) + (size_t)nmeas * cfp_size * g_ts +
+                      3 * np * 2 * g_ts + np * np * 2 * g_ts + 2 * 2 * sizeof(int) +
+                      np * 2 * g_ts;  // :674-682
   int dbg = -1;
   void* args[] = {&nmeas, &cfp_size, &fixp_size, &meas, &params, &cfp, &fixp, &max_iters, &dbg};
   return launch(f, nvox / 2, 2 * 32, smem, args);
@@ -163,8 +179,8 @@ int ref_mcmc(int nparams, int nvox, int nmeas, int cfp_size, int fixp_size, CUde
   const int blocks_rand = (nvox + 255) / 256;
   CUdeviceptr states, propsd, taupsd;
   DRV(cuMemAlloc(&states, (size_t)blocks_rand * 256 * state_bytes));
-  DRV(cuMemAlloc(&propsd, (size_t)nvox * nparams * sizeof(double)));
-  DRV(cuMemAlloc(&taupsd, (size_t)nvox * sizeof(double)));
+  DRV(cuMemAlloc(&propsd, (size_t)nvox * nparams * g_ts));
+  DRV(cuMemAlloc(&taupsd, (size_t)nvox * g_ts));
   CUfunction fs;
   int rc = get_fn(M_MCMC, "_ZN7Cudimot20setup_randoms_kernelEP17curandStateXORWOWd", &fs);
   if (!rc) {
@@ -174,16 +190,15 @@ int ref_mcmc(int nparams, int nvox, int nmeas, int cfp_size, int fixp_size, CUde
     rc = launch(fs, blocks_rand, 256, 0, a0);
   }
   const size_t np = nparams;
-  const size_t smem = 8 * state_bytes + (size_t)nmeas * cfp_size * sizeof(double) +
-                      3 * np * 8 * sizeof(double) + 2 * 8 * sizeof(double) +
-                      3 * 8 * sizeof(double) + 3 * 8 * sizeof(double) + 2 * np * 8 * sizeof(int) +
+  const size_t smem = 8 * state_bytes + (size_t)nmeas * cfp_size * g_ts + 3 * np * 8 * g_ts +
+                      2 * 8 * g_ts + 3 * 8 * g_ts + 3 * 8 * g_ts + 2 * np * 8 * sizeof(int) +
                       2 * 8 * sizeof(int);  // :780-791
   int dbg = -1;
   for (int phase = 0; phase < 2 && !rc; phase++) {
     const int rec = phase;
     const int upd = rec ? update_proposal : 1;
     int niters = rec ? njumps : nburn;
-    std::string name = std::string("_ZN7Cudimot11mcmc_kernelIdLb") + b(rec) + "ELb" + b(upd) +
+    std::string name = std::string("_ZN7Cudimot11mcmc_kernelI") + g_t + "Lb" + b(rec) + "ELb" + b(upd) +
                        "ELb" + b(rician) + "ELb0EEEvP17curandStateXORWOWiiiiiiiPT_S4_S4_S4_S4_S4_S4_S4_i";
     CUfunction f;
     rc = get_fn(M_MCMC, name, &f);
@@ -205,10 +220,11 @@ int ref_bic_aic(int nparams, int nvox, int nmeas, int nsamples, int cfp_size, in
                 CUdeviceptr bic, CUdeviceptr aic, CUdeviceptr tau, int rician) {
   if (nvox % 8) return -1;
   CUfunction f;
-  std::string name = std::string("_ZN7Cudimot14bic_aic_kernelIdLb") + b(rician) + "EEEviiiiPT_S2_S2_S2_S2_S2_S2_";
+  std::string name = std::string("_ZN7Cudimot14bic_aic_kernelI") + g_t + "Lb" + b(rician) +
+                     "EEEviiiiPT_S2_S2_S2_S2_S2_S2_";
   if (get_fn(M_BIC, name, &f)) return -1;
-  const size_t smem = (size_t)nmeas * cfp_size * sizeof(double) + (size_t)nparams * 8 * sizeof(double) +
-                      3 * 8 * sizeof(double);  // :223-228
+  const size_t smem = (size_t)nmeas * cfp_size * g_ts + (size_t)nparams * 8 * g_ts +
+                      3 * 8 * g_ts;  // :223-228
   void* args[] = {&nmeas, &nsamples, &cfp_size, &fixp_size, &meas, &samples, &cfp, &fixp, &bic, &aic, &tau};
   return launch(f, nvox / 8, 8 * 32, smem, args);
 }
@@ -218,8 +234,9 @@ int ref_predicted(int nparams, int nvox, int nmeas, int nsamples, int cfp_size, 
                   CUdeviceptr samples, CUdeviceptr cfp, CUdeviceptr fixp, CUdeviceptr pred) {
   if (nvox % 8) return -1;
   CUfunction f;
-  if (get_fn(M_PRED, "_ZN7Cudimot25getPredictedSignal_kernelIdEEviiiiiPT_S2_S2_S2_", &f)) return -1;
-  const size_t smem = (size_t)nmeas * cfp_size * sizeof(double) + (size_t)nparams * 8 * sizeof(double);
+  if (get_fn(M_PRED, std::string("_ZN7Cudimot25getPredictedSignal_kernelI") + g_t + "EEviiiiiPT_S2_S2_S2_", &f))
+    return -1;
+  const size_t smem = (size_t)nmeas * cfp_size * g_ts + (size_t)nparams * 8 * g_ts;
   void* args[] = {&nvox, &nmeas, &nsamples, &cfp_size, &fixp_size, &samples, &cfp, &fixp, &pred};
   return launch(f, nvox / 8, 8 * 32, smem, args);
 }

@@ -1,5 +1,7 @@
 """ctypes wrapper of refharness.cpp: CUDIMOT's own kernels on torch CUDA
-tensors (test infrastructure; CUDIMOT's layouts, double precision)."""
+tensors (test infrastructure; CUDIMOT's layouts). T = double (the MyType the
+plugins ship with) by default; RefKernels(..., real=torch.float32) runs
+CUDIMOT's float instantiations, and every array passed is then float32."""
 import ctypes as C
 import os
 
@@ -37,15 +39,26 @@ def _arr(v, ct):
 
 
 class RefKernels:
-    def __init__(self, model, nparams):
+    def __init__(self, model, nparams, real=None):
         global _LOADED
+        import torch
         self.lib = _lib()
         self.np = nparams
+        self.real = torch.float64 if real is None else real
+        if self.real not in (torch.float64, torch.float32):
+            raise ValueError("real must be torch.float64 or torch.float32")
         if _LOADED != model:
             rc = self.lib.ref_load(os.path.join(REF, model).encode())
             if rc:
                 raise RuntimeError(self.lib.ref_last_error().decode())
             _LOADED = model
+
+    def _use(self, *arrays):
+        """Select T in the harness and check that every array is a T array."""
+        for a in arrays:
+            if a is not None and a.dtype != self.real:
+                raise TypeError(f"expected {self.real} arrays, got {a.dtype}")
+        self.lib.ref_set_real(8 if self.real.itemsize == 8 else 4)
 
     def _check(self, rc, what):
         if rc:
@@ -58,6 +71,7 @@ class RefKernels:
                 _arr(list(s.bounds_max)[:n], C.c_float))
 
     def gridsearch(self, cfg, meas, params, cfp, fixp, grid):
+        self._use(meas, params, cfp, fixp, grid)
         bt, bmin, bmax = self._lim(cfg)
         s = cfg.struct
         nv, nm = meas.shape
@@ -68,6 +82,7 @@ class RefKernels:
         self._check(rc, "ref_gridsearch")
 
     def levmar(self, cfg, meas, params, cfp, fixp):
+        self._use(meas, params, cfp, fixp)
         bt, bmin, bmax = self._lim(cfg)
         s = cfg.struct
         nv, nm = meas.shape
@@ -77,6 +92,7 @@ class RefKernels:
         self._check(rc, "ref_levmar")
 
     def mcmc(self, cfg, meas, params, cfp, fixp, samples, tau=None):
+        self._use(meas, params, cfp, fixp, samples, tau)
         bt, bmin, bmax = self._lim(cfg)
         s = cfg.struct
         n = self.np
@@ -90,6 +106,7 @@ class RefKernels:
         self._check(rc, "ref_mcmc")
 
     def bic_aic(self, meas, samples, cfp, fixp, bic, aic, tau=None, rician=False):
+        self._use(meas, samples, cfp, fixp, bic, aic, tau)
         nv, nm = meas.shape
         ns = samples.shape[-1] if samples.dim() == 3 else 1
         rc = self.lib.ref_bic_aic(self.np, nv, nm, ns, cfp.shape[1], fixp.shape[1] if fixp is not None else 0,
@@ -98,6 +115,7 @@ class RefKernels:
         self._check(rc, "ref_bic_aic")
 
     def predicted(self, samples, cfp, fixp, pred):
+        self._use(samples, cfp, fixp, pred)
         nv, nm = pred.shape
         ns = samples.shape[-1] if samples.dim() == 3 else 1
         rc = self.lib.ref_predicted(self.np, nv, nm, ns, cfp.shape[1], fixp.shape[1] if fixp is not None else 0,

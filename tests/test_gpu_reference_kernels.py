@@ -71,6 +71,28 @@ def test_b1s_levmar_vs_reference_kernels(built, cuda):
     assert np.mean(ang <= 0.5) >= 0.995
 
 
+def test_b1s_levmar_vs_reference_float_kernels(built, cuda):
+    """CUDIMOT's float instantiation (MyType = float) of the LM kernel: our
+    FP32 fit ends no worse than it (costs by the FP64 oracle)."""
+    need("Ball_1_Stick")
+    wl = b1s(4000, seed=5)
+    cfg = capi.model_cfg("Ball_1_Stick")
+    ref = rk.RefKernels("Ball_1_Stick", 5, real=torch.float32)
+    ours = capi.Cudimot("Ball_1_Stick", cfg)
+    F = lambda x: torch.as_tensor(np.ascontiguousarray(x, dtype=np.float32), device=cuda)  # noqa
+    pr, po = F(wl.init), T(wl.init, cuda)
+    ref.levmar(cfg, F(wl.meas), pr, F(wl.cfp), None)
+    ours.levmar(T(wl.meas, cuda), po, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    torch.cuda.synchronize()
+    r, g = pr.cpu().numpy().astype(np.float64), po.cpu().numpy()
+    assert np.all(np.isfinite(r))
+    o = oracle("Ball_1_Stick")
+    cr, cg = o.cost(wl.meas, r, wl.cfp), o.cost(wl.meas, g, wl.cfp)
+    rel = (cg - cr) / cr
+    assert np.mean(rel <= 1e-4) >= 0.99, np.quantile(rel, [0.5, 0.99, 1])
+    assert np.median(np.abs(rel)) < 1e-4, np.median(np.abs(rel))
+
+
 def test_b1s_mcmc_vs_reference_kernels(built, cuda):
     need("Ball_1_Stick")
     wl = b1s(512, seed=9)
