@@ -183,17 +183,32 @@ def build_mlp(force=False):
     return out, None
 
 
+def zlib_flags():
+    """-DCDM_HAVE_ZLIB -lz when zlib's header and library are present (gzip
+    NIfTI support in libcdm_utils), else nothing."""
+    probe = "#include <zlib.h>\nint main() { return zlibVersion() == 0; }\n"
+    try:
+        r = subprocess.run(["g++", "-x", "c++", "-", "-lz", "-o", os.devnull], input=probe,
+                           capture_output=True, text=True, timeout=60)
+    except (OSError, subprocess.SubprocessError):
+        return []
+    return ["-DCDM_HAVE_ZLIB", "-lz"] if r.returncode == 0 else []
+
+
 def build_utils(force=False):
-    """DTI initialiser, post-processing and part files (include/cdm_utils.h)."""
-    src = os.path.join(CSRC, "utils", "cdm_utils.cu")
-    hdr = os.path.join(ROOT, "include", "cdm_utils.h")
+    """DTI initialiser, post-processing, part files and NIfTI volumes
+    (include/cdm_utils.h, include/cdm_volumes.h)."""
+    srcs = [os.path.join(CSRC, "utils", "cdm_utils.cu"), os.path.join(CSRC, "utils", "cdm_volumes.cpp")]
+    hdrs = [os.path.join(ROOT, "include", "cdm_utils.h"), os.path.join(ROOT, "include", "cdm_volumes.h")]
     out = os.path.join(LIBDIR, "libcdm_utils.so")
-    if not force and os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(src),
-                                                                          os.path.getmtime(hdr)):
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= max(
+            os.path.getmtime(f) for f in srcs + hdrs):
         return out, None
     os.makedirs(LIBDIR, exist_ok=True)
+    zl = zlib_flags()
     cmd = [nvcc_path(), "-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-shared",
-           "-I", os.path.join(ROOT, "include"), src, "-o", out + ".tmp"]
+           "-I", os.path.join(ROOT, "include")] + [f for f in zl if f.startswith("-D")] + srcs + \
+        ["-o", out + ".tmp"] + [f for f in zl if f.startswith("-l")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         return out, (r.stdout + r.stderr)[-4000:]

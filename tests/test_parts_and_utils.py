@@ -13,12 +13,14 @@ import pytest
 
 from cudimot_gb300 import capi, utils
 
-HEADER = os.path.join(os.path.dirname(os.path.dirname(__file__)), "include", "cdm_utils.h")
+INCLUDE = os.path.join(os.path.dirname(os.path.dirname(__file__)), "include")
 
 
-def test_exports(built):
-    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+@pytest.mark.parametrize("header", ["cdm_utils.h", "cdm_volumes.h"])
+def test_exports(built, header):
+    text = re.sub(r"/\*.*?\*/", "", open(os.path.join(INCLUDE, header)).read(), flags=re.S)
     names = set(re.findall(r"\b(cdm_[a-z_0-9]+)\s*\(", text))
+    assert len(names) >= 8
     lib = C.CDLL(os.path.join(capi.LIBDIR, "libcdm_utils.so"))
     for n in names:
         assert hasattr(lib, n), n
