@@ -151,6 +151,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
   cdm_load_cfp(sproto, a.nmeas_pad, 0, cf0);
 
   double energy = 0.0;
+  bool stale = false;  // derived values of P out of date (after a rejection)
   for (int phase = 0; phase < 2; phase++) {
     const bool recording = phase == 1;
     const int niters = recording ? a.njumps : nburn;
@@ -170,6 +171,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
       P[p] = fp32(x);
     }
     cdm_update_derived(P, FixP);
+    stale = false;
     float total_prior = 0.0f;
 #pragma unroll
     for (int p = 0; p < kNP; p++) {
@@ -208,6 +210,8 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
         const float old = tau;
         tau = tau + d.normal * tauSD;
         if (tau > 0.0f) {
+          if (stale) cdm_update_derived(P, FixP);
+          stale = false;
           float tp = 0.0f;
 #pragma unroll
           for (int p = 0; p < kNP; p++) tp += prior[p];
@@ -238,6 +242,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
         if (cdm_in_bounds(L, p, P)) {
           cdm_update_derived(P, FixP);
           derived = true;
+          stale = false;
           const float np_ = cdm_prior(L, p, P, a.nmeas, cf0, FixP);
           float tp = 0.0f;
 #pragma unroll
@@ -253,10 +258,12 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
           cdm_set(acc, p, cdm_get(acc, p) + 1);
         } else {
           cdm_set(rej, p, cdm_get(rej, p) + 1);
-          // Derived_P is a function of P: restoring the parameter and
-          // deriving again restores the derived values exactly.
           cdm_set(P, p, old);
-          if (derived) cdm_update_derived(P, FixP);
+          // The derived values now belong to the rejected point. Derived_P
+          // is a function of P, and the next likelihood (the next proposal,
+          // or the tau proposal) derives first, so they are not recomputed
+          // here (3 % of the MCMC time on NODDI-Watson).
+          stale = stale || derived;  // out of bounds: P and its derived values unchanged
         }
       }
       if (recording && (it % a.sampleevery) == 0) {
