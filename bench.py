@@ -168,16 +168,17 @@ def measured_peaks():
         return {}
 
 
-def cpu_baseline(cfp, meas, fixp, init, n, cfg):
-    """CPU oracle on n voxels: grid search -> LM -> MCMC, all host threads."""
+def cpu_baseline(cfp, meas, fixp, init, n, cfg, prec=0):
+    """CPU oracle on n voxels: grid search -> LM -> MCMC, all host threads;
+    prec 0 = T double (as the plugins ship), 1 = T float."""
     from oracle.oracle import Oracle
     o = Oracle(MODEL)
     threads = o.max_threads()
     sl = slice(0, n)
     t0 = time.perf_counter()
-    p, _, _ = o.gridsearch(cfg, meas[sl], init[sl], cfp, fixp[sl], threads=threads)
-    p, _, _, _ = o.levmar(cfg, meas[sl], p, cfp, fixp[sl], threads=threads)
-    p, s, _ = o.mcmc(cfg, meas[sl], p, cfp, fixp[sl], threads=threads)
+    p, _, _ = o.gridsearch(cfg, meas[sl], init[sl], cfp, fixp[sl], prec=prec, threads=threads)
+    p, _, _, _ = o.levmar(cfg, meas[sl], p, cfp, fixp[sl], prec=prec, threads=threads)
+    p, s, _ = o.mcmc(cfg, meas[sl], p, cfp, fixp[sl], prec=prec, threads=threads)
     dt = time.perf_counter() - t0
     return n / dt, threads, dt
 
@@ -770,6 +771,11 @@ def main():
         line["cpu_baseline"] = {"value": v, "unit": "voxels/s", "cores": threads, "kind": "port",
                                 "sample": f"{n} voxels of this workload, grid search -> LM -> MCMC, "
                                           f"FP64 CPU oracle, {dt:.1f} s"}
+        nf = max(n // 2, 1)
+        vf, _, dtf = cpu_baseline(cfp, meas, fixp, init, nf, cfg, prec=1)
+        line["cpu_baseline"]["float"] = {
+            "value": vf, "unit": "voxels/s", "cores": threads,
+            "sample": f"{nf} voxels, the same CPU oracle with T = float, {dtf:.1f} s"}
     if os.environ.get("CDM_BENCH_REFK", "1") != "0":
         line["reference_kernels"] = reference_kernels_leg(cfp, meas, fixp, init, cfg, dev)
     print(json.dumps(line))

@@ -4,6 +4,8 @@
 // Include order is CUDIMOT's (GridSearch.cu:7-11): math prelude, the
 // plugin's modelparameters.h, macro_numerical.h, the plugin's
 // modelfunctions.h; then this library's plugin tail and kernels.
+#include <math_constants.h>
+
 #include "functions_gpu.h"
 #include "modelparameters.h"
 #include "macro_numerical.h"
@@ -454,6 +456,37 @@ cdm_status reserve_fit(cdm_ctx* c, int nvox, int nmeas) {
   return CDM_OK;
 }
 
+// dMRI_Data::remove_NonPositive_entries (dMRI_Data.cu:15-30), which CUDIMOT
+// applies to every voxel's signals when --rician is set (dMRI_Data.cu:133),
+// so that log(S) in the Rician likelihood stays finite. If the smallest
+// value is non-positive and the largest positive (both read as float, as
+// the reference's MinS/MaxS), every entry that is non-positive as a float
+// takes the smallest remaining value, min(smallest positive entry,
+// float(largest)), rounded to float. One warp per voxel.
+__global__ void cdm_clean_signals_kernel(int nvox, int nmeas, double* __restrict__ meas) {
+  const int v = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = (int)(threadIdx.x & 31);
+  if (v >= nvox) return;
+  double* row = meas + (size_t)v * nmeas;
+  double mn = CUDART_INF, mx = -CUDART_INF, mpos = CUDART_INF;
+  for (int m = lane; m < nmeas; m += 32) {
+    const double x = row[m];
+    mn = fmin(mn, x);
+    mx = fmax(mx, x);
+    if ((float)x > 0.0f) mpos = fmin(mpos, x);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fmin(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
+    mx = fmax(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+    mpos = fmin(mpos, __shfl_xor_sync(0xFFFFFFFFu, mpos, o));
+  }
+  if (!((float)mn <= 0.0f && (float)mx > 0.0f)) return;
+  const double rep = (double)(float)fmin(mpos, (double)(float)mx);
+  for (int m = lane; m < nmeas; m += 32)
+    if ((float)row[m] <= 0.0f) row[m] = rep;
+}
+
 }  // namespace
 
 // =================================================================== C ABI
@@ -871,13 +904,23 @@ cdm_status cdm_get_stats(cdm_ctx* c, cdm_stats* s) {
   return CDM_OK;
 }
 
+cdm_status cdm_clean_signals(int nvox, int nmeas, double* meas, void* stream) {
+  if (nvox < 0 || nmeas <= 0 || (nvox > 0 && !meas)) return cdm_fail(CDM_BAD_ARG, "bad argument");
+  if (nvox == 0) return CDM_OK;
+  const size_t threads = (size_t)nvox * 32;
+  cdm_clean_signals_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      nvox, nmeas, meas);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
 cdm_status cdm_fit_host(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
                         const double* CFP, const double* FixP, double* samples, double* tau,
                         double* pred, double* BIC, double* AIC, int part_size, int64_t timeout_ms) {
   CDM_TRY(check_common(c, nvox, nmeas, CDM_CFP_TSIZE, CDM_FIXP_TSIZE));
   if (!meas || !params || !CFP || !samples || (CDM_FIXP_TSIZE > 0 && !FixP))
     return cdm_fail(CDM_BAD_ARG, "null array");
-  (void)part_size;
+  (void)part_size;  // CUDIMOT's SIZE_PART parts (dMRI_Data.cu:66-79): one part here
   const cdm_model_cfg& o = c->cfg;
   const int ns = o.run_mcmc ? o.njumps / std::max(o.sampleevery, 1) : 1;
   const size_t V = (size_t)nvox;
@@ -904,6 +947,7 @@ cdm_status cdm_fit_host(cdm_ctx* c, int nvox, int nmeas, const double* meas, dou
   if (CDM_FIXP_TSIZE > 0)
     CDM_CUDA(cudaMemcpyAsync(c->h_fixp, FixP, V * CDM_FIXP_TSIZE * sizeof(double),
                              cudaMemcpyHostToDevice, st));
+  if (o.rician) CDM_TRY(cdm_clean_signals(nvox, nmeas, c->h_meas, st));  // dMRI_Data.cu:133
   CDM_TRY(cdm_fit(c, nvox, nmeas, c->h_meas, c->h_params, c->h_cfp, c->h_fixp, c->h_samples,
                   want_tau ? c->h_tau : nullptr, want_pred ? c->h_pred : nullptr,
                   want_bic ? c->h_bic : nullptr, want_bic ? c->h_aic : nullptr, st));

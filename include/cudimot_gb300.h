@@ -187,13 +187,22 @@ cdm_status cdm_fit(cdm_ctx* ctx, int nvox, int nmeas, const double* meas, double
                    double* pred, double* BIC, double* AIC, void* stream);
 
 /* As cdm_fit, with HOST arrays: copies in, fits, copies out, and waits for
- * completion (at most timeout_ms, < 0 = no limit). Voxels are processed in
- * parts of part_size (<= 0: all at once) with copies of one part overlapped
- * with the fit of the previous one. */
+ * completion (at most timeout_ms, < 0 = no limit). The signals go through
+ * cdm_clean_signals first when the cfg has rician, as CUDIMOT's data loader
+ * does. part_size stands for CUDIMOT's SIZE_PART and is ignored: all voxels
+ * are fitted as one part (they fit in HBM). */
 cdm_status cdm_fit_host(cdm_ctx* ctx, int nvox, int nmeas, const double* meas,
                         double* params, const double* CFP, const double* FixP,
                         double* samples, double* tau, double* pred, double* BIC, double* AIC,
                         int part_size, int64_t timeout_ms);
+
+/* dMRI_Data::remove_NonPositive_entries (dMRI_Data.cu:15-30), applied by
+ * CUDIMOT to every voxel when --rician is set (dMRI_Data.cu:133): in each
+ * voxel of meas [nvox][nmeas] (device, in place) whose smallest value is
+ * non-positive and largest positive, the non-positive entries take the
+ * smallest positive value. The stage entry points and cdm_fit use meas as
+ * given, like the reference's method classes. */
+cdm_status cdm_clean_signals(int nvox, int nmeas, double* meas, void* stream);
 
 /* The stage sequence of cdm_fit recorded as plain launches on `stream`
  * (no graph of its own), so that a caller can capture several contexts -
