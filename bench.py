@@ -749,7 +749,7 @@ def main():
         roofline = {"bound": "fp32", "kernel": "cdm_mcmc_kernel", "achieved": achieved,
                     "peak": fp32_peak["tflops"], "unit": "TFLOP/s", "frac": achieved / fp32_peak["tflops"],
                     "peak_source": fp32_peak["source"], "traffic": profiled_traffic(),
-                    "traffic_source": "profiles/mcmc_kernel_noddi_watson.md (full-length 100k-voxel ncu capture scaled by voxels)",
+                    "traffic_source": "profiles/mcmc_kernel_noddi_watson.md (ncu capture of the full 200k-voxel, 1250+1250-jump launch)",
                     "flop_per_voxel": per_voxel_mcmc, "launch_ms": mcmc_ms}
     line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -781,7 +781,7 @@ def main():
     print(json.dumps(line))
 
 
-def reference_kernels_leg(cfp, meas, fixp, init, cfg, dev, n=2048, n_float=8192):
+def reference_kernels_leg(cfp, meas, fixp, init, cfg, dev, n=2048, n_float=2048):
     """CUDIMOT's own GridSearch/LM/MCMC kernels (unmodified sources compiled
     for sm_103a) on the first voxels of this workload, same GPU; wall time of
     the three stages. T = double as the plugins ship (n voxels), and CUDIMOT's

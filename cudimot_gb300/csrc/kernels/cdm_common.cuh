@@ -16,6 +16,11 @@
 //                                        rows padded to NCOLS4 (16 bytes)
 //   signals   float [nchunk][nvox][G]    chunk c holds measurements cG..cG+G-1
 // so a warp's signal load is one contiguous 128-byte line.
+// With the paired signal hook (Predicted_Signal_Pair) the kernels that take
+// the paired cost loop also keep, after the staged protocol in shared
+// memory, a pair table float2 [nchunk/2][G][NCOLS]: entry (j, l, k) holds
+// column k of measurements 2jG+l and (2j+1)G+l, the two a lane evaluates
+// together, so a 16-byte load gives two columns already paired.
 #pragma once
 
 #include <stdint.h>
@@ -38,6 +43,11 @@ constexpr int kNPS = CDM_PSTORE;
 constexpr int kNCOLS = CDM_CFP_TSIZE + CDM_NDCFP;
 constexpr int kNCOLS4 = (kNCOLS + 3) / 4 * 4;  // protocol row stride (floats)
 constexpr int kNFIX = CDM_FIXP_TSIZE > 0 ? CDM_FIXP_TSIZE : 1;
+#ifdef CDM_SIGNAL_PAIR
+constexpr int kPairTables = 1;  // shared-memory protocol copies of the paired-loop kernels
+#else
+constexpr int kPairTables = 0;
+#endif
 
 // Error codes written to the device error word.
 #define CDM_DEVERR_STAGE_TIMEOUT 1
@@ -140,7 +150,44 @@ struct cdm_voxel_io {
   int nmeas;
   int nmeas_pad;
   int lane;
+  const float* pairs;  // this lane's first pair-table entry (paired hook only)
 };
+
+// Build the pair table (see the layout notes above) after the staged
+// protocol, with every thread of the CTA; returns its start. Call before
+// any thread leaves the kernel.
+template <int G>
+__device__ __forceinline__ const float* cdm_build_pair_table(float* sproto, int nmeas_pad,
+                                                             int nchunk) {
+  float2* ptab = reinterpret_cast<float2*>(sproto + (size_t)nmeas_pad * kNCOLS4);
+#ifdef CDM_SIGNAL_PAIR
+  const int total = (nchunk / 2) * G * kNCOLS;
+  for (int i = (int)threadIdx.x; i < total; i += (int)blockDim.x) {
+    const int k = i % kNCOLS, l = (i / kNCOLS) % G, j = i / (kNCOLS * G);
+    ptab[i] = make_float2(sproto[(size_t)(2 * j * G + l) * kNCOLS4 + k],
+                          sproto[(size_t)((2 * j + 1) * G + l) * kNCOLS4 + k]);
+  }
+  __syncthreads();
+#endif
+  return reinterpret_cast<const float*>(ptab);
+}
+
+// One pair-table entry: the NCOLS column pairs of a lane's two measurements.
+__device__ __forceinline__ void cdm_load_pairs(const float* q, float2* ab) {
+  if constexpr (kNCOLS % 2 == 0) {
+    const float4* q4 = reinterpret_cast<const float4*>(q);
+#pragma unroll
+    for (int k = 0; k < kNCOLS / 2; k++) {
+      const float4 v = q4[k];
+      ab[2 * k] = make_float2(v.x, v.y);
+      ab[2 * k + 1] = make_float2(v.z, v.w);
+    }
+  } else {
+    const float2* q2 = reinterpret_cast<const float2*>(q);
+#pragma unroll
+    for (int k = 0; k < kNCOLS; k++) ab[k] = q2[k];
+  }
+}
 
 // Sum of squared residuals over the voxel's measurements: each lane sums its
 // own measurements in FP32, the group total is formed in FP64. The loop walks
@@ -155,17 +202,19 @@ __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const fl
   const float* sig = io.sig;
 #ifdef CDM_SIGNAL_PAIR
   // two chunks per step on the paired FP32 instructions (plugin hook
-  // Predicted_Signal_Pair); two interleaved partial sums
+  // Predicted_Signal_Pair) with the protocol from the pair table; two
+  // interleaved partial sums
   float2 acc2 = make_float2(0.0f, 0.0f);
   int c = 0;
+  const float* q = io.pairs;
 #pragma unroll kPairUnroll
   for (; c + 1 < full; c += 2) {
-    fp32 ca[kNCOLS], cb[kNCOLS];
-    cdm_load_cfp(row, 0, 0, ca);
-    cdm_load_cfp(row + G * kNCOLS4, 0, 0, cb);
-    const float2 s2 = Predicted_Signal_Pair(P, ca, cb, FixP);
+    float2 ab[kNCOLS];
+    cdm_load_pairs(q, ab);
+    const float2 s2 = Predicted_Signal_Pair(P, ab, FixP);
     const float2 r = __fadd2_rn(s2, make_float2(-sig[0], -sig[io.chunk_stride]));
     acc2 = __ffma2_rn(r, r, acc2);
+    q += 2 * G * kNCOLS;
     row += 2 * G * kNCOLS4;
     sig += 2 * io.chunk_stride;
   }

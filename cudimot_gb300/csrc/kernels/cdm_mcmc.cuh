@@ -116,6 +116,7 @@ template <int G, bool RICIAN>
 __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(const __grid_constant__ cdm_mcmc_args a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
+  const float* ptab = cdm_build_pair_table<G>(sproto, a.nmeas_pad, a.nchunk);
   const int v = blockIdx.x * (CDM_NT / G) + (int)threadIdx.x / G;
   if (v >= a.nvox) return;
   const unsigned gm = cdm_group_mask<G>();
@@ -129,6 +130,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
   io.nmeas = a.nmeas;
   io.nmeas_pad = a.nmeas_pad;
   io.lane = lane;
+  io.pairs = ptab + (size_t)lane * kNCOLS * 2;
 
   fp32 P[kNPS], FixP[kNFIX];
   cdm_load_params(a.params + (size_t)v * kNP, P);

@@ -44,7 +44,23 @@ __global__ void __launch_bounds__(CDM_NT) cdm_predicted_kernel(const __grid_cons
   cdm_sample_mean(a.samples + (size_t)v * kNP * a.nsamples, a.nsamples, P);
   cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
   cdm_update_derived(P, FixP);
-  for (int m = lane; m < a.nmeas; m += 32) {
+  int m = lane;
+#ifdef CDM_SIGNAL_PAIR
+  // measurements m and m + 32 through the paired hook, the function the
+  // fitting kernels' cost loops evaluate
+  for (; m + 32 < a.nmeas; m += 64) {
+    fp32 ca[kNCOLS], cb[kNCOLS];
+    cdm_load_cfp(sproto, a.nmeas_pad, m, ca);
+    cdm_load_cfp(sproto, a.nmeas_pad, m + 32, cb);
+    float2 ab[kNCOLS];
+#pragma unroll
+    for (int k = 0; k < kNCOLS; k++) ab[k] = make_float2(ca[k].v, cb[k].v);
+    const float2 s = Predicted_Signal_Pair(P, ab, FixP);
+    a.pred[(size_t)v * a.nmeas + m] = (double)s.x;
+    a.pred[(size_t)v * a.nmeas + m + 32] = (double)s.y;
+  }
+#endif
+  for (; m < a.nmeas; m += 32) {
     fp32 cf[kNCOLS];
     cdm_load_cfp(sproto, a.nmeas_pad, m, cf);
     a.pred[(size_t)v * a.nmeas + m] = (double)(float)Predicted_Signal(NPARAMS, P, cf, FixP);

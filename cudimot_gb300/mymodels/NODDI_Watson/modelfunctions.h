@@ -32,7 +32,9 @@
 // ---------------------------------------------------------------------------
 // Protocol-derived values (double, once per protocol).
 //   d[0]   = exp(-b Diso)
-//   d[1+l] = 0.5 sqrt((4l+1)/(4 pi)) * LGI_l(b Dpar),  l = 0..6,
+//   d[1+l] = 0.5 sqrt((4l+1)/(4 pi)) * LGI_l(b Dpar),  l = 1..6,
+//   d[1]   = 0.5 sqrt(1/(4 pi)) * LGI_0(b Dpar) * c_0 (c_0 = 2 sqrt(pi), the
+//            l = 0 SH coefficient, which does not depend on kappa)
 // with LGI_l(x) = int_{-1}^{1} P_2l(t) exp(-x t^2) dt.
 #define CDM_DERIVED_CFP 8
 
@@ -79,6 +81,7 @@ __host__ __device__ inline void Derived_CFP(const T* cfp, T* d) {
   double L[7];
   watson_lgi(b * WATSON_DPAR, L);
   for (int l = 0; l < 7; l++) d[1 + l] = (T)(0.14104739588693907 * sqrt(4.0 * l + 1.0) * L[l]);
+  d[1] = (T)(0.14104739588693907 * 3.5449077018110318 * L[0]);
 }
 
 // ---------------------------------------------------------------------------
@@ -87,10 +90,12 @@ __host__ __device__ inline void Derived_CFP(const T* cfp, T* d) {
 //   P[5..7]   orientation vector (sin th cos ph, sin th sin ph, cos th)
 //   P[8]      perpendicular equivalent diffusivity dPerp_eq
 //   P[9]      dPar_eq - dPerp_eq
-//   P[10..15] SH coefficients c_1..c_6 of the Watson density (c_0 = 2 sqrt pi)
+//   P[10..15] SH coefficients c_1..c_6 of the Watson density times h_1..h_6
+//             (c_0 = 2 sqrt pi; h_l: scale of the rescaled Legendre
+//             recurrence below)
 //   P[16..18] cos th cos ph, cos th sin ph, sin th (orientation derivatives)
 //   P[19]     d<P_2>/dkappa
-//   P[20..25] dc_1/dkappa .. dc_6/dkappa
+//   P[20..25] h_1 dc_1/dkappa .. h_6 dc_6/dkappa
 //   P[26]     <P_2>
 //   P[27..29] kappa, th, ph the cached blocks were computed for
 //   P[30]     1 once the caches hold values (callers zero the derived slots)
@@ -255,6 +260,48 @@ MACRO void watson_kappa_terms(T k, T* c, T& p2, T* dc, T& dp2) {
   dc[6] = (T)6.0 * c6k * k5;
 }
 
+// Even Legendre polynomials by the recurrence in y = x^2 obtained from two
+// uses of t P_n = ((n+1) P_{n+1} + n P_{n-1})/(2n+1):
+//   P_{n+2} = (a_n y - b_n) P_n - g_n P_{n-2},  n = 0, 2, ..., 10,
+// a_n = 1/alpha, b_n = beta/alpha, g_n = gamma/alpha with
+// alpha = (n+1)(n+2)/((2n+1)(2n+3)),
+// beta = (n+1)^2/((2n+1)(2n+3)) + n^2/((2n+1)(2n-1)),
+// gamma = n(n-1)/((2n+1)(2n-1)).
+__host__ __device__ constexpr double watson_leg_a(int l) {
+  return l == 0 ? 1.5 : l == 1 ? 2.9166666666666665 : l == 2 ? 3.2999999999999998
+       : l == 3 ? 3.4821428571428572 : l == 4 ? 3.588888888888889 : 3.6590909090909087;
+}
+__host__ __device__ constexpr double watson_leg_b(int l) {
+  return l == 0 ? 0.5 : l == 1 ? 1.5277777777777775 : l == 2 ? 1.6714285714285715
+       : l == 3 ? 1.7516233766233769 : l == 4 ? 1.8007407407407408 : 1.8337320574162681;
+}
+__host__ __device__ constexpr double watson_leg_g(int l) {
+  return l == 0 ? 0.0 : l == 1 ? 0.3888888888888889 : l == 2 ? 0.62857142857142856
+       : l == 3 ? 0.73051948051948057 : l == 4 ? 0.78814814814814815 : 0.82535885167464107;
+}
+
+// The recurrence rescaled so that its last term has no coefficient (one
+// multiply fewer per degree): with q_l = P_2l / h_l, h_0 = h_1 = 1 and
+// h_(l+1) = g_l h_(l-1),
+//   q_1 = a_0 y - b_0,  q_(l+1) = (qa_l y - qb_l) q_l - q_(l-1)  (l >= 1),
+//   qa_l = a_l h_l / h_(l+1),  qb_l = b_l h_l / h_(l+1),
+// and the factors h_l are carried by the cached coefficients P[10..15] and
+// P[20..25]. The derivative follows as dq_(l+1) = 2 qa_l x q_l +
+// (qa_l y - qb_l) dq_l - dq_(l-1).
+// h_l, qa_l and qb_l evaluated (literals, so that they fold into immediates):
+__host__ __device__ constexpr double watson_h(int l) {
+  return l <= 1 ? 1.0 : l == 2 ? 0.3888888888888889 : l == 3 ? 0.6285714285714286
+       : l == 4 ? 0.2840909090909091 : l == 5 ? 0.4954074074074074 : 0.23447694649847758;
+}
+__host__ __device__ constexpr double watson_qa(int l) {
+  return l == 0 ? 1.5 : l == 1 ? 7.499999999999999 : l == 2 ? 2.0416666666666665
+       : l == 3 ? 7.704489795918367 : l == 4 ? 2.058044938016529 : 7.730997728395061;
+}
+__host__ __device__ constexpr double watson_qb(int l) {
+  return l == 0 ? 0.5 : l == 1 ? 3.9285714285714275 : l == 2 ? 1.0340909090909092
+       : l == 3 ? 3.8755918367346944 : l == 4 ? 1.0326330741626795 : 3.874344399355878;
+}
+
 MACRO void Derived_P(T* P, T* FixP) {
   const bool valid = P[30] != (T)0.0;
   if (!valid || P[2] != P[27]) {
@@ -263,8 +310,8 @@ MACRO void Derived_P(T* P, T* FixP) {
     watson_kappa_terms(P[2], c, p2, dc, dp2);
 #pragma unroll
     for (int l = 1; l <= 6; l++) {
-      P[9 + l] = c[l];
-      P[19 + l] = dc[l];
+      P[9 + l] = c[l] * (T)watson_h(l);
+      P[19 + l] = dc[l] * (T)watson_h(l);
     }
     P[19] = dp2;
     P[26] = p2;
@@ -289,41 +336,20 @@ MACRO void Derived_P(T* P, T* FixP) {
   P[30] = (T)1.0;
 }
 
-// Even Legendre polynomials by the recurrence in y = x^2 obtained from two
-// uses of t P_n = ((n+1) P_{n+1} + n P_{n-1})/(2n+1):
-//   P_{n+2} = (a_n y - b_n) P_n - g_n P_{n-2},  n = 0, 2, ..., 10,
-// a_n = 1/alpha, b_n = beta/alpha, g_n = gamma/alpha with
-// alpha = (n+1)(n+2)/((2n+1)(2n+3)),
-// beta = (n+1)^2/((2n+1)(2n+3)) + n^2/((2n+1)(2n-1)),
-// gamma = n(n-1)/((2n+1)(2n-1)).
-__host__ __device__ constexpr double watson_leg_a(int l) {
-  return l == 0 ? 1.5 : l == 1 ? 2.9166666666666665 : l == 2 ? 3.2999999999999998
-       : l == 3 ? 3.4821428571428572 : l == 4 ? 3.588888888888889 : 3.6590909090909087;
-}
-__host__ __device__ constexpr double watson_leg_b(int l) {
-  return l == 0 ? 0.5 : l == 1 ? 1.5277777777777775 : l == 2 ? 1.6714285714285715
-       : l == 3 ? 1.7516233766233769 : l == 4 ? 1.8007407407407408 : 1.8337320574162681;
-}
-__host__ __device__ constexpr double watson_leg_g(int l) {
-  return l == 0 ? 0.0 : l == 1 ? 0.3888888888888889 : l == 2 ? 0.62857142857142856
-       : l == 3 ? 0.73051948051948057 : l == 4 ? 0.78814814814814815 : 0.82535885167464107;
-}
-
 // ---------------------------------------------------------------------------
 MACRO T Predicted_Signal(int npar, T* P, T* CFP, T* FixP) {
   const T xv = CFP[0] * P[5] + CFP[1] * P[6] + CFP[2] * P[7];
   const T extra = exp_gpu(-CFP[3] * (P[9] * xv * xv + P[8]));
   // Dispersed-stick SH sum over P_0..P_12 at the clamped cosine.
-  const T x = min_gpu(max_gpu(xv, (T)-1.0), (T)1.0);
-  const T y = x * x;
-  T pm = (T)0.0, pc = (T)1.0;
-  T intra = CFP[5] * (T)3.5449077018110318;
+  const T y = min_gpu(xv * xv, (T)1.0);  // x^2 at the cosine clamped to [-1, 1]
+  T qm = (T)1.0, qc = (T)watson_leg_a(0) * y - (T)watson_leg_b(0);
+  T intra = CFP[5] + CFP[6] * P[10] * qc;
 #pragma unroll
-  for (int l = 0; l < 6; l++) {
-    const T pn = ((T)watson_leg_a(l) * y - (T)watson_leg_b(l)) * pc - (T)watson_leg_g(l) * pm;
-    pm = pc;
-    pc = pn;
-    intra += CFP[6 + l] * P[10 + l] * pc;
+  for (int l = 1; l < 6; l++) {
+    const T qn = ((T)watson_qa(l) * y - (T)watson_qb(l)) * qc - qm;
+    qm = qc;
+    qc = qn;
+    intra += CFP[6 + l] * P[10 + l] * qc;
   }
   if (intra < (T)0.0) intra = (T)0.5e-3;
   const T aniso = ((T)1.0 - P[1]) * extra + P[1] * intra;
@@ -331,40 +357,45 @@ MACRO T Predicted_Signal(int npar, T* P, T* CFP, T* FixP) {
 }
 
 // Two measurements per call on Blackwell's paired FP32 instructions
-// (FFMA2/FMUL2/FADD2 on float2): the same arithmetic as Predicted_Signal
-// for measurements a and b, with every multiply and add issued once for
-// both. Used by the kernels' cost loops (optional hook CDM_SIGNAL_PAIR).
+// (FFMA2/FMUL2/FADD2 on float2): the arithmetic of Predicted_Signal for
+// measurements a and b, with every multiply and add issued once for both.
+// ab[k] = (column k of a, column k of b). The extra-cellular exponential uses
+// the hardware exp2 approximation (__expf): its error is at most about
+// (2 + |x| log2(e)) ulp of e^x, and because |x| is large only where e^x is
+// small, at most 2e-7 S0 of the signal. Used by the kernels' cost loops
+// (optional hook CDM_SIGNAL_PAIR).
 #if defined(__CUDACC__) && !defined(CDM_NO_SIGNAL_PAIR)
 #define CDM_SIGNAL_PAIR 1
 __device__ __forceinline__ float2 watson_bc(float x) { return make_float2(x, x); }
-__device__ __forceinline__ float2 Predicted_Signal_Pair(const fp32* P, const fp32* A, const fp32* B,
+__device__ __forceinline__ float2 Predicted_Signal_Pair(const fp32* P, const float2* ab,
                                                         const fp32* FixP) {
-  float2 xv = __fmul2_rn(make_float2(A[0].v, B[0].v), watson_bc(P[5].v));
-  xv = __ffma2_rn(make_float2(A[1].v, B[1].v), watson_bc(P[6].v), xv);
-  xv = __ffma2_rn(make_float2(A[2].v, B[2].v), watson_bc(P[7].v), xv);
+  // S = k1 extra + k2 intra + k3 CFP4: the compartment weights folded
+  const float k3 = FixP[0].v * P[0].v;
+  const float k0 = FixP[0].v * (1.0f - P[0].v);
+  const float k1 = k0 * (1.0f - P[1].v), k2 = k0 * P[1].v;
+  float2 xv = __fmul2_rn(ab[0], watson_bc(P[5].v));
+  xv = __ffma2_rn(ab[1], watson_bc(P[6].v), xv);
+  xv = __ffma2_rn(ab[2], watson_bc(P[7].v), xv);
   const float2 q = __ffma2_rn(__fmul2_rn(watson_bc(P[9].v), xv), xv, watson_bc(P[8].v));
-  const float2 z = __fmul2_rn(make_float2(-A[3].v, -B[3].v), q);
-  const float2 extra = make_float2((float)exp_gpu(fp32(z.x)), (float)exp_gpu(fp32(z.y)));
-  const float2 x = make_float2(fminf(fmaxf(xv.x, -1.0f), 1.0f), fminf(fmaxf(xv.y, -1.0f), 1.0f));
-  const float2 y = __fmul2_rn(x, x);
-  float2 pm = make_float2(0.0f, 0.0f), pc = make_float2(1.0f, 1.0f);
-  float2 intra = __fmul2_rn(make_float2(A[5].v, B[5].v), watson_bc(3.5449077018110318f));
+  const float2 z = __fmul2_rn(ab[3], q);
+  const float2 extra = make_float2(__expf(-z.x), __expf(-z.y));
+  float2 y = __fmul2_rn(xv, xv);  // x^2 at the cosine clamped to [-1, 1]
+  y = make_float2(fminf(y.x, 1.0f), fminf(y.y, 1.0f));
+  float2 qm = make_float2(1.0f, 1.0f);
+  float2 qc = __ffma2_rn(watson_bc((float)watson_leg_a(0)), y, watson_bc(-(float)watson_leg_b(0)));
+  float2 intra = __ffma2_rn(__fmul2_rn(ab[6], watson_bc(P[10].v)), qc, ab[5]);
 #pragma unroll
-  for (int l = 0; l < 6; l++) {
-    const float2 u = __ffma2_rn(watson_bc((float)watson_leg_a(l)), y, watson_bc(-(float)watson_leg_b(l)));
-    const float2 pn = __ffma2_rn(u, pc, __fmul2_rn(watson_bc(-(float)watson_leg_g(l)), pm));
-    pm = pc;
-    pc = pn;
-    intra = __ffma2_rn(__fmul2_rn(make_float2(A[6 + l].v, B[6 + l].v), watson_bc(P[10 + l].v)), pc,
-                       intra);
+  for (int l = 1; l < 6; l++) {
+    const float2 u = __ffma2_rn(watson_bc((float)watson_qa(l)), y, watson_bc(-(float)watson_qb(l)));
+    const float2 qn = __ffma2_rn(u, qc, make_float2(-qm.x, -qm.y));
+    qm = qc;
+    qc = qn;
+    intra = __ffma2_rn(__fmul2_rn(ab[6 + l], watson_bc(P[10 + l].v)), qc, intra);
   }
   if (intra.x < 0.0f) intra.x = 0.5e-3f;
   if (intra.y < 0.0f) intra.y = 0.5e-3f;
-  const float2 aniso =
-      __ffma2_rn(watson_bc(1.0f - P[1].v), extra, __fmul2_rn(watson_bc(P[1].v), intra));
-  const float2 s = __ffma2_rn(watson_bc(1.0f - P[0].v), aniso,
-                              __fmul2_rn(watson_bc(P[0].v), make_float2(A[4].v, B[4].v)));
-  return __fmul2_rn(watson_bc(FixP[0].v), s);
+  return __ffma2_rn(watson_bc(k3), ab[4],
+                    __ffma2_rn(watson_bc(k1), extra, __fmul2_rn(watson_bc(k2), intra)));
 }
 #endif
 
@@ -379,24 +410,25 @@ MACRO void Partial_Derivatives(int npar, T* P, T* CFP, T* FixP, T* derivatives) 
   const T x = min_gpu(max_gpu(xv, (T)-1.0), (T)1.0);
   const bool inside = (xv > (T)-1.0) && (xv < (T)1.0);
   const T y = x * x;
-  // P_2l and dP_2l/dx by the even recurrence and its derivative
-  // dP_{n+2} = 2 a_n x P_n + (a_n y - b_n) dP_n - g_n dP_{n-2}.
-  T pm = (T)0.0, pc = (T)1.0, dpm = (T)0.0, dpc = (T)0.0;
-  T intra = CFP[5] * (T)3.5449077018110318;
-  T dintra_x = (T)0.0, dintra_k = (T)0.0;
+  // q_l = P_2l / h_l and dq_l/dx by the rescaled recurrence and its
+  // derivative (see watson_h)
+  T qm = (T)1.0, qc = (T)watson_leg_a(0) * y - (T)watson_leg_b(0);
+  T dqm = (T)0.0, dqc = (T)2.0 * (T)watson_leg_a(0) * x;
+  T intra = CFP[5] + CFP[6] * P[10] * qc;
+  T dintra_x = CFP[6] * P[10] * dqc, dintra_k = CFP[6] * P[20] * qc;
 #pragma unroll
-  for (int l = 0; l < 6; l++) {
-    const T a = (T)watson_leg_a(l);
-    const T f = a * y - (T)watson_leg_b(l);
-    const T pn = f * pc - (T)watson_leg_g(l) * pm;
-    const T dpn = (T)2.0 * a * x * pc + f * dpc - (T)watson_leg_g(l) * dpm;
-    pm = pc;
-    pc = pn;
-    dpm = dpc;
-    dpc = dpn;
-    intra += CFP[6 + l] * P[10 + l] * pc;
-    dintra_x += CFP[6 + l] * P[10 + l] * dpc;
-    dintra_k += CFP[6 + l] * P[20 + l] * pc;
+  for (int l = 1; l < 6; l++) {
+    const T a = (T)watson_qa(l);
+    const T f = a * y - (T)watson_qb(l);
+    const T qn = f * qc - qm;
+    const T dqn = (T)2.0 * a * x * qc + f * dqc - dqm;
+    qm = qc;
+    qc = qn;
+    dqm = dqc;
+    dqc = dqn;
+    intra += CFP[6 + l] * P[10 + l] * qc;
+    dintra_x += CFP[6 + l] * P[10 + l] * dqc;
+    dintra_k += CFP[6 + l] * P[20 + l] * qc;
   }
   if (intra < (T)0.0) {
     intra = (T)0.5e-3;

@@ -38,6 +38,11 @@ def test_predicted_signal_watson(built, cuda):
     got = pred.cpu().numpy()
     tol = 2e-5 * np.abs(ref) + 2e-6 * wl.fixp
     assert np.all(np.abs(got - ref) <= tol), np.max(np.abs(got - ref) / np.abs(ref))
+    # measurements 0..255 come from the paired hook (the cost loops'
+    # function, with the hardware exp2 in the extra-cellular term), the
+    # rest from Predicted_Signal: both within 1e-6 S0
+    err = np.abs(got - ref) / wl.fixp
+    assert err[:, :256].max() <= 1e-6 and err[:, 256:].max() <= 1e-6, (err[:, :256].max(), err[:, 256:].max())
 
 
 def test_predicted_signal_ball_1_stick_mean_of_samples(built, cuda):
