@@ -359,14 +359,19 @@ MACRO T Predicted_Signal(int npar, T* P, T* CFP, T* FixP) {
 // Two measurements per call on Blackwell's paired FP32 instructions
 // (FFMA2/FMUL2/FADD2 on float2): the arithmetic of Predicted_Signal for
 // measurements a and b, with every multiply and add issued once for both.
-// ab[k] = (column k of a, column k of b). The extra-cellular exponential uses
-// the hardware exp2 approximation (__expf): its error is at most about
+// ab[k] = (column k of a, column k of b). The extra-cellular exponential is
+// the hardware exp2 approximation of its base-2 form: its error is about
 // (2 + |x| log2(e)) ulp of e^x, and because |x| is large only where e^x is
 // small, at most 2e-7 S0 of the signal. Used by the kernels' cost loops
 // (optional hook CDM_SIGNAL_PAIR).
 #if defined(__CUDACC__) && !defined(CDM_NO_SIGNAL_PAIR)
 #define CDM_SIGNAL_PAIR 1
 __device__ __forceinline__ float2 watson_bc(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float watson_ex2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 __device__ __forceinline__ float2 Predicted_Signal_Pair(const fp32* P, const float2* ab,
                                                         const fp32* FixP) {
   // S = k1 extra + k2 intra + k3 CFP4: the compartment weights folded
@@ -376,9 +381,14 @@ __device__ __forceinline__ float2 Predicted_Signal_Pair(const fp32* P, const flo
   float2 xv = __fmul2_rn(ab[0], watson_bc(P[5].v));
   xv = __ffma2_rn(ab[1], watson_bc(P[6].v), xv);
   xv = __ffma2_rn(ab[2], watson_bc(P[7].v), xv);
-  const float2 q = __ffma2_rn(__fmul2_rn(watson_bc(P[9].v), xv), xv, watson_bc(P[8].v));
+  // extra = exp(-b q) = 2^(b * (-log2(e) q)): the factor -log2(e) rides on
+  // the (per-proposal) diffusivities, and the power of two is the hardware
+  // ex2.approx.ftz (relative error ~2^-22; results below 2^-126, where the
+  // term no longer counts, flush to zero)
+  const float nl2e = -1.4426950408889634f;
+  const float2 q = __ffma2_rn(__fmul2_rn(watson_bc(P[9].v * nl2e), xv), xv, watson_bc(P[8].v * nl2e));
   const float2 z = __fmul2_rn(ab[3], q);
-  const float2 extra = make_float2(__expf(-z.x), __expf(-z.y));
+  const float2 extra = make_float2(watson_ex2(z.x), watson_ex2(z.y));
   float2 y = __fmul2_rn(xv, xv);  // x^2 at the cosine clamped to [-1, 1]
   y = make_float2(fminf(y.x, 1.0f), fminf(y.y, 1.0f));
   float2 qm = make_float2(1.0f, 1.0f);
