@@ -192,9 +192,9 @@ cdm_status set_smem(K kernel, size_t bytes) {
   return CDM_OK;
 }
 
-// Lanes per voxel: explicit choice, else a per-stage default measured on
-// GB300 for a 200k-voxel, 288-measurement NODDI-Watson fit (MCMC and LM: 4,
-// grid search: 8). Each lane repeats the parameter-only work and takes part
+// Lanes per voxel: explicit choice, else a per-stage floor measured on
+// GB300 for a 200k-voxel, 288-measurement NODDI-Watson fit (grid search 2,
+// LM 4, MCMC 2). Each lane repeats the parameter-only work and takes part
 // in the group reductions, so few lanes are best while there are enough
 // voxels to fill the GPU; with fewer voxels than about four waves of
 // resident threads the group is widened.
@@ -361,10 +361,10 @@ cdm_status run_mcmc(cdm_ctx* c, int nvox, int nmeas, const double* meas, double*
   if (!samples) return cdm_fail(CDM_BAD_ARG, "samples is null");
   if (c->cfg.rician && !tau) return cdm_fail(CDM_BAD_ARG, "rician MCMC needs tau_samples");
   CDM_TRY(prep_protocol(c, nmeas, CFP, st));
-  // measured on NODDI-Watson, 200k voxels, 500 + 500 jumps: 1 lane 466 ms,
-  // 2 lanes 469 ms, 4 lanes 504 ms (fewer lanes per voxel share the
-  // per-proposal work among fewer threads)
-  const int G = pick_lanes(c, c->cfg.lanes_mcmc, 1, nvox);
+  // measured on NODDI-Watson, 200k voxels, 500 + 500 jumps: 2 lanes 420 ms,
+  // 1 lane 443 ms, 4 lanes 469 ms: fewer lanes per voxel repeat the
+  // per-proposal work in fewer threads
+  const int G = pick_lanes(c, c->cfg.lanes_mcmc, 2, nvox);
   CDM_TRY(pack_signals(c, G, nvox, nmeas, meas, st));
   if (nvox == 0) return CDM_OK;
   const bool ric = c->cfg.rician != 0;

@@ -215,10 +215,10 @@ __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const fl
     const float2 r = __fadd2_rn(s2, make_float2(-sig[0], -sig[io.chunk_stride]));
     acc2 = __ffma2_rn(r, r, acc2);
     q += 2 * G * kNCOLS;
-    row += 2 * G * kNCOLS4;
     sig += 2 * io.chunk_stride;
   }
   acc = acc2.x + acc2.y;
+  row += (size_t)c * G * kNCOLS4;
   if (c < full) {
     fp32 cf[kNCOLS];
     cdm_load_cfp(row, 0, 0, cf);
