@@ -101,7 +101,7 @@ bool ends_with(const std::string& s, const char* suffix) {
 // plain files through unchanged).
 class in_file {
  public:
-  explicit in_file(const char* path) : path_(path) {
+  explicit in_file(const char* path) {
 #ifdef CDM_HAVE_ZLIB
     gz_ = gzopen(path, "rb");
     ok_ = gz_ != nullptr;
@@ -153,7 +153,7 @@ class in_file {
   }
 
  private:
-  std::string path_, err_;
+  std::string err_;
   bool ok_ = false, gzipped_ = false;
 #ifdef CDM_HAVE_ZLIB
   gzFile gz_ = nullptr;
