@@ -662,6 +662,8 @@ def bench_bingham(a, dev):
                      lm_iterations_per_voxel=lib.stats().lm_iterations / (n + k),
                      fp32_vs_fp64_oracle_lm=vs_oracle, posterior_mean_vs_truth=vs_truth,
                      reference_kernels=refk, gpu_launches=9)
+    # one pass of the 1M-voxel fit (a few minutes) is the measurement
+    line["steps"], line["warmup"] = 1, 0
     print(json.dumps(line))
 
 
