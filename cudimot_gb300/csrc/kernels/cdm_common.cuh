@@ -18,9 +18,10 @@
 // so a warp's signal load is one contiguous 128-byte line.
 // With the paired signal hook (Predicted_Signal_Pair) the kernels that take
 // the paired cost loop also keep, after the staged protocol in shared
-// memory, a pair table float2 [nchunk/2][G][NCOLS]: entry (j, l, k) holds
-// column k of measurements 2jG+l and (2j+1)G+l, the two a lane evaluates
-// together, so a 16-byte load gives two columns already paired.
+// memory, a pair table float2 [nchunk/2][G][NCOLSP] (NCOLS rounded up to
+// even, the pad column zero): entry (j, l, k) holds column k of
+// measurements 2jG+l and (2j+1)G+l, the two a lane evaluates together, so a
+// 16-byte load gives two columns already paired.
 #pragma once
 
 #include <stdint.h>
@@ -43,6 +44,7 @@ constexpr int kNPS = CDM_PSTORE;
 constexpr int kNCOLS = CDM_CFP_TSIZE + CDM_NDCFP;
 constexpr int kNCOLS4 = (kNCOLS + 3) / 4 * 4;  // protocol row stride (floats)
 constexpr int kNFIX = CDM_FIXP_TSIZE > 0 ? CDM_FIXP_TSIZE : 1;
+constexpr int kNCOLSP = (kNCOLS + 1) / 2 * 2;  // pair-table entry stride (column pairs, even)
 #ifdef CDM_SIGNAL_PAIR
 constexpr int kPairTables = 1;  // shared-memory protocol copies of the paired-loop kernels
 #else
@@ -161,31 +163,27 @@ __device__ __forceinline__ const float* cdm_build_pair_table(float* sproto, int 
                                                              int nchunk) {
   float2* ptab = reinterpret_cast<float2*>(sproto + (size_t)nmeas_pad * kNCOLS4);
 #ifdef CDM_SIGNAL_PAIR
-  const int total = (nchunk / 2) * G * kNCOLS;
+  const int total = (nchunk / 2) * G * kNCOLSP;
   for (int i = (int)threadIdx.x; i < total; i += (int)blockDim.x) {
-    const int k = i % kNCOLS, l = (i / kNCOLS) % G, j = i / (kNCOLS * G);
-    ptab[i] = make_float2(sproto[(size_t)(2 * j * G + l) * kNCOLS4 + k],
-                          sproto[(size_t)((2 * j + 1) * G + l) * kNCOLS4 + k]);
+    const int k = i % kNCOLSP, l = (i / kNCOLSP) % G, j = i / (kNCOLSP * G);
+    ptab[i] = k < kNCOLS ? make_float2(sproto[(size_t)(2 * j * G + l) * kNCOLS4 + k],
+                                       sproto[(size_t)((2 * j + 1) * G + l) * kNCOLS4 + k])
+                         : make_float2(0.0f, 0.0f);
   }
   __syncthreads();
 #endif
   return reinterpret_cast<const float*>(ptab);
 }
 
-// One pair-table entry: the NCOLS column pairs of a lane's two measurements.
+// One pair-table entry: the NCOLS column pairs of a lane's two measurements
+// (16-byte loads: entries are a whole number of 16-byte units).
 __device__ __forceinline__ void cdm_load_pairs(const float* q, float2* ab) {
-  if constexpr (kNCOLS % 2 == 0) {
-    const float4* q4 = reinterpret_cast<const float4*>(q);
+  const float4* q4 = reinterpret_cast<const float4*>(q);
 #pragma unroll
-    for (int k = 0; k < kNCOLS / 2; k++) {
-      const float4 v = q4[k];
-      ab[2 * k] = make_float2(v.x, v.y);
-      ab[2 * k + 1] = make_float2(v.z, v.w);
-    }
-  } else {
-    const float2* q2 = reinterpret_cast<const float2*>(q);
-#pragma unroll
-    for (int k = 0; k < kNCOLS; k++) ab[k] = q2[k];
+  for (int k = 0; k < kNCOLSP / 2; k++) {
+    const float4 v = q4[k];
+    ab[2 * k] = make_float2(v.x, v.y);
+    if (2 * k + 1 < kNCOLS) ab[2 * k + 1] = make_float2(v.z, v.w);
   }
 }
 
@@ -214,7 +212,7 @@ __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const fl
     const float2 s2 = Predicted_Signal_Pair(P, ab, FixP);
     const float2 r = __fadd2_rn(s2, make_float2(-sig[0], -sig[io.chunk_stride]));
     acc2 = __ffma2_rn(r, r, acc2);
-    q += 2 * G * kNCOLS;
+    q += 2 * G * kNCOLSP;
     sig += 2 * io.chunk_stride;
   }
   acc = acc2.x + acc2.y;

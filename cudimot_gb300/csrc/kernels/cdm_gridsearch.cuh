@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_gridsearch_kernel(const __grid_con
   io.nmeas = a.nmeas;
   io.nmeas_pad = a.nmeas_pad;
   io.lane = lane;
-  io.pairs = ptab + (size_t)lane * kNCOLS * 2;
+  io.pairs = ptab + (size_t)lane * kNCOLSP * 2;
 
   double base[kNP];
 #pragma unroll

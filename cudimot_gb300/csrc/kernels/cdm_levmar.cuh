@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
   io.nmeas = a.nmeas;
   io.nmeas_pad = a.nmeas_pad;
   io.lane = lane;
-  io.pairs = ptab + (size_t)lane * kNCOLS * 2;
+  io.pairs = ptab + (size_t)lane * kNCOLSP * 2;
 
   fp32 P[kNPS], FixP[kNFIX];
   float Pt[kNP];

@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
   io.nmeas = a.nmeas;
   io.nmeas_pad = a.nmeas_pad;
   io.lane = lane;
-  io.pairs = ptab + (size_t)lane * kNCOLS * 2;
+  io.pairs = ptab + (size_t)lane * kNCOLSP * 2;
 
   fp32 P[kNPS], FixP[kNFIX];
   cdm_load_params(a.params + (size_t)v * kNP, P);

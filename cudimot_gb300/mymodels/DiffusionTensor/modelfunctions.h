@@ -40,6 +40,32 @@ MACRO T Predicted_Signal(int npar, T* P, T* CFP, T* FixP) {
   return P[0] * exp_gpu(dt_exponent(P, CFP, 9));
 }
 
+// Two measurements per call on the paired FP32 instructions (optional hook
+// CDM_SIGNAL_PAIR; ab[k] = column k of both measurements): the same six
+// products and exponential, with the exponential in base 2 -- the factor
+// -log2(e) rides on the (per-proposal) tensor entries -- on the hardware
+// ex2.approx.ftz (relative error ~2^-22).
+#if defined(__CUDACC__) && !defined(CDM_NO_SIGNAL_PAIR)
+#define CDM_SIGNAL_PAIR 1
+__device__ __forceinline__ float2 dt_bc(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float dt_ex2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float2 Predicted_Signal_Pair(const fp32* P, const float2* ab,
+                                                        const fp32* FixP) {
+  const float k = -1.4426950408889634f;
+  float2 z = __fmul2_rn(ab[4], dt_bc(P[1].v * k));
+  z = __ffma2_rn(ab[7], dt_bc(P[4].v * k), z);
+  z = __ffma2_rn(ab[9], dt_bc(P[6].v * k), z);
+  z = __ffma2_rn(ab[5], dt_bc(P[2].v * k), z);
+  z = __ffma2_rn(ab[6], dt_bc(P[3].v * k), z);
+  z = __ffma2_rn(ab[8], dt_bc(P[5].v * k), z);
+  return __fmul2_rn(dt_bc(P[0].v), make_float2(dt_ex2(z.x), dt_ex2(z.y)));
+}
+#endif
+
 MACRO bool ConstraintsMCMC(int npar, T* P) { return true; }
 
 MACRO void Partial_Derivatives(int npar, T* P, T* CFP, T* FixP, T* derivatives) {

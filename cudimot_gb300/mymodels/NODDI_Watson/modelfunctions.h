@@ -391,17 +391,22 @@ __device__ __forceinline__ float2 Predicted_Signal_Pair(const fp32* P, const flo
   const float2 extra = make_float2(watson_ex2(z.x), watson_ex2(z.y));
   float2 y = __fmul2_rn(xv, xv);  // x^2 at the cosine clamped to [-1, 1]
   y = make_float2(fminf(y.x, 1.0f), fminf(y.y, 1.0f));
-  float2 qm = make_float2(1.0f, 1.0f);
-  float2 qc = __ffma2_rn(watson_bc((float)watson_leg_a(0)), y, watson_bc(-(float)watson_leg_b(0)));
-  float2 intra = __ffma2_rn(__fmul2_rn(ab[6], watson_bc(P[10].v)), qc, ab[5]);
+  // intra = sum_l a_l q_l (a_0 = ab[5], a_l = ab[5+l] P[9+l]) by Clenshaw's
+  // backward recurrence on the rescaled one: b_l = a_l + u_l b_(l+1) -
+  // b_(l+2) for l = 6..1, intra = a_0 + u_0 b_1 - b_2 (three operations per
+  // degree instead of four)
+  float2 b2 = make_float2(0.0f, 0.0f);
+  float2 b1 = __fmul2_rn(ab[11], watson_bc(P[15].v));
 #pragma unroll
-  for (int l = 1; l < 6; l++) {
+  for (int l = 5; l >= 1; l--) {
     const float2 u = __ffma2_rn(watson_bc((float)watson_qa(l)), y, watson_bc(-(float)watson_qb(l)));
-    const float2 qn = __ffma2_rn(u, qc, make_float2(-qm.x, -qm.y));
-    qm = qc;
-    qc = qn;
-    intra = __ffma2_rn(__fmul2_rn(ab[6 + l], watson_bc(P[10 + l].v)), qc, intra);
+    const float2 t = __ffma2_rn(ab[5 + l], watson_bc(P[9 + l].v), make_float2(-b2.x, -b2.y));
+    const float2 bn = __ffma2_rn(u, b1, t);
+    b2 = b1;
+    b1 = bn;
   }
+  const float2 u0 = __ffma2_rn(watson_bc((float)watson_qa(0)), y, watson_bc(-(float)watson_qb(0)));
+  float2 intra = __ffma2_rn(u0, b1, __fadd2_rn(ab[5], make_float2(-b2.x, -b2.y)));
   if (intra.x < 0.0f) intra.x = 0.5e-3f;
   if (intra.y < 0.0f) intra.y = 0.5e-3f;
   return __ffma2_rn(watson_bc(k3), ab[4],

@@ -156,8 +156,12 @@ inline int gridsearch_voxel(const Limits& L, int ngp, const int* gparams, int co
   int best = -1;
   T bestP[NPS];
   for (int i = 0; i < NPS; i++) bestP[i] = (i < NP) ? base[i] : (T)0.0;
+  // one parameter array across the combinations: its derived slots start at
+  // zero (Derived_P's caches count as empty) and then always belong to the
+  // previous combination, as the plugin's caches expect
+  T trial[NPS];
+  for (int i = 0; i < NPS; i++) trial[i] = (i < NP) ? base[i] : (T)0.0;
   for (int c = 0; c < combs; c++) {
-    T trial[NPS];
     for (int i = 0; i < NP; i++) trial[i] = base[i];
     for (int i = 0; i < ngp; i++) trial[gparams[i]] = (T)grid[(size_t)c * ngp + i];
     if (!gs_check_bounds(L, trial)) continue;

@@ -17,7 +17,7 @@ import pytest
 import torch
 
 from cudimot_gb300 import capi
-from tests.helpers import angle_deg, b1s, oracle, watson
+from tests.helpers import angle_deg, b1s, b2s, dt, oracle, watson
 
 pytestmark = pytest.mark.gpu
 
@@ -43,6 +43,22 @@ def test_predicted_signal_watson(built, cuda):
     # rest from Predicted_Signal: both within 1e-6 S0
     err = np.abs(got - ref) / wl.fixp
     assert err[:, :256].max() <= 1e-6 and err[:, 256:].max() <= 1e-6, (err[:, :256].max(), err[:, 256:].max())
+
+
+@pytest.mark.parametrize("model,make", [("DiffusionTensor", dt), ("Ball_2_Sticks", b2s)])
+def test_predicted_signal_paired_hook(built, cuda, model, make):
+    """DT and Ball_2_Sticks through their paired hooks (measurements m and
+    m + 32 of each lane; base-2 exponentials on the hardware ex2) and
+    Predicted_Signal (the rest): within 1e-6 S0 of the FP64 oracle."""
+    wl = make(3000, seed=4)
+    o = oracle(model)
+    lib = capi.Cudimot(model, capi.model_cfg(model))
+    pred = torch.zeros(wl.nvox, wl.nmeas, dtype=torch.float64, device=cuda)
+    lib.predicted_signal(T(wl.truth[:, :, None], cuda), T(wl.cfp, cuda), T(wl.fixp, cuda), pred)
+    torch.cuda.synchronize()
+    ref = o.signal(wl.truth, wl.cfp, wl.fixp)
+    err = np.abs(pred.cpu().numpy() - ref) / wl.truth[:, :1]
+    assert err.max() <= 1e-6, err.max()
 
 
 def test_predicted_signal_ball_1_stick_mean_of_samples(built, cuda):
