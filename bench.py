@@ -56,13 +56,14 @@ def parse():
     ap.add_argument("--nburn", type=int, default=NBURN)
     ap.add_argument("--njumps", type=int, default=NJUMPS)
     ap.add_argument("--workload", default="noddi_watson",
-                    choices=["noddi_watson", "ball_1_stick_lm", "heterogeneous", "learned_init",
-                             "noddi_bingham"],
+                    choices=["noddi_watson", "noddi_watson_rician", "ball_1_stick_lm", "heterogeneous",
+                             "learned_init", "noddi_bingham"],
                     help="noddi_watson: the headline (200k voxels GS->LM->MCMC); "
                          "ball_1_stick_lm: 10k voxels plain LM; heterogeneous: DiffusionTensor "
                          "400k + Ball_2_Sticks 300k + NODDI_Watson 500k LM+MCMC in one graph; "
                          "learned_init: network-initialised vs grid-initialised NODDI_Watson; "
-                         "noddi_bingham: 1M voxels GS (11,050) -> LM -> MCMC, precision study")
+                         "noddi_bingham: 1M voxels GS (11,050) -> LM -> MCMC, precision study; "
+                         "noddi_watson_rician: the headline fit with the Rician likelihood")
     ap.add_argument("--train-signals", type=int, default=20_000_000)
     ap.add_argument("--lm-targets", type=int, default=1_000_000)
     ap.add_argument("--epochs", type=int, default=2)
@@ -551,6 +552,79 @@ def bench_learned(a, dev):
     print(json.dumps(line))
 
 
+# FP32 operations of the Rician term per measurement beyond the signal:
+# -tau/2 (y^2 + S^2) (4), tau S y (2), the accumulation (1) and log I0
+# (cdm_log_i0: the x / 3.75 scaling, its square and a degree-6 polynomial,
+# 16; its logarithm is a transcendental, not counted)
+F_RICIAN = 23
+
+
+def bench_rician(a, dev):
+    """The headline fit (200k NODDI-Watson voxels, GS -> LM -> MCMC 1250 +
+    1250) with the Rician likelihood (--rician: tau sampled with the
+    parameters, CUDIMOT's MCMC.cu Rician energy), device-resident inputs."""
+    import torch
+    from cudimot_gb300 import capi, flops
+    nvox = a.nvox or NVOX
+    cfp, meas, fixp, init, truth = make_workload(nvox, 8219, dev)
+    cfg = workload_cfg()
+    cfg.rician = 1
+    lib = capi.Cudimot(MODEL, cfg)
+    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
+    m, c, f, p0 = t(meas), t(cfp), t(fixp), t(init)
+    p = p0.clone()
+    ns = NJUMPS // SE
+    samples = torch.zeros(nvox, 5, ns, dtype=torch.float64, device=dev)
+    tau = torch.zeros(nvox, ns, dtype=torch.float64, device=dev)
+
+    def step():
+        p.copy_(p0)
+        lib.fit(m, p, c, f, samples, tau=tau)
+
+    for _ in range(a.warmup):
+        step()
+    with ClockSampler(dev.index or 0) as clk:
+        ms = statistics.median(timed_events(step, a.steps))
+    # the MCMC launch alone, from the grid-search + LM start
+    q = p0.clone()
+    lib.gridsearch(m, q, c, f)
+    lib.levmar(m, q, c, f)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    lib.mcmc(m, q, c, f, samples, tau=tau)
+    e1.record(st)
+    torch.cuda.synchronize()
+    mcmc_ms = e0.elapsed_time(e1)
+    fl = flops.watson_c1_flops_per_voxel()
+    ops = fl["ops"]
+    like = ops["derived_p_one_param"] + 288 * (ops["signal"] + F_RICIAN)
+    like_tau = 288 * (ops["signal"] + F_RICIAN)
+    per_voxel = (NBURN + NJUMPS) * (5 * like + like_tau)
+    peak = fp32_peak_tflops(dev)
+    achieved = per_voxel * nvox / (mcmc_ms / 1e3) / 1e12
+    roof = None
+    if peak:
+        roof = {"bound": "fp32", "kernel": "cdm_mcmc_kernel", "achieved": achieved,
+                "peak": peak["tflops"], "unit": "TFLOP/s", "frac": achieved / peak["tflops"],
+                "peak_source": peak["source"], "flop_per_voxel": per_voxel, "launch_ms": mcmc_ms,
+                "flop_note": f"signal from the operation-count build + {F_RICIAN} per measurement for the "
+                             "Rician term; one tau proposal per iteration besides the 5 parameters"}
+    s = samples.cpu().numpy().mean(2)
+    line = base_line("voxels/s fitted (GS+LM+MCMC), NODDI-Watson, Rician likelihood",
+                     nvox / (ms / 1e3), "voxels/s", a, ms,
+                     {"workload": "noddi_watson_rician_gs_lm_mcmc", "model": MODEL, "nvox": nvox,
+                      "nmeas": 288, "grid_combs": 968, "nburn": NBURN, "njumps": NJUMPS,
+                      "sampleevery": SE, "likelihood": "rician",
+                      "l2": "inputs larger than L2 (no flush)"},
+                     clk.summary(), roofline=roof, gpu_launches=gpu_launches_per_step(cfg) * a.steps,
+                     posterior_mean_vs_truth={
+                         "fiso_rmse": float(np.sqrt(np.mean((s[:, 0] - truth[:, 0]) ** 2))),
+                         "fintra_rmse": float(np.sqrt(np.mean((s[:, 1] - truth[:, 1]) ** 2)))})
+    print(json.dumps(line))
+
+
 def bench_bingham(a, dev):
     """NODDI-Bingham precision study: --nvox voxels (default 1,000,000) of
     the NODDI-Watson protocol and parameters plus beta = U(0,0.9) kappa and
@@ -678,7 +752,8 @@ def main():
         torch.cuda.set_device(local)
         dev = torch.device("cuda", local)
         {"ball_1_stick_lm": bench_b1s_lm, "heterogeneous": bench_heterogeneous,
-         "learned_init": bench_learned, "noddi_bingham": bench_bingham}[a.workload](a, dev)
+         "learned_init": bench_learned, "noddi_bingham": bench_bingham,
+         "noddi_watson_rician": bench_rician}[a.workload](a, dev)
         return
     if a.impl == "reference":
         if world > 1:

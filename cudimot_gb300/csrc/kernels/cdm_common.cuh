@@ -269,7 +269,32 @@ template <int G>
 __device__ __forceinline__ double cdm_group_rician(const cdm_voxel_io& io, const float* sproto,
                                                    fp32* P, fp32* FixP, float tau, unsigned gmask) {
   float acc = 0.0f;
-  for (int c = 0; c < io.nchunk; c++) {
+  int c0 = 0;
+#ifdef CDM_SIGNAL_PAIR
+  // full chunk pairs through the paired signal hook (the pair table), the
+  // log I0 term per measurement
+  {
+    const int full = io.nmeas / G;
+    const float* q = io.pairs;
+    const float* sig = io.sig;
+    float2 acc2 = make_float2(0.0f, 0.0f);
+    const float2 nht = make_float2(-0.5f * tau, -0.5f * tau);
+    for (; c0 + 1 < full; c0 += 2) {
+      float2 ab[kNCOLS];
+      cdm_load_pairs(q, ab);
+      const float2 s2 = Predicted_Signal_Pair(P, ab, FixP);
+      const float2 y2 = make_float2(sig[0], sig[io.chunk_stride]);
+      const float2 e = __ffma2_rn(y2, y2, __fmul2_rn(s2, s2));
+      acc2 = __ffma2_rn(nht, e, acc2);
+      acc2.x += cdm_log_i0(tau * s2.x * y2.x);
+      acc2.y += cdm_log_i0(tau * s2.y * y2.y);
+      q += 2 * G * kNCOLSP;
+      sig += 2 * io.chunk_stride;
+    }
+    acc = acc2.x + acc2.y;
+  }
+#endif
+  for (int c = c0; c < io.nchunk; c++) {
     const int m = c * G + io.lane;
     const bool valid = m < io.nmeas;
     fp32 cf[kNCOLS];
