@@ -262,6 +262,24 @@ __device__ __forceinline__ float cdm_log_i0(float x) {
                   a * 0.00392377f)))))))) * rsqrtf(b));
 }
 
+// log I0 for the MCMC energies: the same polynomials with the hardware
+// reciprocal and logarithm approximations (absolute error ~2e-7 per term,
+// far below the energy differences the Metropolis test compares); BIC/AIC
+// keep cdm_log_i0.
+__device__ __forceinline__ float cdm_log_i0_fast(float x) {
+  const float b = fabsf(x);
+  if (b < 3.75f) {
+    float a = x * (1.0f / 3.75f);
+    a *= a;
+    return __logf(1.0f + a * (3.5156229f + a * (3.0899424f + a * (1.2067492f + a * (0.2659732f +
+                          a * (0.0360768f + a * 0.0045813f))))));
+  }
+  const float a = __fdividef(3.75f, b);
+  return b + __logf((0.39894228f + a * (0.01328592f + a * (0.00225319f + a * (-0.00157565f +
+                    a * (0.00916281f + a * (-0.02057706f + a * (0.02635537f + a * (-0.01647633f +
+                    a * 0.00392377f)))))))) * rsqrtf(b));
+}
+
 // Rician log-likelihood sum without the voxel-constant sum of log(y)
 // (which cancels in every Metropolis ratio): sum of
 // -tau/2 (y^2 + S^2) + log I0(tau S y).
@@ -286,8 +304,8 @@ __device__ __forceinline__ double cdm_group_rician(const cdm_voxel_io& io, const
       const float2 y2 = make_float2(sig[0], sig[io.chunk_stride]);
       const float2 e = __ffma2_rn(y2, y2, __fmul2_rn(s2, s2));
       acc2 = __ffma2_rn(nht, e, acc2);
-      acc2.x += cdm_log_i0(tau * s2.x * y2.x);
-      acc2.y += cdm_log_i0(tau * s2.y * y2.y);
+      acc2.x += cdm_log_i0_fast(tau * s2.x * y2.x);
+      acc2.y += cdm_log_i0_fast(tau * s2.y * y2.y);
       q += 2 * G * kNCOLSP;
       sig += 2 * io.chunk_stride;
     }
@@ -301,7 +319,7 @@ __device__ __forceinline__ double cdm_group_rician(const cdm_voxel_io& io, const
     cdm_load_cfp(sproto, io.nmeas_pad, valid ? m : 0, cf);
     const float y = io.sig[(size_t)c * io.chunk_stride];
     const float s = (float)Predicted_Signal(NPARAMS, P, cf, FixP);
-    const float t = -0.5f * tau * (y * y + s * s) + cdm_log_i0(tau * s * y);
+    const float t = -0.5f * tau * (y * y + s * s) + cdm_log_i0_fast(tau * s * y);
     acc = valid ? acc + t : acc;
   }
   return cdm_group_sum<G>((double)acc, gmask);

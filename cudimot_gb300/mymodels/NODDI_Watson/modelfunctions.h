@@ -389,8 +389,8 @@ __device__ __forceinline__ float2 Predicted_Signal_Pair(const fp32* P, const flo
   const float2 q = __ffma2_rn(__fmul2_rn(watson_bc(P[9].v * nl2e), xv), xv, watson_bc(P[8].v * nl2e));
   const float2 z = __fmul2_rn(ab[3], q);
   const float2 extra = make_float2(watson_ex2(z.x), watson_ex2(z.y));
-  float2 y = __fmul2_rn(xv, xv);  // x^2 at the cosine clamped to [-1, 1]
-  y = make_float2(fminf(y.x, 1.0f), fminf(y.y, 1.0f));
+  // x^2 at the cosine clamped to [-1, 1]: a saturated multiply per half
+  const float2 y = make_float2(__saturatef(xv.x * xv.x), __saturatef(xv.y * xv.y));
   // intra = sum_l a_l q_l (a_0 = ab[5], a_l = ab[5+l] P[9+l]) by Clenshaw's
   // backward recurrence on the rescaled one: b_l = a_l + u_l b_(l+1) -
   // b_(l+2) for l = 6..1, intra = a_0 + u_0 b_1 - b_2 (three operations per
