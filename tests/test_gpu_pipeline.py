@@ -6,8 +6,11 @@
   * the steps do what the scripts do: the grid search leaves theta/phi at
     the tensor fit's V1, FitFractions leaves kappa at the grid value, and
     the final fit's cost is no worse than the grid search's;
-  * Ball_1_Stick's one-step pipeline from the tensor fit matches LM from
-    the same initial values."""
+  * Ball_1_Stick's and Ball_2_Sticks' one-step pipelines from the tensor
+    fit match LM from the same initial values;
+  * NODDI-Bingham's pipeline (grid search + LM with the orientation fixed,
+    then all but fiso) replays its graph exactly and passes fiso through
+    the last step unchanged."""
 import numpy as np
 import pytest
 import torch
@@ -92,3 +95,46 @@ def test_ball_1_stick_pipeline(built, cuda):
     lib.levmar(m, q, T(wl.cfp, cuda), T(wl.fixp, cuda))
     torch.cuda.synchronize()
     assert torch.equal(pl.params, q)
+
+
+def test_ball_2_sticks_pipeline(built, cuda):
+    """Pipeline_Ball_2_Sticks.sh: one fit from S0, L1, FA, V1, FA/4, V2 of the
+    tensor fit, as LM from those values."""
+    from tests.helpers import b2s
+    wl = b2s(2048, seed=34)
+    m = T(wl.meas, cuda)
+    pl = Pipeline("Ball_2_Sticks", m, wl.cfp[:, :3], wl.cfp[:, 3])
+    pl.run()
+    torch.cuda.synchronize()
+    d = pl.dti.cpu().numpy()
+    init = np.stack([d[:, 0], d[:, 1], d[:, 10], d[:, 12], d[:, 13], 0.25 * d[:, 10], d[:, 14],
+                     d[:, 15]], 1)
+    lib = capi.Cudimot("Ball_2_Sticks", capi.model_cfg("Ball_2_Sticks"))
+    q = T(init, cuda)
+    lib.levmar(m, q, T(wl.cfp, cuda), T(wl.fixp, cuda))
+    torch.cuda.synchronize()
+    assert torch.equal(pl.params, q)
+
+
+def test_bingham_pipeline_graph_equals_eager(built, cuda):
+    """Pipeline_NODDI_Bingham.sh: grid search + LM with the orientation
+    fixed (psi from the tensor fit), then all but fiso; the graph replay
+    equals the eager run, fiso passes the second step unchanged, and the
+    finish step gives finite dyads and OD."""
+    from tests.helpers import bingham
+    wl = bingham(512, seed=35)
+    m = T(wl.meas, cuda)
+    eager = Pipeline("NODDI_Bingham", m, wl.cfp[:, :3], wl.cfp[:, 3], run_mcmc=True, nburn=40,
+                     njumps=40, sampleevery=10)
+    eager.run(graph=False)
+    torch.cuda.synchronize()
+    g = Pipeline("NODDI_Bingham", m, wl.cfp[:, :3], wl.cfp[:, 3], run_mcmc=True, nburn=40,
+                 njumps=40, sampleevery=10)
+    g.run()
+    torch.cuda.synchronize()
+    assert torch.equal(g.samples, eager.samples)
+    s = g.samples.cpu().numpy()
+    # fiso is fixed in the last step: every sample equals the grid/LM value
+    assert np.all(s[:, 0, :] == s[:, 0, :1])
+    np.testing.assert_array_equal(s[:, 0, 0], g.params.cpu().numpy()[:, 0])
+    assert np.all(np.isfinite(g.dyads.cpu().numpy())) and np.all(np.isfinite(g.od.cpu().numpy()))
