@@ -216,6 +216,7 @@ def _declare(lib):
         "cdm_fit": [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "cdm_fit_host": [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, i, i64],
         "cdm_clean_signals": [i, i, _vp, _vp],
+        "cdm_selftest_wait_timeout": [_vp, i, _vp],
         "cdm_fit_reserve": [_vp, i, i],
         "cdm_mcmc_seeded": [_vp, i, i, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "cdm_synth_signals": [_vp, i, i, _vp, _vp, _vp, C.c_double, C.c_double, C.c_uint64, i,
@@ -246,7 +247,8 @@ EXPORTED = ("cdm_get_model_info", "cdm_default_cfg", "cdm_status_string", "cdm_l
             "cdm_bic_aic", "cdm_predicted_signal", "cdm_fit", "cdm_fit_host",
             "cdm_fit_reserve", "cdm_fit_enqueue", "cdm_synchronize", "cdm_get_stats",
             "cdm_mcmc_seeded", "cdm_synth_signals", "cdm_mlp_head_info", "cdm_mlp_targets",
-            "cdm_mlp_decode", "cdm_cost", "cdm_select_worse", "cdm_rows", "cdm_clean_signals")
+            "cdm_mlp_decode", "cdm_cost", "cdm_select_worse", "cdm_rows", "cdm_clean_signals",
+            "cdm_selftest_wait_timeout")
 
 
 def lib_path(model: str) -> str:
@@ -362,6 +364,11 @@ class Cudimot:
         _check(self.lib, self.lib.cdm_fit_host(self.ctx, nv, nm, p(meas), p(params), p(cfp), p(fixp),
                                                p(samples), p(tau), p(pred), p(bic), p(aic),
                                                part_size, timeout_ms), "fit_host")
+
+    def selftest_wait_timeout(self, limit_ms=50):
+        """cdm_selftest_wait_timeout on the current torch stream."""
+        _check(self.lib, self.lib.cdm_selftest_wait_timeout(self.ctx, limit_ms, self._stream()),
+               "selftest_wait_timeout")
 
     def clean_signals(self, meas):
         """cdm_clean_signals in place on a CUDA float64 [nvox][nmeas] tensor."""

@@ -497,6 +497,18 @@ __global__ void cdm_clean_signals_kernel(int nvox, int nmeas, double* __restrict
     if ((float)row[m] <= 0.0f) row[m] = rep;
 }
 
+// Self-test of the bounded waits: the CTA initialises an mbarrier that
+// expects one arrival nobody makes and waits on it; the wait must give up
+// after limit_ns and record CDM_DEVERR_STAGE_TIMEOUT (no copy is in flight,
+// so the CTA can simply return).
+__global__ void cdm_wait_selftest_kernel(uint64_t limit_ns, int* err) {
+  __shared__ __align__(8) uint64_t bar;
+  const uint32_t sbar = (uint32_t)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sbar), "r"(1) : "memory");
+  __syncthreads();
+  cdm_mbar_wait_phase0(sbar, limit_ns, threadIdx.x == 0 ? err : nullptr);
+}
+
 }  // namespace
 
 // =================================================================== C ABI
@@ -911,6 +923,15 @@ cdm_status cdm_get_stats(cdm_ctx* c, cdm_stats* s) {
   int err = 0;
   CDM_CUDA(cudaMemcpy(&err, c->err, sizeof(int), cudaMemcpyDeviceToHost));
   s->device_errors = err;
+  return CDM_OK;
+}
+
+cdm_status cdm_selftest_wait_timeout(cdm_ctx* c, int limit_ms, void* stream) {
+  if (!c) return cdm_fail(CDM_BAD_ARG, "null context");
+  if (limit_ms < 1 || limit_ms > 2000) return cdm_fail(CDM_BAD_ARG, "limit_ms must be in 1..2000");
+  CDM_TRY(ensure_base(c));
+  cdm_wait_selftest_kernel<<<1, 32, 0, (cudaStream_t)stream>>>((uint64_t)limit_ms * 1000000ull, c->err);
+  CDM_CUDA(cudaGetLastError());
   return CDM_OK;
 }
 

@@ -81,6 +81,29 @@ __device__ __forceinline__ V cdm_group_sum(V v, unsigned mask) {
   return v;
 }
 
+// Wait for phase 0 of the mbarrier at shared address sbar, at most limit_ns
+// of %globaltimer; on expiry record CDM_DEVERR_STAGE_TIMEOUT in *err (may
+// be null) and return false instead of spinning forever.
+__device__ __forceinline__ bool cdm_mbar_wait_phase0(uint32_t sbar, uint64_t limit_ns, int* err) {
+  uint64_t t0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (;;) {
+    uint32_t done = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(sbar)
+        : "memory");
+    if (done) return true;
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 > limit_ns) {
+      if (err) atomicOr(err, CDM_DEVERR_STAGE_TIMEOUT);
+      return false;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Protocol staging: one elected thread issues a bulk asynchronous copy
 // (cp.async.bulk, the TMA engine's 1-D form) of the whole protocol table from
@@ -106,25 +129,9 @@ __device__ __forceinline__ bool cdm_stage_protocol(const float* __restrict__ gsr
         "l"(gsrc), "r"(bytes), "r"(sbar)
         : "memory");
   }
-  uint64_t t0;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-  uint32_t done = 0;
-  for (;;) {
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(sbar)
-        : "memory");
-    if (done) break;
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    if (t - t0 > 2000000000ull) {
-      if (err) atomicOr(err, CDM_DEVERR_STAGE_TIMEOUT);
-      break;
-    }
-  }
+  const bool done = cdm_mbar_wait_phase0(sbar, 2000000000ull, err);
   __syncthreads();
-  return done != 0;
+  return done;
 }
 
 // Load one measurement's protocol values (raw CFP then derived) from the

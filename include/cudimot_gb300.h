@@ -196,6 +196,14 @@ cdm_status cdm_fit_host(cdm_ctx* ctx, int nvox, int nmeas, const double* meas,
                         double* samples, double* tau, double* pred, double* BIC, double* AIC,
                         int part_size, int64_t timeout_ms);
 
+/* Self-test of the bounded device waits (no CUDIMOT counterpart; CUDIMOT's
+ * kernels have no waits that can run out): launches a kernel whose mbarrier
+ * wait can never complete. The wait gives up after limit_ms (1..2000) and
+ * records a device error, which the next cdm_synchronize on this context
+ * reports as CDM_TIMEOUT and clears; the context stays usable. Every wait in
+ * the fitting kernels takes the same path with a 2 s limit. */
+cdm_status cdm_selftest_wait_timeout(cdm_ctx* ctx, int limit_ms, void* stream);
+
 /* dMRI_Data::remove_NonPositive_entries (dMRI_Data.cu:15-30), applied by
  * CUDIMOT to every voxel when --rician is set (dMRI_Data.cu:133): in each
  * voxel of meas [nvox][nmeas] (device, in place) whose smallest value is
