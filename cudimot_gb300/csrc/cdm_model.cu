@@ -358,8 +358,8 @@ cdm_status run_mcmc(cdm_ctx* c, int nvox, int nmeas, const double* meas, double*
   if (c->cfg.sampleevery <= 0 || c->cfg.njumps < c->cfg.sampleevery)
     return cdm_fail(CDM_BAD_ARG,
                     "MCMC must record at least one sample: --nj must be >= --se (MCMC.cu:707-710)");
-  if (!samples) return cdm_fail(CDM_BAD_ARG, "samples is null");
-  if (c->cfg.rician && !tau) return cdm_fail(CDM_BAD_ARG, "rician MCMC needs tau_samples");
+  if (!samples && nvox > 0) return cdm_fail(CDM_BAD_ARG, "samples is null");
+  if (c->cfg.rician && !tau && nvox > 0) return cdm_fail(CDM_BAD_ARG, "rician MCMC needs tau_samples");
   CDM_TRY(prep_protocol(c, nmeas, CFP, st));
   // measured on NODDI-Watson, 200k voxels, 500 + 500 jumps: 2 lanes 420 ms,
   // 1 lane 443 ms, 4 lanes 469 ms: fewer lanes per voxel repeat the
@@ -810,10 +810,10 @@ cdm_status cdm_fit(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* 
                    const double* CFP, const double* FixP, double* samples, double* tau,
                    double* pred, double* BIC, double* AIC, void* stream) {
   CDM_TRY(check_common(c, nvox, nmeas, CDM_CFP_TSIZE, CDM_FIXP_TSIZE));
-  if (!samples) return cdm_fail(CDM_BAD_ARG, "samples is null");
+  if (!samples && nvox > 0) return cdm_fail(CDM_BAD_ARG, "samples is null");
   if (c->cfg.run_mcmc && (c->cfg.sampleevery <= 0 || c->cfg.njumps < c->cfg.sampleevery))
     return cdm_fail(CDM_BAD_ARG, "MCMC must record at least one sample: --nj must be >= --se");
-  if (c->cfg.run_mcmc && c->cfg.rician && !tau) return cdm_fail(CDM_BAD_ARG, "rician needs tau");
+  if (c->cfg.run_mcmc && c->cfg.rician && !tau && nvox > 0) return cdm_fail(CDM_BAD_ARG, "rician needs tau");
   cudaStream_t st = (cudaStream_t)stream;
   if (nvox == 0) return CDM_OK;
   CDM_TRY(reserve_fit(c, nvox, nmeas));
@@ -864,10 +864,10 @@ cdm_status cdm_fit_enqueue(cdm_ctx* c, int nvox, int nmeas, const double* meas, 
                            const double* CFP, const double* FixP, double* samples, double* tau,
                            double* pred, double* BIC, double* AIC, void* stream) {
   CDM_TRY(check_common(c, nvox, nmeas, CDM_CFP_TSIZE, CDM_FIXP_TSIZE));
-  if (!samples) return cdm_fail(CDM_BAD_ARG, "samples is null");
+  if (!samples && nvox > 0) return cdm_fail(CDM_BAD_ARG, "samples is null");
   if (c->cfg.run_mcmc && (c->cfg.sampleevery <= 0 || c->cfg.njumps < c->cfg.sampleevery))
     return cdm_fail(CDM_BAD_ARG, "MCMC must record at least one sample: --nj must be >= --se");
-  if (c->cfg.run_mcmc && c->cfg.rician && !tau) return cdm_fail(CDM_BAD_ARG, "rician needs tau");
+  if (c->cfg.run_mcmc && c->cfg.rician && !tau && nvox > 0) return cdm_fail(CDM_BAD_ARG, "rician needs tau");
   if (nvox == 0) return CDM_OK;
   cudaStream_t st = (cudaStream_t)stream;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;

@@ -149,7 +149,9 @@ cdm_status cdm_destroy(cdm_ctx* ctx);
 
 /* Stage calls; device pointers, asynchronous on `stream` (cudaStream_t,
  * 0 = legacy default stream). Argument meaning follows CUDIMOT's run():
- * CFP_size / FixP_size are the total sizes CFP_Tsize / FixP_Tsize. */
+ * CFP_size / FixP_size are the total sizes CFP_Tsize / FixP_Tsize.
+ * nvox = 0 is valid: the call returns CDM_OK and touches no per-voxel array,
+ * which may then be null (CFP must still hold nmeas rows). */
 /* GridSearch<T>::run, GridSearch.cu:291-317 */
 cdm_status cdm_gridsearch(cdm_ctx* ctx, int nvox, int nmeas, int CFP_size, int FixP_size,
                           const double* meas, double* params, const double* CFP,
