@@ -53,6 +53,8 @@ def parse():
                     default=None,
                     help="run the preceding stages, then one launch of this stage (for ncu); "
                          "mlp_forward: two inference passes of the network on --nvox voxels")
+    ap.add_argument("--rician", action="store_true",
+                    help="with --profile-stage mcmc: the Rician likelihood (tau sampled)")
     ap.add_argument("--nburn", type=int, default=NBURN)
     ap.add_argument("--njumps", type=int, default=NJUMPS)
     ap.add_argument("--workload", default="noddi_watson",
@@ -260,7 +262,7 @@ def profile_stage(a):
     a.nvox = a.nvox or 20000
     cfp, meas, fixp, init, _ = make_workload(a.nvox, 8219, dev)
     cfg = capi.model_cfg(MODEL, grid=synth.WATSON_GRID, run_mcmc=1, nburn=a.nburn,
-                         njumps=a.njumps, sampleevery=SE)
+                         njumps=a.njumps, sampleevery=SE, rician=int(a.rician))
     lib = capi.Cudimot(MODEL, cfg)
     t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
     m, c, f, p = t(meas), t(cfp), t(fixp), t(init)
@@ -276,11 +278,14 @@ def profile_stage(a):
     elif a.profile_stage == "levmar":
         lib.levmar(m, p, c, f)
     else:
-        s = torch.zeros(a.nvox, 5, max(a.njumps // SE, 1), dtype=torch.float64, device=dev)
-        lib.mcmc(m, p, c, f, s)
+        ns = max(a.njumps // SE, 1)
+        s = torch.zeros(a.nvox, 5, ns, dtype=torch.float64, device=dev)
+        tau = torch.zeros(a.nvox, ns, dtype=torch.float64, device=dev) if a.rician else None
+        lib.mcmc(m, p, c, f, s, tau=tau)
     e1.record()
     torch.cuda.synchronize()
-    print(json.dumps({"stage": a.profile_stage, "nvox": a.nvox, "ms": e0.elapsed_time(e1)}))
+    print(json.dumps({"stage": a.profile_stage, "rician": a.rician, "nvox": a.nvox,
+                      "ms": e0.elapsed_time(e1)}))
 
 
 def profiled_traffic():

@@ -287,6 +287,42 @@ __device__ __forceinline__ float cdm_log_i0_fast(float x) {
                     a * 0.00392377f)))))))) * rsqrtf(b));
 }
 
+#ifdef CDM_SIGNAL_PAIR
+// cdm_log_i0_fast on both halves of a pair without branches: the two
+// polynomial pieces are evaluated on the paired FP32 instructions (the same
+// Horner steps, so each half gets cdm_log_i0_fast's value) and the piece
+// that applies is selected per half. Lanes of a warp hold different voxels
+// and measurements, so the branchy form runs both pieces in most warps
+// anyway, one half at a time. The piece not selected may be inf or NaN
+// (|x| = 0 in the reciprocal and rsqrt); a select does not propagate it.
+__device__ __forceinline__ float2 cdm_log_i0_fast2(float2 x) {
+  const float2 b = make_float2(fabsf(x.x), fabsf(x.y));
+  float2 a = __fmul2_rn(x, make_float2(1.0f / 3.75f, 1.0f / 3.75f));
+  a = __fmul2_rn(a, a);
+  float2 ps = make_float2(0.0045813f, 0.0045813f);
+  ps = __ffma2_rn(a, ps, make_float2(0.0360768f, 0.0360768f));
+  ps = __ffma2_rn(a, ps, make_float2(0.2659732f, 0.2659732f));
+  ps = __ffma2_rn(a, ps, make_float2(1.2067492f, 1.2067492f));
+  ps = __ffma2_rn(a, ps, make_float2(3.0899424f, 3.0899424f));
+  ps = __ffma2_rn(a, ps, make_float2(3.5156229f, 3.5156229f));
+  ps = __ffma2_rn(a, ps, make_float2(1.0f, 1.0f));
+  const float2 al = make_float2(__fdividef(3.75f, b.x), __fdividef(3.75f, b.y));
+  float2 pl = make_float2(0.00392377f, 0.00392377f);
+  pl = __ffma2_rn(al, pl, make_float2(-0.01647633f, -0.01647633f));
+  pl = __ffma2_rn(al, pl, make_float2(0.02635537f, 0.02635537f));
+  pl = __ffma2_rn(al, pl, make_float2(-0.02057706f, -0.02057706f));
+  pl = __ffma2_rn(al, pl, make_float2(0.00916281f, 0.00916281f));
+  pl = __ffma2_rn(al, pl, make_float2(-0.00157565f, -0.00157565f));
+  pl = __ffma2_rn(al, pl, make_float2(0.00225319f, 0.00225319f));
+  pl = __ffma2_rn(al, pl, make_float2(0.01328592f, 0.01328592f));
+  pl = __ffma2_rn(al, pl, make_float2(0.39894228f, 0.39894228f));
+  pl = __fmul2_rn(pl, make_float2(rsqrtf(b.x), rsqrtf(b.y)));
+  const bool sx = b.x < 3.75f, sy = b.y < 3.75f;
+  const float lx = __logf(sx ? ps.x : pl.x), ly = __logf(sy ? ps.y : pl.y);
+  return make_float2(sx ? lx : b.x + lx, sy ? ly : b.y + ly);
+}
+#endif
+
 // Rician log-likelihood sum without the voxel-constant sum of log(y)
 // (which cancels in every Metropolis ratio): sum of
 // -tau/2 (y^2 + S^2) + log I0(tau S y).
@@ -304,6 +340,8 @@ __device__ __forceinline__ double cdm_group_rician(const cdm_voxel_io& io, const
     const float* sig = io.sig;
     float2 acc2 = make_float2(0.0f, 0.0f);
     const float2 nht = make_float2(-0.5f * tau, -0.5f * tau);
+    const float2 tau2 = make_float2(tau, tau);
+#pragma unroll kPairUnroll
     for (; c0 + 1 < full; c0 += 2) {
       float2 ab[kNCOLS];
       cdm_load_pairs(q, ab);
@@ -311,8 +349,7 @@ __device__ __forceinline__ double cdm_group_rician(const cdm_voxel_io& io, const
       const float2 y2 = make_float2(sig[0], sig[io.chunk_stride]);
       const float2 e = __ffma2_rn(y2, y2, __fmul2_rn(s2, s2));
       acc2 = __ffma2_rn(nht, e, acc2);
-      acc2.x += cdm_log_i0_fast(tau * s2.x * y2.x);
-      acc2.y += cdm_log_i0_fast(tau * s2.y * y2.y);
+      acc2 = __fadd2_rn(acc2, cdm_log_i0_fast2(__fmul2_rn(__fmul2_rn(tau2, s2), y2)));
       q += 2 * G * kNCOLSP;
       sig += 2 * io.chunk_stride;
     }
