@@ -20,8 +20,7 @@
 extern "C" {
 #endif
 
-typedef struct cdm_batch cdm_batch;
-typedef struct cdm_ctx cdm_ctx;
+typedef struct cdm_batch cdm_batch;  /* cdm_ctx comes from cudimot_gb300.h */
 
 /* cdm_fit_reserve / cdm_fit_enqueue of the item's model library */
 typedef cdm_status (*cdm_reserve_fn)(cdm_ctx*, int nvox, int nmeas);
