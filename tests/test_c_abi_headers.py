@@ -1,7 +1,8 @@
 """The public headers are a C ABI: each compiles on its own and all together
 as strict C99 and C11 (gcc -pedantic -Werror) and as C++17, and a plain C
 program links against a model library and calls its host-only entry points
-(what a cgo, JNI or N-API binding does first). No GPU is needed.
+(what a cgo, JNI or N-API binding does first); two threads that fail at
+the same time each read their own cdm_last_error. No GPU is needed.
 """
 import os
 import shutil
@@ -87,3 +88,62 @@ def test_c_program_links_and_calls(built, tmp_path):
     assert out["fixed"] == "01010"
     assert out["bad_create"] == "1" and out["msg"] == "1"
     assert out["status"]
+
+
+THREAD_PROGRAM = r"""
+#include <pthread.h>
+#include <stdio.h>
+#include <string.h>
+#include "cudimot_gb300.h"
+
+static pthread_barrier_t bar;
+static int ok[2];
+
+static void* create_bad(void* arg) {
+  cdm_model_cfg cfg;
+  cdm_ctx* ctx = NULL;
+  (void)arg;
+  cdm_default_cfg(&cfg);
+  cfg.nparams = 4;
+  int st = cdm_create(&cfg, &ctx);
+  pthread_barrier_wait(&bar);   /* both threads have failed */
+  ok[0] = st == CDM_BAD_ARG && strstr(cdm_last_error(), "nparams") != NULL &&
+          strstr(cdm_last_error(), "Wrong number") == NULL;
+  return NULL;
+}
+
+static void* parse_bad(void* arg) {
+  int fixed[CDM_MAX_PARAMS];
+  (void)arg;
+  int st = cdm_parse_fixed("9", fixed);
+  pthread_barrier_wait(&bar);
+  ok[1] = st == CDM_BAD_ARG && strstr(cdm_last_error(), "Wrong number of parameter 9") != NULL;
+  return NULL;
+}
+
+int main(void) {
+  pthread_t a, b;
+  pthread_barrier_init(&bar, NULL, 2);
+  pthread_create(&a, NULL, create_bad, NULL);
+  pthread_create(&b, NULL, parse_bad, NULL);
+  pthread_join(a, NULL);
+  pthread_join(b, NULL);
+  printf("%d %d\n", ok[0], ok[1]);
+  return ok[0] && ok[1] ? 0 : 1;
+}
+"""
+
+
+def test_last_error_is_per_thread(built, tmp_path):
+    """cdm_last_error reports the failure of the calling thread: two threads
+    fail differently at the same time and each reads its own message."""
+    src = tmp_path / "threads.c"
+    src.write_text(THREAD_PROGRAM)
+    libdir = os.path.dirname(capi.lib_path("NODDI_Watson"))
+    exe = tmp_path / "threads"
+    r = subprocess.run(["gcc", "-std=gnu99", "-Wall", "-Werror", "-pthread", "-I", INC, str(src),
+                        "-o", str(exe), "-L", libdir, "-lcudimot_NODDI_Watson",
+                        f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.stdout, r.stderr)
