@@ -498,9 +498,9 @@ def bench_learned(a, dev):
     wsamp = torch.zeros(w, 5, 1, dtype=torch.float64, device=dev)
     wl.mcmc(meas[:w], wp, li.cfp, s0[:w], wsamp)
     li.fit(meas[:w].contiguous(), s0[:w].contiguous(), wcfg, wsamp,
-           judge_cost=torch.zeros(w, dtype=torch.float64, device=dev), margin=0.0)
+           plain_cost=torch.zeros(w, dtype=torch.float64, device=dev), margin=0.0)
     torch.cuda.synchronize()
-    # grid-initialised path: GS -> LM | judge cost | MCMC
+    # grid-initialised path: GS -> LM | its cost (the refit yardstick) | MCMC
     with ClockSampler(dev.index or 0) as clk:
         p = init.clone()
         e = [ev() for _ in range(6)]
@@ -509,7 +509,7 @@ def bench_learned(a, dev):
         e[4].record(st)
         plain.levmar(meas, p, li.cfp, s0)
         e[1].record(st)
-        judge = li.cost(meas, p, s0)
+        plain_cost = li.cost(meas, p, s0)
         e[2].record(st)
         plain.mcmc(meas, p, li.cfp, s0, sp)
         e[3].record(st)
@@ -522,7 +522,7 @@ def bench_learned(a, dev):
         q = None
         f0, f1 = ev(), ev()
         f0.record(st)
-        q, info = li.fit(meas, s0, fit_cfg, ss, judge_cost=judge, margin=0.01, ctx=ctx)
+        q, info = li.fit(meas, s0, fit_cfg, ss, plain_cost=plain_cost, margin=0.01, ctx=ctx)
         f1.record(st)
         torch.cuda.synchronize()
         t_sur = f0.elapsed_time(f1)

@@ -14,7 +14,7 @@ Training data are made by the method itself, all on the GPU:
 The network is trained with Adam on the Gaussian NLL (cdm_mlp_train_step).
 
 `fit` runs the surrogate-initialised path. The plain grid-search path is
-its judge and fallback: voxels whose LM cost exceeds the plain fit's by
+its yardstick and fallback: voxels whose LM cost exceeds the plain fit's by
 more than `margin` are refit by grid search + LM before MCMC.
 """
 from __future__ import annotations
@@ -209,9 +209,9 @@ class LearnedInit:
                    m=f(cap, self.nmeas), s0=f(cap, 1), p=f(cap, npar), cap=cap)
         return lib, g, buf
 
-    def fit(self, meas, s0, fit_cfg, samples, judge_cost=None, margin=0.01, ctx=None):
+    def fit(self, meas, s0, fit_cfg, samples, plain_cost=None, margin=0.01, ctx=None):
         """Surrogate-initialised fit: network -> LM -> (refit by grid search +
-        LM where the LM cost exceeds judge_cost by more than margin) -> MCMC
+        LM where the LM cost exceeds plain_cost by more than margin) -> MCMC
         with network-seeded proposal widths. Returns (params, info)."""
         torch = self.torch
         n = meas.shape[0]
@@ -229,9 +229,9 @@ class LearnedInit:
         lib.levmar(meas, P, self.cfp, s0)
         mark()
         info = {"refit": 0}
-        if judge_cost is not None:
+        if plain_cost is not None:
             self.cost(meas, P, s0, out=buf["cost"])
-            lib.select_worse(buf["cost"], judge_cost, margin, buf["idx"], buf["count"])
+            lib.select_worse(buf["cost"], plain_cost, margin, buf["idx"], buf["count"])
             nbad = int(buf["count"].item())
             info["refit"] = nbad
             cap = buf["cap"]
