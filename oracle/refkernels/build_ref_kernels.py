@@ -2,7 +2,7 @@
 
     python oracle/refkernels/build_ref_kernels.py --reference /root/reference [--models ...]
 
-Here (where the CUDIMOT tree is): compiles GridSearch.cu,
+Where the CUDIMOT source tree is present: compiles GridSearch.cu,
 Levenberg_Marquardt.cu, MCMC.cu, BIC_AIC.cu and getPredictedSignal.cu of the
 CUDIMOT tree, unmodified, against a model's unmodified plugin, to sm_103a
 cubins in oracle/_ref/<Model>/ (flags of CUDIMOT's Makefile:13-22: -O3,
@@ -10,8 +10,9 @@ cubins in oracle/_ref/<Model>/ (flags of CUDIMOT's Makefile:13-22: -O3,
 tracer_plus.h are replaced by the stubs in oracle/refkernels/stubs (the
 host classes they serve are never run).
 
-On the GPU machine (no CUDIMOT tree): build_harness() compiles refharness.cpp
-(driver API) into oracle/_ref/librefharness.so, which loads those cubins.
+On a machine with the GPU but without the CUDIMOT tree, build_harness()
+compiles refharness.cpp (driver API) into oracle/_ref/librefharness.so,
+which loads those cubins.
 """
 import argparse
 import concurrent.futures as cf
