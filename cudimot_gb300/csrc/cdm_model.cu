@@ -907,7 +907,10 @@ cdm_status cdm_synchronize(cdm_ctx* c, void* stream, int64_t timeout_ms) {
   int err = 0;
   CDM_CUDA(cudaMemcpy(&err, c->err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) {
-    cudaMemset(c->err, 0, sizeof(int));
+    const cudaError_t ce = cudaMemset(c->err, 0, sizeof(int));
+    if (ce != cudaSuccess)
+      return cdm_fail(CDM_CUDA_ERROR, std::string("clearing the device error word: ") +
+                                          cudaGetErrorString(ce));
     return cdm_fail(CDM_TIMEOUT, "a bounded device wait ran out (code " + std::to_string(err) + ")");
   }
   return CDM_OK;
