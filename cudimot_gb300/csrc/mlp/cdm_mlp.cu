@@ -660,7 +660,7 @@ cdm_status cdm_mlp_check(cdm_mlp* m) {
   int e = 0;
   MLP_CUDA(cudaMemcpy(&e, m->err, sizeof(int), cudaMemcpyDeviceToHost));
   if (e) {
-    cudaMemset(m->err, 0, sizeof(int));
+    MLP_CUDA(cudaMemset(m->err, 0, sizeof(int)));
     return fail(CDM_TIMEOUT, "a bounded tensor-core pipeline wait ran out");
   }
   return CDM_OK;
