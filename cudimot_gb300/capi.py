@@ -230,6 +230,8 @@ def _declare(lib):
         "cdm_fit_enqueue": [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "cdm_synchronize": [_vp, _vp, i64],
         "cdm_get_stats": [_vp, C.POINTER(Stats)],
+        "cdm_levmar_noalloc": [C.POINTER(CfgStruct), i, i, i, i, _vp, _vp, _vp, _vp, _vp],
+        "cdm_noalloc_status": [_vp],
     }
     for name, args in sigs.items():
         f = getattr(lib, name)
@@ -248,7 +250,7 @@ EXPORTED = ("cdm_get_model_info", "cdm_default_cfg", "cdm_status_string", "cdm_l
             "cdm_fit_reserve", "cdm_fit_enqueue", "cdm_synchronize", "cdm_get_stats",
             "cdm_mcmc_seeded", "cdm_synth_signals", "cdm_mlp_head_info", "cdm_mlp_targets",
             "cdm_mlp_decode", "cdm_cost", "cdm_select_worse", "cdm_rows", "cdm_clean_signals",
-            "cdm_selftest_wait_timeout")
+            "cdm_selftest_wait_timeout", "cdm_levmar_noalloc", "cdm_noalloc_status")
 
 
 def lib_path(model: str) -> str:

@@ -4,7 +4,27 @@
 // Include order is CUDIMOT's (GridSearch.cu:7-11): math prelude, the
 // plugin's modelparameters.h, macro_numerical.h, the plugin's
 // modelfunctions.h; then this library's plugin tail and kernels.
+//
+// System and library headers come first: a plugin's object-like macros
+// (CUDIMOT's NODDI_Watson defines H, MPI, NMAX, A1-A3; its Legendre header
+// MN) stay in force for everything included after it, so only the kernels,
+// written with prefixed or multi-letter names, follow the plugin.
 #include <math_constants.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "cdm_host.h"
+#include "cudimot_gb300.h"
 
 #include "functions_gpu.h"
 #include "modelparameters.h"
@@ -19,20 +39,6 @@
 #include "cdm_mcmc.cuh"
 #include "cdm_postfit.cuh"
 #include "cdm_synth.cuh"
-
-#include "cdm_host.h"
-#include "cudimot_gb300.h"
-
-#include <cuda_runtime.h>
-
-#include <algorithm>
-#include <chrono>
-#include <cstdio>
-#include <cstring>
-#include <string>
-#include <mutex>
-#include <thread>
-#include <vector>
 
 #ifndef CDM_MODEL_NAME
 #define CDM_MODEL_NAME "model"
@@ -162,20 +168,20 @@ cdm_status prep_protocol(cdm_ctx* c, int nmeas, const double* CFP, cudaStream_t 
   return CDM_OK;
 }
 
-template <int G>
+template <int Gw>
 cdm_status pack_signals_g(cdm_ctx* c, int nvox, int nmeas, const double* meas, cudaStream_t st) {
-  const int nchunk = (nmeas + G - 1) / G;
-  CDM_TRY(dev_alloc(&c->sig, &c->sig_cap, (size_t)nchunk * std::max(nvox, 1) * G));
+  const int nchunk = (nmeas + Gw - 1) / Gw;
+  CDM_TRY(dev_alloc(&c->sig, &c->sig_cap, (size_t)nchunk * std::max(nvox, 1) * Gw));
   if (nvox == 0) return CDM_OK;
-  const size_t total = (size_t)nchunk * nvox * G;
+  const size_t total = (size_t)nchunk * nvox * Gw;
   const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)c->num_sms * 32);
-  cdm_pack_signals_kernel<G><<<blocks, 256, 0, st>>>(meas, nvox, nmeas, nchunk, c->sig);
+  cdm_pack_signals_kernel<Gw><<<blocks, 256, 0, st>>>(meas, nvox, nmeas, nchunk, c->sig);
   CDM_CUDA(cudaGetLastError());
   return CDM_OK;
 }
 
-cdm_status pack_signals(cdm_ctx* c, int G, int nvox, int nmeas, const double* meas, cudaStream_t st) {
-  switch (G) {
+cdm_status pack_signals(cdm_ctx* c, int Gw, int nvox, int nmeas, const double* meas, cudaStream_t st) {
+  switch (Gw) {
     case 1: return pack_signals_g<1>(c, nvox, nmeas, meas, st);
     case 2: return pack_signals_g<2>(c, nvox, nmeas, meas, st);
     case 4: return pack_signals_g<4>(c, nvox, nmeas, meas, st);
@@ -186,8 +192,8 @@ cdm_status pack_signals(cdm_ctx* c, int G, int nvox, int nmeas, const double* me
   return cdm_fail(CDM_BAD_ARG, "lanes per voxel must be 1, 2, 4, 8, 16 or 32");
 }
 
-template <class K>
-cdm_status set_smem(K kernel, size_t bytes) {
+template <class Kfn>
+cdm_status set_smem(Kfn kernel, size_t bytes) {
   if (bytes > 48 * 1024) CDM_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   return CDM_OK;
 }
@@ -209,11 +215,11 @@ int pick_lanes(const cdm_ctx* c, int requested, int base, int nvox) {
 }
 
 template <class Args>
-void fill_common(cdm_ctx* c, Args& a, int nvox, int nmeas, int G) {
+void fill_common(cdm_ctx* c, Args& a, int nvox, int nmeas, int Gw) {
   a.nvox = nvox;
   a.nmeas = nmeas;
   a.nmeas_pad = c->nmeas_pad;
-  a.nchunk = (nmeas + G - 1) / G;
+  a.nchunk = (nmeas + Gw - 1) / Gw;
   a.fixp_tsize = CDM_FIXP_TSIZE;
   a.proto_bytes = (uint32_t)proto_bytes(c->nmeas_pad);
   a.proto = c->proto32;
@@ -222,14 +228,14 @@ void fill_common(cdm_ctx* c, Args& a, int nvox, int nmeas, int G) {
   a.lim = c->lim;
 }
 
-int blocks_for(int nvox, int G) { return (nvox + (CDM_NT / G) - 1) / (CDM_NT / G); }
+int blocks_for(int nvox, int Gw) { return (nvox + (CDM_NT / Gw) - 1) / (CDM_NT / Gw); }
 
 // ------------------------------------------------------------------ stages
-template <int G>
+template <int Gw>
 cdm_status launch_gs(cdm_ctx* c, int nvox, int nmeas, double* params, const double* FixP,
                      cudaStream_t st) {
   cdm_gs_args a;
-  fill_common(c, a, nvox, nmeas, G);
+  fill_common(c, a, nvox, nmeas, Gw);
   a.params = params;
   a.fixp = FixP;
   a.grid = c->grid_dev;
@@ -241,8 +247,8 @@ cdm_status launch_gs(cdm_ctx* c, int nvox, int nmeas, double* params, const doub
   a.cand = c->gs_cand;
   a.best = c->gs_best;
   const size_t sm = fit_smem(c->nmeas_pad);
-  CDM_TRY(set_smem(cdm_gridsearch_kernel<G>, sm));
-  cdm_gridsearch_kernel<G><<<blocks_for(nvox, G), CDM_NT, sm, st>>>(a);
+  CDM_TRY(set_smem(cdm_gridsearch_kernel<Gw>, sm));
+  cdm_gridsearch_kernel<Gw><<<blocks_for(nvox, Gw), CDM_NT, sm, st>>>(a);
   CDM_CUDA(cudaGetLastError());
   return CDM_OK;
 }
@@ -254,14 +260,14 @@ cdm_status run_gridsearch(cdm_ctx* c, int nvox, int nmeas, const double* meas, d
   // narrowest groups first: measured on NODDI-Watson, 200k voxels x 288
   // measurements, 968 combinations: 2 lanes 91 ms, 4 lanes 100 ms, 8 lanes
   // 150 ms (1 lane 164 ms)
-  const int G = pick_lanes(c, c->cfg.lanes_gridsearch, 2, nvox);
-  CDM_TRY(pack_signals(c, G, nvox, nmeas, meas, st));
+  const int Gw = pick_lanes(c, c->cfg.lanes_gridsearch, 2, nvox);
+  CDM_TRY(pack_signals(c, Gw, nvox, nmeas, meas, st));
   const size_t n = (size_t)std::max(nvox, 1);
   CDM_TRY(dev_alloc(&c->gs_flags, &c->gs_flags_cap, n));
   CDM_TRY(dev_alloc(&c->gs_cand, &c->gs_cand_cap, n * kGsTop));
   CDM_TRY(dev_alloc(&c->gs_best, &c->gs_best_cap, n));
   if (nvox == 0) return CDM_OK;
-  switch (G) {
+  switch (Gw) {
     case 1: CDM_TRY(launch_gs<1>(c, nvox, nmeas, params, FixP, st)); break;
     case 2: CDM_TRY(launch_gs<2>(c, nvox, nmeas, params, FixP, st)); break;
     case 4: CDM_TRY(launch_gs<4>(c, nvox, nmeas, params, FixP, st)); break;
@@ -292,11 +298,11 @@ cdm_status run_gridsearch(cdm_ctx* c, int nvox, int nmeas, const double* meas, d
   return CDM_OK;
 }
 
-template <int G>
+template <int Gw>
 cdm_status launch_lm(cdm_ctx* c, int nvox, int nmeas, double* params, const double* FixP,
                      cudaStream_t st) {
   cdm_lm_args a;
-  fill_common(c, a, nvox, nmeas, G);
+  fill_common(c, a, nvox, nmeas, Gw);
   a.params = params;
   a.fixp = FixP;
   a.max_iters = c->cfg.iter_levmar;
@@ -304,8 +310,8 @@ cdm_status launch_lm(cdm_ctx* c, int nvox, int nmeas, double* params, const doub
   a.iter_count = c->counters + 0;
   a.succ_count = c->counters + 1;
   const size_t sm = fit_smem(c->nmeas_pad);
-  CDM_TRY(set_smem(cdm_levmar_kernel<G>, sm));
-  cdm_levmar_kernel<G><<<blocks_for(nvox, G), CDM_NT, sm, st>>>(a);
+  CDM_TRY(set_smem(cdm_levmar_kernel<Gw>, sm));
+  cdm_levmar_kernel<Gw><<<blocks_for(nvox, Gw), CDM_NT, sm, st>>>(a);
   CDM_CUDA(cudaGetLastError());
   return CDM_OK;
 }
@@ -313,10 +319,10 @@ cdm_status launch_lm(cdm_ctx* c, int nvox, int nmeas, double* params, const doub
 cdm_status run_levmar(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
                       const double* CFP, const double* FixP, cudaStream_t st) {
   CDM_TRY(prep_protocol(c, nmeas, CFP, st));
-  const int G = pick_lanes(c, c->cfg.lanes_levmar, 4, nvox);
-  CDM_TRY(pack_signals(c, G, nvox, nmeas, meas, st));
+  const int Gw = pick_lanes(c, c->cfg.lanes_levmar, 4, nvox);
+  CDM_TRY(pack_signals(c, Gw, nvox, nmeas, meas, st));
   if (nvox == 0) return CDM_OK;
-  switch (G) {
+  switch (Gw) {
     case 1: return launch_lm<1>(c, nvox, nmeas, params, FixP, st);
     case 2: return launch_lm<2>(c, nvox, nmeas, params, FixP, st);
     case 4: return launch_lm<4>(c, nvox, nmeas, params, FixP, st);
@@ -327,11 +333,11 @@ cdm_status run_levmar(cdm_ctx* c, int nvox, int nmeas, const double* meas, doubl
   }
 }
 
-template <int G, bool RICIAN>
+template <int Gw, bool RICIAN>
 cdm_status launch_mcmc(cdm_ctx* c, int nvox, int nmeas, double* params, const double* FixP,
                        double* samples, double* tau, uint32_t voxel_offset, cudaStream_t st) {
   cdm_mcmc_args a;
-  fill_common(c, a, nvox, nmeas, G);
+  fill_common(c, a, nvox, nmeas, Gw);
   a.params = params;
   a.fixp = FixP;
   a.samples = samples;
@@ -346,8 +352,8 @@ cdm_status launch_mcmc(cdm_ctx* c, int nvox, int nmeas, double* params, const do
   a.voxel_offset = voxel_offset;
   a.prop_sd = c->prop_sd;
   const size_t sm = fit_smem(c->nmeas_pad);
-  CDM_TRY(set_smem(cdm_mcmc_kernel<G, RICIAN>, sm));
-  cdm_mcmc_kernel<G, RICIAN><<<blocks_for(nvox, G), CDM_NT, sm, st>>>(a);
+  CDM_TRY(set_smem(cdm_mcmc_kernel<Gw, RICIAN>, sm));
+  cdm_mcmc_kernel<Gw, RICIAN><<<blocks_for(nvox, Gw), CDM_NT, sm, st>>>(a);
   CDM_CUDA(cudaGetLastError());
   return CDM_OK;
 }
@@ -364,15 +370,15 @@ cdm_status run_mcmc(cdm_ctx* c, int nvox, int nmeas, const double* meas, double*
   // measured on NODDI-Watson, 200k voxels, 500 + 500 jumps: 2 lanes 420 ms,
   // 1 lane 443 ms, 4 lanes 469 ms: fewer lanes per voxel repeat the
   // per-proposal work in fewer threads
-  const int G = pick_lanes(c, c->cfg.lanes_mcmc, 2, nvox);
-  CDM_TRY(pack_signals(c, G, nvox, nmeas, meas, st));
+  const int Gw = pick_lanes(c, c->cfg.lanes_mcmc, 2, nvox);
+  CDM_TRY(pack_signals(c, Gw, nvox, nmeas, meas, st));
   if (nvox == 0) return CDM_OK;
   const bool ric = c->cfg.rician != 0;
-#define CDM_MCMC_CASE(GG)                                                                     \
-  case GG:                                                                                    \
-    return ric ? launch_mcmc<GG, true>(c, nvox, nmeas, params, FixP, samples, tau, voxel_offset, st) \
-               : launch_mcmc<GG, false>(c, nvox, nmeas, params, FixP, samples, tau, voxel_offset, st);
-  switch (G) {
+#define CDM_MCMC_CASE(Gw2)                                                                     \
+  case Gw2:                                                                                    \
+    return ric ? launch_mcmc<Gw2, true>(c, nvox, nmeas, params, FixP, samples, tau, voxel_offset, st) \
+               : launch_mcmc<Gw2, false>(c, nvox, nmeas, params, FixP, samples, tau, voxel_offset, st);
+  switch (Gw) {
     CDM_MCMC_CASE(1)
     CDM_MCMC_CASE(2)
     CDM_MCMC_CASE(4)
@@ -452,7 +458,7 @@ cdm_status reserve_fit(cdm_ctx* c, int nvox, int nmeas) {
   CDM_TRY(dev_alloc(&c->proto32, &c->proto32_cap, (size_t)kNCOLS4 * pad));
   CDM_TRY(dev_alloc(&c->proto64, &c->proto64_cap, (size_t)kNCOLS * nmeas));
   size_t sig = 0;
-  for (int G : {1, 2, 4, 8, 16, 32}) sig = std::max(sig, (size_t)((nmeas + G - 1) / G) * std::max(nvox, 1) * G);
+  for (int Gw : {1, 2, 4, 8, 16, 32}) sig = std::max(sig, (size_t)((nmeas + Gw - 1) / Gw) * std::max(nvox, 1) * Gw);
   CDM_TRY(dev_alloc(&c->sig, &c->sig_cap, sig));
   const size_t n = (size_t)std::max(nvox, 1);
   CDM_TRY(dev_alloc(&c->gs_flags, &c->gs_flags_cap, n));
@@ -510,6 +516,10 @@ __global__ void cdm_wait_selftest_kernel(uint64_t limit_ns, int* err) {
 }
 
 }  // namespace
+
+// cdm_selftest_wait_timeout without a context: the no-allocation error word
+// (defined with that word, at the end of this file).
+static cdm_status noalloc_selftest(int limit_ms, cudaStream_t st);
 
 // =================================================================== C ABI
 extern "C" {
@@ -876,8 +886,8 @@ cdm_status cdm_fit_enqueue(cdm_ctx* c, int nvox, int nmeas, const double* meas, 
     // no allocation may happen under capture: the shape must be reserved
     const int pad = round_up(nmeas, 32);
     size_t sig = 0;
-    for (int G : {1, 2, 4, 8, 16, 32})
-      sig = std::max(sig, (size_t)((nmeas + G - 1) / G) * std::max(nvox, 1) * G);
+    for (int Gw : {1, 2, 4, 8, 16, 32})
+      sig = std::max(sig, (size_t)((nmeas + Gw - 1) / Gw) * std::max(nvox, 1) * Gw);
     if (c->proto32_cap < (size_t)kNCOLS4 * pad || c->sig_cap < sig ||
         c->gs_flags_cap < (size_t)std::max(nvox, 1))
       return cdm_fail(CDM_BAD_ARG, "cdm_fit_enqueue under stream capture needs cdm_fit_reserve "
@@ -930,8 +940,8 @@ cdm_status cdm_get_stats(cdm_ctx* c, cdm_stats* s) {
 }
 
 cdm_status cdm_selftest_wait_timeout(cdm_ctx* c, int limit_ms, void* stream) {
-  if (!c) return cdm_fail(CDM_BAD_ARG, "null context");
   if (limit_ms < 1 || limit_ms > 2000) return cdm_fail(CDM_BAD_ARG, "limit_ms must be in 1..2000");
+  if (!c) return noalloc_selftest(limit_ms, (cudaStream_t)stream);
   CDM_TRY(ensure_base(c));
   cdm_wait_selftest_kernel<<<1, 32, 0, (cudaStream_t)stream>>>((uint64_t)limit_ms * 1000000ull, c->err);
   CDM_CUDA(cudaGetLastError());
@@ -957,44 +967,44 @@ cdm_status cdm_fit_host(cdm_ctx* c, int nvox, int nmeas, const double* meas, dou
   (void)part_size;  // CUDIMOT's SIZE_PART parts (dMRI_Data.cu:66-79): one part here
   const cdm_model_cfg& o = c->cfg;
   const int ns = o.run_mcmc ? o.njumps / std::max(o.sampleevery, 1) : 1;
-  const size_t V = (size_t)nvox;
-  CDM_TRY(dev_alloc(&c->h_meas, &c->h_meas_cap, V * nmeas));
-  CDM_TRY(dev_alloc(&c->h_params, &c->h_params_cap, V * kNP));
+  const size_t nv = (size_t)nvox;
+  CDM_TRY(dev_alloc(&c->h_meas, &c->h_meas_cap, nv * nmeas));
+  CDM_TRY(dev_alloc(&c->h_params, &c->h_params_cap, nv * kNP));
   CDM_TRY(dev_alloc(&c->h_cfp, &c->h_cfp_cap, (size_t)nmeas * CDM_CFP_TSIZE));
-  CDM_TRY(dev_alloc(&c->h_fixp, &c->h_fixp_cap, std::max<size_t>(1, V * CDM_FIXP_TSIZE)));
-  CDM_TRY(dev_alloc(&c->h_samples, &c->h_samples_cap, V * kNP * ns));
+  CDM_TRY(dev_alloc(&c->h_fixp, &c->h_fixp_cap, std::max<size_t>(1, nv * CDM_FIXP_TSIZE)));
+  CDM_TRY(dev_alloc(&c->h_samples, &c->h_samples_cap, nv * kNP * ns));
   const bool want_tau = o.run_mcmc && o.rician && tau;
   const bool want_pred = o.get_predicted && pred;
   const bool want_bic = o.bic_aic && BIC && AIC;
-  if (want_tau) CDM_TRY(dev_alloc(&c->h_tau, &c->h_tau_cap, V * ns));
-  if (want_pred) CDM_TRY(dev_alloc(&c->h_pred, &c->h_pred_cap, V * nmeas));
+  if (want_tau) CDM_TRY(dev_alloc(&c->h_tau, &c->h_tau_cap, nv * ns));
+  if (want_pred) CDM_TRY(dev_alloc(&c->h_pred, &c->h_pred_cap, nv * nmeas));
   if (want_bic) {
-    CDM_TRY(dev_alloc(&c->h_bic, &c->h_bic_cap, V));
-    CDM_TRY(dev_alloc(&c->h_aic, &c->h_aic_cap, V));
+    CDM_TRY(dev_alloc(&c->h_bic, &c->h_bic_cap, nv));
+    CDM_TRY(dev_alloc(&c->h_aic, &c->h_aic_cap, nv));
   }
   if (!c->own_stream) CDM_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
   cudaStream_t st = c->own_stream;
-  CDM_CUDA(cudaMemcpyAsync(c->h_meas, meas, V * nmeas * sizeof(double), cudaMemcpyHostToDevice, st));
-  CDM_CUDA(cudaMemcpyAsync(c->h_params, params, V * kNP * sizeof(double), cudaMemcpyHostToDevice, st));
+  CDM_CUDA(cudaMemcpyAsync(c->h_meas, meas, nv * nmeas * sizeof(double), cudaMemcpyHostToDevice, st));
+  CDM_CUDA(cudaMemcpyAsync(c->h_params, params, nv * kNP * sizeof(double), cudaMemcpyHostToDevice, st));
   CDM_CUDA(cudaMemcpyAsync(c->h_cfp, CFP, (size_t)nmeas * CDM_CFP_TSIZE * sizeof(double),
                            cudaMemcpyHostToDevice, st));
   if (CDM_FIXP_TSIZE > 0)
-    CDM_CUDA(cudaMemcpyAsync(c->h_fixp, FixP, V * CDM_FIXP_TSIZE * sizeof(double),
+    CDM_CUDA(cudaMemcpyAsync(c->h_fixp, FixP, nv * CDM_FIXP_TSIZE * sizeof(double),
                              cudaMemcpyHostToDevice, st));
   if (o.rician) CDM_TRY(cdm_clean_signals(nvox, nmeas, c->h_meas, st));  // dMRI_Data.cu:133
   CDM_TRY(cdm_fit(c, nvox, nmeas, c->h_meas, c->h_params, c->h_cfp, c->h_fixp, c->h_samples,
                   want_tau ? c->h_tau : nullptr, want_pred ? c->h_pred : nullptr,
                   want_bic ? c->h_bic : nullptr, want_bic ? c->h_aic : nullptr, st));
-  CDM_CUDA(cudaMemcpyAsync(params, c->h_params, V * kNP * sizeof(double), cudaMemcpyDeviceToHost, st));
-  CDM_CUDA(cudaMemcpyAsync(samples, c->h_samples, V * kNP * ns * sizeof(double),
+  CDM_CUDA(cudaMemcpyAsync(params, c->h_params, nv * kNP * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CDM_CUDA(cudaMemcpyAsync(samples, c->h_samples, nv * kNP * ns * sizeof(double),
                            cudaMemcpyDeviceToHost, st));
   if (want_tau)
-    CDM_CUDA(cudaMemcpyAsync(tau, c->h_tau, V * ns * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CDM_CUDA(cudaMemcpyAsync(tau, c->h_tau, nv * ns * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (want_pred)
-    CDM_CUDA(cudaMemcpyAsync(pred, c->h_pred, V * nmeas * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CDM_CUDA(cudaMemcpyAsync(pred, c->h_pred, nv * nmeas * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (want_bic) {
-    CDM_CUDA(cudaMemcpyAsync(BIC, c->h_bic, V * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CDM_CUDA(cudaMemcpyAsync(AIC, c->h_aic, V * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CDM_CUDA(cudaMemcpyAsync(BIC, c->h_bic, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CDM_CUDA(cudaMemcpyAsync(AIC, c->h_aic, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
   }
   return cdm_synchronize(c, st, timeout_ms);
 }
@@ -1027,7 +1037,10 @@ std::mutex g_noalloc_mutex;
 
 // Device address of the scratch array for the current device. The first
 // call on a device resolves it with cudaGetSymbolAddress while that device
-// is current; later calls reuse the cached address.
+// is current and clears the error word (a synchronous cudaMemset, which
+// allocates nothing); later calls reuse the cached address. After that the
+// error word is cleared only by cdm_noalloc_status, so a wait that ran out
+// in any call stays visible until the caller asks.
 cdm_status noalloc_scratch(unsigned char** out) {
   int dev = 0;
   CDM_CUDA(cudaGetDevice(&dev));
@@ -1037,20 +1050,21 @@ cdm_status noalloc_scratch(unsigned char** out) {
   if (!g_noalloc_ptr[dev]) {
     void* p = nullptr;
     CDM_CUDA(cudaGetSymbolAddress(&p, cdm_noalloc_scratch));
+    CDM_CUDA(cudaMemset(p, 0, kNoAllocHeader));
     g_noalloc_ptr[dev] = (unsigned char*)p;
   }
   *out = g_noalloc_ptr[dev];
   return CDM_OK;
 }
 
-template <int G>
-cdm_status noalloc_lm_launch(const cdm_model_cfg* cfg, unsigned char* scratch, int nvox, int nmeas,
-                             const double* meas, double* params, const double* CFP,
+template <int Gw>
+cdm_status noalloc_lm_launch(const cdm_model_cfg* cfg, unsigned char* scratch, int sms, int nvox,
+                             int nmeas, const double* meas, double* params, const double* CFP,
                              const double* FixP, cudaStream_t st) {
   const int pad = round_up(nmeas, 32);
-  const int nchunk = (nmeas + G - 1) / G;
+  const int nchunk = (nmeas + Gw - 1) / Gw;
   const size_t pbytes = proto_bytes(pad);
-  const size_t sbytes = (size_t)nchunk * nvox * G * sizeof(float);
+  const size_t sbytes = (size_t)nchunk * nvox * Gw * sizeof(float);
   const size_t soff = kNoAllocHeader + (pbytes + 255) / 256 * 256;
   if (soff + sbytes > kNoAllocScratchBytes)
     return cdm_fail(CDM_BAD_ARG,
@@ -1061,17 +1075,14 @@ cdm_status noalloc_lm_launch(const cdm_model_cfg* cfg, unsigned char* scratch, i
   int* err = (int*)scratch;
   float* proto = (float*)(scratch + kNoAllocHeader);
   float* sig = (float*)(scratch + soff);
-  // The error word accumulates with atomicOr and must start at zero; the
-  // protocol table and the signals are fully rewritten by every call.
-  CDM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+  // The error word accumulates with atomicOr across calls (cleared at
+  // set-up and by cdm_noalloc_status); the protocol table and the signals
+  // are fully rewritten by every call.
   cdm_prep_protocol_kernel<<<(pad + 127) / 128, 128, 0, st>>>(CFP, nmeas, pad, proto, nullptr);
   CDM_CUDA(cudaGetLastError());
   if (nvox == 0) return CDM_OK;
-  int dev = 0, sms = 0;
-  CDM_CUDA(cudaGetDevice(&dev));
-  CDM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const size_t total = (size_t)nchunk * nvox * G;
-  cdm_pack_signals_kernel<G><<<(int)std::min<size_t>((total + 255) / 256, (size_t)std::max(sms, 1) * 32),
+  const size_t total = (size_t)nchunk * nvox * Gw;
+  cdm_pack_signals_kernel<Gw><<<(int)std::min<size_t>((total + 255) / 256, (size_t)std::max(sms, 1) * 32),
                                256, 0, st>>>(meas, nvox, nmeas, nchunk, sig);
   CDM_CUDA(cudaGetLastError());
   cdm_lm_args a;
@@ -1099,8 +1110,8 @@ cdm_status noalloc_lm_launch(const cdm_model_cfg* cfg, unsigned char* scratch, i
     a.lim.pb[p] = (float)cfg->priors_b[p];
     a.lim.fixed[p] = cfg->fixed[p];
   }
-  CDM_TRY(set_smem(cdm_levmar_kernel<G>, fit_smem(pad)));
-  cdm_levmar_kernel<G><<<blocks_for(nvox, G), CDM_NT, fit_smem(pad), st>>>(a);
+  CDM_TRY(set_smem(cdm_levmar_kernel<Gw>, fit_smem(pad)));
+  cdm_levmar_kernel<Gw><<<blocks_for(nvox, Gw), CDM_NT, fit_smem(pad), st>>>(a);
   CDM_CUDA(cudaGetLastError());
   return CDM_OK;
 }
@@ -1117,20 +1128,56 @@ extern "C" cdm_status cdm_levmar_noalloc(const cdm_model_cfg* cfg, int nvox, int
   if (nvox < 0 || nmeas <= 0) return cdm_fail(CDM_BAD_ARG, "nvox must be >= 0 and nmeas > 0");
   if (CFP_size != CDM_CFP_TSIZE || FixP_size != CDM_FIXP_TSIZE)
     return cdm_fail(CDM_BAD_ARG, "CFP_size/FixP_size do not match the model");
-  if (proto_bytes(round_up(nmeas, 32)) > 48 * 1024)
-    return cdm_fail(CDM_BAD_ARG, "cdm_levmar_noalloc: protocol larger than 48 KB of shared memory");
+  // the shared-memory bound of every other entry point (check_common)
+  if (fit_smem(round_up(nmeas, 32)) > 200 * 1024)
+    return cdm_fail(CDM_BAD_ARG, "protocol too large for shared memory staging");
   unsigned char* scratch = nullptr;
   CDM_TRY(noalloc_scratch(&scratch));
-  int G = cfg->lanes_levmar;
-  if (G == 0) G = 8;
+  int dev = 0, sms = 0;
+  CDM_CUDA(cudaGetDevice(&dev));
+  CDM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  // lanes per voxel: cdm_levmar's rule (pick_lanes), on this device's SM count
+  int Gw = cfg->lanes_levmar;
+  if (Gw == 0) {
+    const long resident = (long)std::max(sms, 1) * 512;
+    Gw = 4;
+    while (Gw < 32 && (long)nvox * Gw < 4 * resident) Gw *= 2;
+  }
   cudaStream_t st = (cudaStream_t)stream;
-  switch (G) {
-    case 1: return noalloc_lm_launch<1>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
-    case 2: return noalloc_lm_launch<2>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
-    case 4: return noalloc_lm_launch<4>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
-    case 8: return noalloc_lm_launch<8>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
-    case 16: return noalloc_lm_launch<16>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
-    case 32: return noalloc_lm_launch<32>(cfg, scratch, nvox, nmeas, meas, params, CFP, FixP, st);
+  switch (Gw) {
+    case 1: return noalloc_lm_launch<1>(cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP, st);
+    case 2: return noalloc_lm_launch<2>(cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP, st);
+    case 4: return noalloc_lm_launch<4>(cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP, st);
+    case 8: return noalloc_lm_launch<8>(cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP, st);
+    case 16: return noalloc_lm_launch<16>(cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP, st);
+    case 32: return noalloc_lm_launch<32>(cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP, st);
   }
   return cdm_fail(CDM_BAD_ARG, "lanes_levmar must be 0, 1, 2, 4, 8, 16 or 32");
+}
+
+// Reads and clears the no-allocation error word of the current device after
+// the caller's stream has finished: CDM_TIMEOUT if a bounded wait of any
+// cdm_levmar_noalloc call (or of cdm_selftest_wait_timeout with no context)
+// ran out since the last check. Waiting, the 4-byte read and the clear
+// allocate nothing.
+extern "C" cdm_status cdm_noalloc_status(void* stream) {
+  unsigned char* scratch = nullptr;
+  CDM_TRY(noalloc_scratch(&scratch));
+  CDM_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+  int err = 0;
+  CDM_CUDA(cudaMemcpy(&err, scratch, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!err) return CDM_OK;
+  CDM_CUDA(cudaMemset(scratch, 0, sizeof(int)));
+  return cdm_fail(CDM_TIMEOUT, "a bounded device wait of a no-allocation call ran out (code " +
+                                   std::to_string(err) + ")");
+}
+
+// cdm_selftest_wait_timeout with a null context records into the
+// no-allocation error word.
+static cdm_status noalloc_selftest(int limit_ms, cudaStream_t st) {
+  unsigned char* scratch = nullptr;
+  CDM_TRY(noalloc_scratch(&scratch));
+  cdm_wait_selftest_kernel<<<1, 32, 0, st>>>((uint64_t)limit_ms * 1000000ull, (int*)scratch);
+  CDM_CUDA(cudaGetLastError());
+  return CDM_OK;
 }

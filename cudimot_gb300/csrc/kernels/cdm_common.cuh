@@ -5,22 +5,22 @@
 // cdm_model_sizes.h, which the build generates from modelparameters.cc
 // (CDM_CFP_TSIZE, CDM_FIXP_TSIZE).
 //
-// Work decomposition: a voxel is processed by a group of G consecutive lanes
-// of one warp (G in {1, 2, 4, 8, 16, 32}); lane j of the group takes measurements
-// j, j+G, j+2G, ... Group sums are butterfly (xor) shuffles, which leave the
+// Work decomposition: a voxel is processed by a group of Gw consecutive lanes
+// of one warp (Gw in {1, 2, 4, 8, 16, 32}); lane j of the group takes measurements
+// j, j+Gw, j+2G, ... Group sums are butterfly (xor) shuffles, which leave the
 // identical value in every lane, so every lane of a group takes the same
-// decisions without a broadcast. Several groups share a warp when G < 32.
+// decisions without a broadcast. Several groups share a warp when Gw < 32.
 //
 // HBM layouts the kernels read (built by cdm_pack_* kernels):
 //   protocol  float [nmeas_pad][NCOLS4]  NCOLS = CFP_Tsize + derived CFP,
 //                                        rows padded to NCOLS4 (16 bytes)
-//   signals   float [nchunk][nvox][G]    chunk c holds measurements cG..cG+G-1
+//   signals   float [nchunk][nvox][Gw]    chunk c holds measurements cG..cG+Gw-1
 // so a warp's signal load is one contiguous 128-byte line.
 // With the paired signal hook (Predicted_Signal_Pair) the kernels that take
 // the paired cost loop also keep, after the staged protocol in shared
-// memory, a pair table float2 [nchunk/2][G][NCOLSP] (NCOLS rounded up to
+// memory, a pair table float2 [nchunk/2][Gw][NCOLSP] (NCOLS rounded up to
 // even, the pad column zero): entry (j, l, k) holds column k of
-// measurements 2jG+l and (2j+1)G+l, the two a lane evaluates together, so a
+// measurements 2jG+l and (2j+1)Gw+l, the two a lane evaluates together, so a
 // 16-byte load gives two columns already paired.
 #pragma once
 
@@ -66,18 +66,18 @@ struct cdm_limits {
   int fixed[kNP];
 };
 
-template <int G>
+template <int Gw>
 __device__ __forceinline__ unsigned cdm_group_mask() {
-  if (G == 32) return 0xFFFFFFFFu;
-  if (G == 1) return 1u << (threadIdx.x & 31u);
+  if (Gw == 32) return 0xFFFFFFFFu;
+  if (Gw == 1) return 1u << (threadIdx.x & 31u);
   const unsigned lane = threadIdx.x & 31u;
-  return ((1u << G) - 1u) << (lane & ~(unsigned)(G - 1));
+  return ((1u << Gw) - 1u) << (lane & ~(unsigned)(Gw - 1));
 }
 
-template <int G, class V>
-__device__ __forceinline__ V cdm_group_sum(V v, unsigned mask) {
+template <int Gw, class Tv>
+__device__ __forceinline__ Tv cdm_group_sum(Tv v, unsigned mask) {
 #pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+  for (int o = Gw / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
   return v;
 }
 
@@ -136,7 +136,7 @@ __device__ __forceinline__ bool cdm_stage_protocol(const float* __restrict__ gsr
 
 // Load one measurement's protocol values (raw CFP then derived) from the
 // staged table into a register array the plugin can index: one 16-byte
-// shared-memory load per four values. The G lanes of a group read G
+// shared-memory load per four values. The Gw lanes of a group read Gw
 // consecutive rows (distinct banks for 48-byte rows); other groups of the
 // warp read the same rows (broadcast).
 __device__ __forceinline__ void cdm_load_cfp(const float* sproto, int nmeas_pad, int m, fp32* cf) {
@@ -165,16 +165,16 @@ struct cdm_voxel_io {
 // Build the pair table (see the layout notes above) after the staged
 // protocol, with every thread of the CTA; returns its start. Call before
 // any thread leaves the kernel.
-template <int G>
+template <int Gw>
 __device__ __forceinline__ const float* cdm_build_pair_table(float* sproto, int nmeas_pad,
                                                              int nchunk) {
   float2* ptab = reinterpret_cast<float2*>(sproto + (size_t)nmeas_pad * kNCOLS4);
 #ifdef CDM_SIGNAL_PAIR
-  const int total = (nchunk / 2) * G * kNCOLSP;
+  const int total = (nchunk / 2) * Gw * kNCOLSP;
   for (int i = (int)threadIdx.x; i < total; i += (int)blockDim.x) {
-    const int k = i % kNCOLSP, l = (i / kNCOLSP) % G, j = i / (kNCOLSP * G);
-    ptab[i] = k < kNCOLS ? make_float2(sproto[(size_t)(2 * j * G + l) * kNCOLS4 + k],
-                                       sproto[(size_t)((2 * j + 1) * G + l) * kNCOLS4 + k])
+    const int k = i % kNCOLSP, l = (i / kNCOLSP) % Gw, j = i / (kNCOLSP * Gw);
+    ptab[i] = k < kNCOLS ? make_float2(sproto[(size_t)(2 * j * Gw + l) * kNCOLS4 + k],
+                                       sproto[(size_t)((2 * j + 1) * Gw + l) * kNCOLS4 + k])
                          : make_float2(0.0f, 0.0f);
   }
   __syncthreads();
@@ -198,11 +198,11 @@ __device__ __forceinline__ void cdm_load_pairs(const float* q, float2* ab) {
 // own measurements in FP32, the group total is formed in FP64. The loop walks
 // a protocol-row pointer and a signal pointer; chunks where every lane has a
 // measurement need no bounds test, only the last chunk may be partial.
-template <int G>
+template <int Gw>
 __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const float* sproto,
                                                 fp32* P, fp32* FixP, unsigned gmask) {
   float acc = 0.0f;
-  const int full = io.nmeas / G;
+  const int full = io.nmeas / Gw;
   const float* row = sproto + (size_t)io.lane * kNCOLS4;
   const float* sig = io.sig;
 #ifdef CDM_SIGNAL_PAIR
@@ -219,17 +219,17 @@ __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const fl
     const float2 s2 = Predicted_Signal_Pair(P, ab, FixP);
     const float2 r = __fadd2_rn(s2, make_float2(-sig[0], -sig[io.chunk_stride]));
     acc2 = __ffma2_rn(r, r, acc2);
-    q += 2 * G * kNCOLSP;
+    q += 2 * Gw * kNCOLSP;
     sig += 2 * io.chunk_stride;
   }
   acc = acc2.x + acc2.y;
-  row += (size_t)c * G * kNCOLS4;
+  row += (size_t)c * Gw * kNCOLS4;
   if (c < full) {
     fp32 cf[kNCOLS];
     cdm_load_cfp(row, 0, 0, cf);
     const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - *sig;
     acc = fmaf(r, r, acc);
-    row += G * kNCOLS4;
+    row += Gw * kNCOLS4;
     sig += io.chunk_stride;
   }
 #else
@@ -239,18 +239,18 @@ __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const fl
     cdm_load_cfp(row, 0, 0, cf);
     const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - *sig;
     acc = fmaf(r, r, acc);
-    row += G * kNCOLS4;
+    row += Gw * kNCOLS4;
     sig += io.chunk_stride;
   }
 #endif
   if (full < io.nchunk) {
-    const bool valid = full * G + io.lane < io.nmeas;
+    const bool valid = full * Gw + io.lane < io.nmeas;
     fp32 cf[kNCOLS];
     cdm_load_cfp(valid ? row : sproto, 0, 0, cf);
     const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - *sig;
     acc = valid ? fmaf(r, r, acc) : acc;
   }
-  return cdm_group_sum<G>((double)acc, gmask);
+  return cdm_group_sum<Gw>((double)acc, gmask);
 }
 
 // log I0(x) with the polynomial approximations of Abramowitz & Stegun
@@ -326,7 +326,7 @@ __device__ __forceinline__ float2 cdm_log_i0_fast2(float2 x) {
 // Rician log-likelihood sum without the voxel-constant sum of log(y)
 // (which cancels in every Metropolis ratio): sum of
 // -tau/2 (y^2 + S^2) + log I0(tau S y).
-template <int G>
+template <int Gw>
 __device__ __forceinline__ double cdm_group_rician(const cdm_voxel_io& io, const float* sproto,
                                                    fp32* P, fp32* FixP, float tau, unsigned gmask) {
   float acc = 0.0f;
@@ -335,7 +335,7 @@ __device__ __forceinline__ double cdm_group_rician(const cdm_voxel_io& io, const
   // full chunk pairs through the paired signal hook (the pair table), the
   // log I0 term per measurement
   {
-    const int full = io.nmeas / G;
+    const int full = io.nmeas / Gw;
     const float* q = io.pairs;
     const float* sig = io.sig;
     float2 acc2 = make_float2(0.0f, 0.0f);
@@ -350,14 +350,14 @@ __device__ __forceinline__ double cdm_group_rician(const cdm_voxel_io& io, const
       const float2 e = __ffma2_rn(y2, y2, __fmul2_rn(s2, s2));
       acc2 = __ffma2_rn(nht, e, acc2);
       acc2 = __fadd2_rn(acc2, cdm_log_i0_fast2(__fmul2_rn(__fmul2_rn(tau2, s2), y2)));
-      q += 2 * G * kNCOLSP;
+      q += 2 * Gw * kNCOLSP;
       sig += 2 * io.chunk_stride;
     }
     acc = acc2.x + acc2.y;
   }
 #endif
   for (int c = c0; c < io.nchunk; c++) {
-    const int m = c * G + io.lane;
+    const int m = c * Gw + io.lane;
     const bool valid = m < io.nmeas;
     fp32 cf[kNCOLS];
     cdm_load_cfp(sproto, io.nmeas_pad, valid ? m : 0, cf);
@@ -366,20 +366,20 @@ __device__ __forceinline__ double cdm_group_rician(const cdm_voxel_io& io, const
     const float t = -0.5f * tau * (y * y + s * s) + cdm_log_i0_fast(tau * s * y);
     acc = valid ? acc + t : acc;
   }
-  return cdm_group_sum<G>((double)acc, gmask);
+  return cdm_group_sum<Gw>((double)acc, gmask);
 }
 
 // Sum of log(y) over the voxel (for BIC/AIC, which need the full Rician
 // likelihood).
-template <int G>
+template <int Gw>
 __device__ __forceinline__ double cdm_group_sum_log_meas(const cdm_voxel_io& io, unsigned gmask) {
   float acc = 0.0f;
   for (int c = 0; c < io.nchunk; c++) {
-    const int m = c * G + io.lane;
+    const int m = c * Gw + io.lane;
     const float y = io.sig[(size_t)c * io.chunk_stride];
     acc = (m < io.nmeas) ? acc + logf(y) : acc;
   }
-  return cdm_group_sum<G>((double)acc, gmask);
+  return cdm_group_sum<Gw>((double)acc, gmask);
 }
 
 __device__ __forceinline__ void cdm_load_params(const double* __restrict__ src, fp32* P) {
@@ -390,7 +390,7 @@ __device__ __forceinline__ void cdm_load_params(const double* __restrict__ src, 
 }
 
 __device__ __forceinline__ void cdm_load_fixp(const double* __restrict__ src, int fixp_tsize,
-                                              fp32* F) {
+                                              fp32* fixv) {
 #pragma unroll
-  for (int k = 0; k < kNFIX; k++) F[k] = fp32(k < fixp_tsize ? (float)src[k] : 0.0f);
+  for (int k = 0; k < kNFIX; k++) fixv[k] = fp32(k < fixp_tsize ? (float)src[k] : 0.0f);
 }

@@ -39,35 +39,35 @@ struct cdm_gs_args {
   cdm_limits lim;
 };
 
-__device__ __forceinline__ bool cdm_gs_in_bounds(const cdm_limits& L, const double* x) {
+__device__ __forceinline__ bool cdm_gs_in_bounds(const cdm_limits& lim, const double* x) {
 #pragma unroll
   for (int p = 0; p < kNP; p++) {
-    if (L.btype[p] == BMIN) {
-      if (x[p] < (double)L.bmin[p]) return false;
-    } else if (L.btype[p] == BMAX) {
-      if (x[p] > (double)L.bmax[p]) return false;
-    } else if (L.btype[p] == BMINMAX) {
-      if (x[p] < (double)L.bmin[p]) return false;
-      if (x[p] > (double)L.bmax[p]) return false;
+    if (lim.btype[p] == BMIN) {
+      if (x[p] < (double)lim.bmin[p]) return false;
+    } else if (lim.btype[p] == BMAX) {
+      if (x[p] > (double)lim.bmax[p]) return false;
+    } else if (lim.btype[p] == BMINMAX) {
+      if (x[p] < (double)lim.bmin[p]) return false;
+      if (x[p] > (double)lim.bmax[p]) return false;
     }
   }
   return true;
 }
 
-template <int G>
+template <int Gw>
 __global__ void __launch_bounds__(CDM_NT) cdm_gridsearch_kernel(const __grid_constant__ cdm_gs_args a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
-  const float* ptab = cdm_build_pair_table<G>(sproto, a.nmeas_pad, a.nchunk);
-  const int v = blockIdx.x * (CDM_NT / G) + (int)threadIdx.x / G;
+  const float* ptab = cdm_build_pair_table<Gw>(sproto, a.nmeas_pad, a.nchunk);
+  const int v = blockIdx.x * (CDM_NT / Gw) + (int)threadIdx.x / Gw;
   if (v >= a.nvox) return;
-  const unsigned gm = cdm_group_mask<G>();
-  const int lane = (int)threadIdx.x % G;
-  const cdm_limits& L = a.lim;
+  const unsigned gm = cdm_group_mask<Gw>();
+  const int lane = (int)threadIdx.x % Gw;
+  const cdm_limits& lim = a.lim;
 
   cdm_voxel_io io;
-  io.sig = a.sig + (size_t)v * G + lane;
-  io.chunk_stride = (size_t)a.nvox * G;
+  io.sig = a.sig + (size_t)v * Gw + lane;
+  io.chunk_stride = (size_t)a.nvox * Gw;
   io.nchunk = a.nchunk;
   io.nmeas = a.nmeas;
   io.nmeas_pad = a.nmeas_pad;
@@ -92,14 +92,14 @@ __global__ void __launch_bounds__(CDM_NT) cdm_gridsearch_kernel(const __grid_con
 #pragma unroll
     for (int p = 0; p < kNP; p++)
       trial[p] = a.gpos[p] >= 0 ? __ldg(a.grid + (size_t)c * a.ngp + a.gpos[p]) : base[p];
-    if (!cdm_gs_in_bounds(L, trial)) continue;
+    if (!cdm_gs_in_bounds(lim, trial)) continue;
     fp32 P[kNPS];
 #pragma unroll
     for (int i = 0; i < kNPS; i++) P[i] = fp32(0.0f);
 #pragma unroll
     for (int p = 0; p < kNP; p++) P[p] = fp32((float)trial[p]);
     cdm_update_derived(P, FixP);
-    const double cost = cdm_group_sse<G>(io, sproto, P, FixP, gm);
+    const double cost = cdm_group_sse<Gw>(io, sproto, P, FixP, gm);
     // Sorted insertion with constant indices (register arrays): entries
     // strictly worse than `cost` move down one place, equal costs keep the
     // earlier combination first (CUDIMOT's strict '<').
@@ -122,10 +122,10 @@ __global__ void __launch_bounds__(CDM_NT) cdm_gridsearch_kernel(const __grid_con
     a.flags[v] = 0;
     return;
   }
-  const double lim = bcost[0] * (1.0 + (double)a.band);
+  const double band_cost = bcost[0] * (1.0 + (double)a.band);
   int nin = 0;
 #pragma unroll
-  for (int k = 0; k < kGsTop; k++) nin += (bcomb[k] >= 0 && bcost[k] <= lim) ? 1 : 0;
+  for (int k = 0; k < kGsTop; k++) nin += (bcomb[k] >= 0 && bcost[k] <= band_cost) ? 1 : 0;
   a.flags[v] = nin <= 1 ? 0 : (nin < kGsTop ? 1 : 2);
 #pragma unroll
   for (int k = 0; k < kGsTop; k++) a.cand[(size_t)v * kGsTop + k] = bcomb[k];

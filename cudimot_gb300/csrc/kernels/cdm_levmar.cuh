@@ -51,20 +51,20 @@ __device__ __forceinline__ float cdm_minmax_inv(float x, float lo, float hi) {
 }
 
 // invtransformAll (Levenberg_Marquardt.cu:90-103).
-__device__ __forceinline__ void cdm_lm_inv_transform(const cdm_limits& L, fp32* P, float* Pt) {
+__device__ __forceinline__ void cdm_lm_inv_transform(const cdm_limits& lim, fp32* P, float* Pt) {
 #pragma unroll
   for (int p = 0; p < kNP; p++) {
-    const float lo = L.bmin[p], hi = L.bmax[p];
+    const float lo = lim.bmin[p], hi = lim.bmax[p];
     float x = (float)P[p];
-    if (L.fixed[p]) {  // a fixed parameter never moves: no round trip through the transform
+    if (lim.fixed[p]) {  // a fixed parameter never moves: no round trip through the transform
       Pt[p] = x;
       continue;
     }
-    if (L.btype[p] == BMIN) {
+    if (lim.btype[p] == BMIN) {
       Pt[p] = logf(x - lo);
-    } else if (L.btype[p] == BMAX) {
+    } else if (lim.btype[p] == BMAX) {
       Pt[p] = logf(hi - x);
-    } else if (L.btype[p] == BMINMAX) {
+    } else if (lim.btype[p] == BMINMAX) {
       if (x <= lo + kAvoidf) x += kAvoidf;
       if (x >= hi - kAvoidf) x -= kAvoidf;
       P[p] = fp32(x);
@@ -76,16 +76,16 @@ __device__ __forceinline__ void cdm_lm_inv_transform(const cdm_limits& L, fp32* 
 }
 
 // transformAll (Levenberg_Marquardt.cu:105-118); may nudge Pt.
-__device__ __forceinline__ void cdm_lm_transform(const cdm_limits& L, fp32* P, float* Pt) {
+__device__ __forceinline__ void cdm_lm_transform(const cdm_limits& lim, fp32* P, float* Pt) {
 #pragma unroll
   for (int p = 0; p < kNP; p++) {
-    const float lo = L.bmin[p], hi = L.bmax[p];
-    if (L.fixed[p]) continue;
-    if (L.btype[p] == BMIN) {
+    const float lo = lim.bmin[p], hi = lim.bmax[p];
+    if (lim.fixed[p]) continue;
+    if (lim.btype[p] == BMIN) {
       P[p] = fp32(expf(Pt[p]) + lo);
-    } else if (L.btype[p] == BMAX) {
+    } else if (lim.btype[p] == BMAX) {
       P[p] = fp32(hi - expf(Pt[p]));
-    } else if (L.btype[p] == BMINMAX) {
+    } else if (lim.btype[p] == BMINMAX) {
       float x = (hi - lo) * 0.5f * atanf(Pt[p] / kSpeedf) * kTwoDivPIf + (lo + hi) * 0.5f;
       if (x <= lo + kAvoidf) {
         x += kAvoidf;
@@ -103,15 +103,15 @@ __device__ __forceinline__ void cdm_lm_transform(const cdm_limits& L, fp32* P, f
 }
 
 // d theta / d theta_t per parameter (derivative_transf, :120-135).
-__device__ __forceinline__ void cdm_lm_chain(const cdm_limits& L, const float* Pt, float* f) {
+__device__ __forceinline__ void cdm_lm_chain(const cdm_limits& lim, const float* Pt, float* f) {
 #pragma unroll
   for (int p = 0; p < kNP; p++) {
-    if (L.btype[p] == BMIN)
+    if (lim.btype[p] == BMIN)
       f[p] = expf(Pt[p]);
-    else if (L.btype[p] == BMAX)
+    else if (lim.btype[p] == BMAX)
       f[p] = -expf(Pt[p]);
-    else if (L.btype[p] == BMINMAX)
-      f[p] = (L.bmax[p] - L.bmin[p]) * 0.5f * kTwoDivPIf * (kSpeedf / (kSpeedf * kSpeedf + Pt[p] * Pt[p]));
+    else if (lim.btype[p] == BMINMAX)
+      f[p] = (lim.bmax[p] - lim.bmin[p]) * 0.5f * kTwoDivPIf * (kSpeedf / (kSpeedf * kSpeedf + Pt[p] * Pt[p]));
     else
       f[p] = 1.0f;
   }
@@ -133,32 +133,32 @@ __host__ __device__ constexpr int cdm_hidx(int i, int q) { return i * kNP - i * 
 #define CDM_LM_CFTOL 1.0e-6
 #endif
 
-// Damped normal equations (H + damping) x = g in FP64, all in registers:
+// Damped normal equations (hess + damping) x = g in FP64, all in registers:
 // symmetric Gaussian elimination on the packed upper triangle (no pivoting,
 // the pivot order of CUDIMOT's Gauss-Jordan LUsolver,
 // Levenberg_Marquardt.cu:334-407), then back substitution. ~n^3/6
 // multiply-adds instead of Gauss-Jordan's ~n^3/2.
-__device__ __forceinline__ void cdm_lm_solve(const double (&H)[kNH], const double (&g)[kNP],
+__device__ __forceinline__ void cdm_lm_solve(const double (&hess)[kNH], const double (&g)[kNP],
                                              double lambda, bool marquardt, double (&x)[kNP]) {
-  double A[kNH], b[kNP];
+  double amat[kNH], b[kNP];
 #pragma unroll
   for (int i = 0; i < kNP; i++) {
     b[i] = g[i];
 #pragma unroll
     for (int q = i; q < kNP; q++) {
-      const double h = H[cdm_hidx(i, q)];
-      A[cdm_hidx(i, q)] = i == q ? (marquardt ? (1.0 + lambda) * h : h + lambda) : h;
+      const double h = hess[cdm_hidx(i, q)];
+      amat[cdm_hidx(i, q)] = i == q ? (marquardt ? (1.0 + lambda) * h : h + lambda) : h;
     }
   }
   double dinv[kNP];
 #pragma unroll
   for (int j = 0; j < kNP; j++) {
-    dinv[j] = 1.0 / A[cdm_hidx(j, j)];
+    dinv[j] = 1.0 / amat[cdm_hidx(j, j)];
 #pragma unroll
     for (int i = j + 1; i < kNP; i++) {
-      const double f = A[cdm_hidx(j, i)] * dinv[j];
+      const double f = amat[cdm_hidx(j, i)] * dinv[j];
 #pragma unroll
-      for (int q = i; q < kNP; q++) A[cdm_hidx(i, q)] -= f * A[cdm_hidx(j, q)];
+      for (int q = i; q < kNP; q++) amat[cdm_hidx(i, q)] -= f * amat[cdm_hidx(j, q)];
       b[i] -= f * b[j];
     }
   }
@@ -166,25 +166,25 @@ __device__ __forceinline__ void cdm_lm_solve(const double (&H)[kNH], const doubl
   for (int i = kNP - 1; i >= 0; i--) {
     double acc = b[i];
 #pragma unroll
-    for (int q = i + 1; q < kNP; q++) acc -= A[cdm_hidx(i, q)] * x[q];
+    for (int q = i + 1; q < kNP; q++) acc -= amat[cdm_hidx(i, q)] * x[q];
     x[i] = acc * dinv[i];
   }
 }
 
-template <int G>
+template <int Gw>
 __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constant__ cdm_lm_args a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
-  const float* ptab = cdm_build_pair_table<G>(sproto, a.nmeas_pad, a.nchunk);
-  const int v = blockIdx.x * (CDM_NT / G) + (int)threadIdx.x / G;
+  const float* ptab = cdm_build_pair_table<Gw>(sproto, a.nmeas_pad, a.nchunk);
+  const int v = blockIdx.x * (CDM_NT / Gw) + (int)threadIdx.x / Gw;
   if (v >= a.nvox) return;
-  const unsigned gm = cdm_group_mask<G>();
-  const int lane = (int)threadIdx.x % G;
-  const cdm_limits& L = a.lim;
+  const unsigned gm = cdm_group_mask<Gw>();
+  const int lane = (int)threadIdx.x % Gw;
+  const cdm_limits& lim = a.lim;
 
   cdm_voxel_io io;
-  io.sig = a.sig + (size_t)v * G + lane;
-  io.chunk_stride = (size_t)a.nvox * G;
+  io.sig = a.sig + (size_t)v * Gw + lane;
+  io.chunk_stride = (size_t)a.nvox * Gw;
   io.nchunk = a.nchunk;
   io.nmeas = a.nmeas;
   io.nmeas_pad = a.nmeas_pad;
@@ -195,13 +195,13 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
   float Pt[kNP];
   cdm_load_params(a.params + (size_t)v * kNP, P);
   cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
-  cdm_lm_inv_transform(L, P, Pt);
+  cdm_lm_inv_transform(lim, P, Pt);
   cdm_update_derived(P, FixP);
-  double pcf = cdm_group_sse<G>(io, sproto, P, FixP, gm);
+  double pcf = cdm_group_sse<Gw>(io, sproto, P, FixP, gm);
 
-  double H[kNH], g[kNP];
+  double hess[kNH], g[kNP];
 #pragma unroll
-  for (int i = 0; i < kNH; i++) H[i] = 0.0;
+  for (int i = 0; i < kNH; i++) hess[i] = 0.0;
 #pragma unroll
   for (int i = 0; i < kNP; i++) g[i] = 0.0;
   double lambda = 0.1;
@@ -211,14 +211,14 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
     passes++;
     if (success) {
       float chain[kNP];
-      cdm_lm_chain(L, Pt, chain);
+      cdm_lm_chain(lim, Pt, chain);
       float gl[kNP], hl[kNH];
 #pragma unroll
       for (int i = 0; i < kNP; i++) gl[i] = 0.0f;
 #pragma unroll
       for (int i = 0; i < kNH; i++) hl[i] = 0.0f;
       for (int c = 0; c < io.nchunk; c++) {
-        const int m = c * G + lane;
+        const int m = c * Gw + lane;
         const bool valid = m < io.nmeas;
         fp32 cf[kNCOLS];
         cdm_load_cfp(sproto, io.nmeas_pad, valid ? m : 0, cf);
@@ -242,18 +242,18 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
       }
       // Group sums in FP64; factor 2 of CUDIMOT's gradient/Hessian (:240, :308).
 #pragma unroll
-      for (int i = 0; i < kNP; i++) g[i] = L.fixed[i] ? 0.0 : 2.0 * cdm_group_sum<G>((double)gl[i], gm);
+      for (int i = 0; i < kNP; i++) g[i] = lim.fixed[i] ? 0.0 : 2.0 * cdm_group_sum<Gw>((double)gl[i], gm);
       int k = 0;
 #pragma unroll
       for (int i = 0; i < kNP; i++)
 #pragma unroll
         for (int q = i; q < kNP; q++) {
-          const double s = 2.0 * cdm_group_sum<G>((double)hl[k], gm);
-          H[k++] = (L.fixed[i] || L.fixed[q]) ? (i == q ? 1.0 : 0.0) : s;
+          const double s = 2.0 * cdm_group_sum<Gw>((double)hl[k], gm);
+          hess[k++] = (lim.fixed[i] || lim.fixed[q]) ? (i == q ? 1.0 : 0.0) : s;
         }
     }
     double x[kNP];
-    cdm_lm_solve(H, g, lambda, a.marquardt != 0, x);
+    cdm_lm_solve(hess, g, lambda, a.marquardt != 0, x);
 
     float step[kNP];
 #pragma unroll
@@ -261,9 +261,9 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
     fp32 Pn[kNPS];
 #pragma unroll
     for (int i = 0; i < kNPS; i++) Pn[i] = P[i];
-    cdm_lm_transform(L, Pn, step);
+    cdm_lm_transform(lim, Pn, step);
     cdm_update_derived(Pn, FixP);
-    const double ncf = cdm_group_sse<G>(io, sproto, Pn, FixP, gm);
+    const double ncf = cdm_group_sse<Gw>(io, sproto, Pn, FixP, gm);
     success = ncf < pcf;
     if (success) {
       nsucc++;
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
       if (2.0 * fabs(pcf - ncf) <= CDM_LM_CFTOL * (fabs(pcf) + fabs(ncf) + 2.0e-16)) end = true;
       pcf = ncf;
     } else {
-      // A rejected step that moved no parameter at all: larger damping only
+      // amat rejected step that moved no parameter at all: larger damping only
       // shrinks the step further, so every later trial is the same point.
       bool moved = false;
 #pragma unroll
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
       if (lambda > 1.0e20 || !moved) end = true;
       // CUDIMOT re-derives P from Pt after a rejected step (:593), which can
       // nudge Pt at a two-sided bound.
-      cdm_lm_transform(L, P, Pt);
+      cdm_lm_transform(lim, P, Pt);
       cdm_update_derived(P, FixP);
     }
     if (end) break;
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
       // value in full double precision
       const double in = a.params[(size_t)v * kNP + p];
       a.params[(size_t)v * kNP + p] =
-          (L.fixed[p] && (float)P[p] == (float)in) ? in : (double)(float)P[p];
+          (lim.fixed[p] && (float)P[p] == (float)in) ? in : (double)(float)P[p];
     }
     if (a.iter_count) atomicAdd(a.iter_count, (unsigned long long)passes);
     if (a.succ_count) atomicAdd(a.succ_count, (unsigned long long)nsucc);

@@ -42,21 +42,21 @@ struct cdm_mcmc_args {
   cdm_limits lim;
 };
 
-__device__ __forceinline__ float cdm_prior(const cdm_limits& L, int p, fp32* P, int nmeas,
+__device__ __forceinline__ float cdm_prior(const cdm_limits& lim, int p, fp32* P, int nmeas,
                                            fp32* cfp_all, fp32* FixP) {
   fp32 xv = P[0];
 #pragma unroll
   for (int k = 1; k < kNP; k++) xv = (k == p) ? P[k] : xv;
   const float x = (float)xv;
-  switch (L.ptype[p]) {
+  switch (lim.ptype[p]) {
     case GAUSSPRIOR: {
-      const float d = x - L.pa[p];
-      return d * d / (2.0f * L.pb[p] * L.pb[p]);
+      const float d = x - lim.pa[p];
+      return d * d / (2.0f * lim.pb[p] * lim.pb[p]);
     }
     case GAMMAPRIOR:
-      return (1.0f - L.pa[p]) * logf(x) + L.pb[p] * x;
+      return (1.0f - lim.pa[p]) * logf(x) + lim.pb[p] * x;
     case ARDPRIOR:
-      return L.pa[p] * logf(x);
+      return lim.pa[p] * logf(x);
     case SINPRIOR:
       return -logf(fabsf(sinf(x) * 0.5f));
     case CUSTOM:
@@ -66,15 +66,15 @@ __device__ __forceinline__ float cdm_prior(const cdm_limits& L, int p, fp32* P, 
   }
 }
 
-__device__ __forceinline__ bool cdm_in_bounds(const cdm_limits& L, int p, fp32* P) {
+__device__ __forceinline__ bool cdm_in_bounds(const cdm_limits& lim, int p, fp32* P) {
   if (!ConstraintsMCMC(NPARAMS, P)) return false;
   fp32 xv = P[0];
 #pragma unroll
   for (int k = 1; k < kNP; k++) xv = (k == p) ? P[k] : xv;
   const float x = (float)xv;
-  if (L.btype[p] == BMIN) return !(x < L.bmin[p]);
-  if (L.btype[p] == BMAX) return !(x > L.bmax[p]);
-  if (L.btype[p] == BMINMAX) return !(x < L.bmin[p]) && !(x > L.bmax[p]);
+  if (lim.btype[p] == BMIN) return !(x < lim.bmin[p]);
+  if (lim.btype[p] == BMAX) return !(x > lim.bmax[p]);
+  if (lim.btype[p] == BMINMAX) return !(x < lim.bmin[p]) && !(x > lim.bmax[p]);
   return true;
 }
 
@@ -83,27 +83,27 @@ __device__ __forceinline__ bool cdm_in_bounds(const cdm_limits& L, int p, fp32* 
 // instruction cache instead of NPARAMS), and these unrolled selects keep
 // the arrays in registers.
 // Only the first kNP entries are ever selected (the model parameters).
-template <class V>
-__device__ __forceinline__ V cdm_get(const V* a, int i) {
-  V v = a[0];
+template <class Tv>
+__device__ __forceinline__ Tv cdm_get(const Tv* a, int i) {
+  Tv v = a[0];
 #pragma unroll
   for (int k = 1; k < kNP; k++) v = (k == i) ? a[k] : v;
   return v;
 }
-template <class V>
-__device__ __forceinline__ void cdm_set(V* a, int i, V x) {
+template <class Tv>
+__device__ __forceinline__ void cdm_set(Tv* a, int i, Tv x) {
 #pragma unroll
   for (int k = 0; k < kNP; k++) a[k] = (k == i) ? x : a[k];
 }
 
-template <int G, bool RICIAN>
+template <int Gw, bool RICIAN>
 __device__ __forceinline__ double cdm_likelihood(const cdm_voxel_io& io, const float* sproto,
                                                  fp32* P, fp32* FixP, float tau, unsigned gmask) {
   if (RICIAN) {
-    const double s = cdm_group_rician<G>(io, sproto, P, FixP, tau, gmask);
+    const double s = cdm_group_rician<Gw>(io, sproto, P, FixP, tau, gmask);
     return -(double)io.nmeas * (double)logf(tau) - s;
   }
-  const double sse = cdm_group_sse<G>(io, sproto, P, FixP, gmask);
+  const double sse = cdm_group_sse<Gw>(io, sproto, P, FixP, gmask);
   return (double)(0.5f * (float)io.nmeas * logf(0.5f * (float)sse));
 }
 
@@ -112,20 +112,20 @@ __device__ __forceinline__ double cdm_likelihood(const cdm_voxel_io& io, const f
 #define CDM_MCMC_MIN_BLOCKS 4
 #endif
 
-template <int G, bool RICIAN>
+template <int Gw, bool RICIAN>
 __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(const __grid_constant__ cdm_mcmc_args a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
-  const float* ptab = cdm_build_pair_table<G>(sproto, a.nmeas_pad, a.nchunk);
-  const int v = blockIdx.x * (CDM_NT / G) + (int)threadIdx.x / G;
+  const float* ptab = cdm_build_pair_table<Gw>(sproto, a.nmeas_pad, a.nchunk);
+  const int v = blockIdx.x * (CDM_NT / Gw) + (int)threadIdx.x / Gw;
   if (v >= a.nvox) return;
-  const unsigned gm = cdm_group_mask<G>();
-  const int lane = (int)threadIdx.x % G;
-  const cdm_limits& L = a.lim;
+  const unsigned gm = cdm_group_mask<Gw>();
+  const int lane = (int)threadIdx.x % Gw;
+  const cdm_limits& lim = a.lim;
 
   cdm_voxel_io io;
-  io.sig = a.sig + (size_t)v * G + lane;
-  io.chunk_stride = (size_t)a.nvox * G;
+  io.sig = a.sig + (size_t)v * Gw + lane;
+  io.chunk_stride = (size_t)a.nvox * Gw;
   io.nchunk = a.nchunk;
   io.nmeas = a.nmeas;
   io.nmeas_pad = a.nmeas_pad;
@@ -162,13 +162,13 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
       acc[p] = 0;
       rej[p] = 0;
       float x = (float)P[p];
-      if (L.btype[p] == BMIN) {
-        if (x < L.bmin[p]) x = L.bmin[p];
-      } else if (L.btype[p] == BMAX) {
-        if (x > L.bmax[p]) x = L.bmax[p];
-      } else if (L.btype[p] == BMINMAX) {
-        if (x < L.bmin[p]) x = L.bmin[p];
-        else if (x > L.bmax[p]) x = L.bmax[p];
+      if (lim.btype[p] == BMIN) {
+        if (x < lim.bmin[p]) x = lim.bmin[p];
+      } else if (lim.btype[p] == BMAX) {
+        if (x > lim.bmax[p]) x = lim.bmax[p];
+      } else if (lim.btype[p] == BMINMAX) {
+        if (x < lim.bmin[p]) x = lim.bmin[p];
+        else if (x > lim.bmax[p]) x = lim.bmax[p];
       }
       P[p] = fp32(x);
     }
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
     float total_prior = 0.0f;
 #pragma unroll
     for (int p = 0; p < kNP; p++) {
-      prior[p] = cdm_prior(L, p, P, a.nmeas, cf0, FixP);
+      prior[p] = cdm_prior(lim, p, P, a.nmeas, cf0, FixP);
       total_prior += prior[p];
     }
     tacc = trej = 0;
@@ -185,25 +185,25 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
       // Initialise_TauRician (MCMC.cu:193-251): tau = 1 / variance of residuals.
       float s1 = 0.0f;
       for (int c = 0; c < io.nchunk; c++) {
-        const int m = c * G + lane;
+        const int m = c * Gw + lane;
         fp32 cf[kNCOLS];
         cdm_load_cfp(sproto, io.nmeas_pad, m < io.nmeas ? m : 0, cf);
         const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - io.sig[(size_t)c * io.chunk_stride];
         s1 = (m < io.nmeas) ? s1 + r : s1;
       }
-      const float mean = (float)(cdm_group_sum<G>((double)s1, gm) / io.nmeas);
+      const float mean = (float)(cdm_group_sum<Gw>((double)s1, gm) / io.nmeas);
       float s2 = 0.0f;
       for (int c = 0; c < io.nchunk; c++) {
-        const int m = c * G + lane;
+        const int m = c * Gw + lane;
         fp32 cf[kNCOLS];
         cdm_load_cfp(sproto, io.nmeas_pad, m < io.nmeas ? m : 0, cf);
         const float r = mean - ((float)Predicted_Signal(NPARAMS, P, cf, FixP) - io.sig[(size_t)c * io.chunk_stride]);
         s2 = (m < io.nmeas) ? fmaf(r, r, s2) : s2;
       }
-      tau = (float)((double)io.nmeas / cdm_group_sum<G>((double)s2, gm));
+      tau = (float)((double)io.nmeas / cdm_group_sum<Gw>((double)s2, gm));
       tauSD = tau * 0.5f;
     }
-    energy = (double)total_prior + cdm_likelihood<G, RICIAN>(io, sproto, P, FixP, tau, gm);
+    energy = (double)total_prior + cdm_likelihood<Gw, RICIAN>(io, sproto, P, FixP, tau, gm);
 
     for (int it = 0; it < niters; it++) {
       const uint32_t git = (uint32_t)(recording ? nburn + it : it);
@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
           float tp = 0.0f;
 #pragma unroll
           for (int p = 0; p < kNP; p++) tp += prior[p];
-          const double ne = (double)tp + cdm_likelihood<G, RICIAN>(io, sproto, P, FixP, tau, gm);
+          const double ne = (double)tp + cdm_likelihood<Gw, RICIAN>(io, sproto, P, FixP, tau, gm);
           if (expf((float)(energy - ne)) > d.uniform) {
             tacc++;
             energy = ne;
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
       }
 #pragma unroll 1
       for (int p = 0; p < kNP; p++) {
-        if (L.fixed[p]) {
+        if (lim.fixed[p]) {
           cdm_set(acc, p, cdm_get(acc, p) + 1);
           continue;
         }
@@ -241,15 +241,15 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
         cdm_set(P, p, fp32((float)old + d.normal * cdm_get(propSD, p)));
         bool accepted = false;
         bool derived = false;
-        if (cdm_in_bounds(L, p, P)) {
+        if (cdm_in_bounds(lim, p, P)) {
           cdm_update_derived(P, FixP);
           derived = true;
           stale = false;
-          const float np_ = cdm_prior(L, p, P, a.nmeas, cf0, FixP);
+          const float np_ = cdm_prior(lim, p, P, a.nmeas, cf0, FixP);
           float tp = 0.0f;
 #pragma unroll
           for (int q = 0; q < kNP; q++) tp += (q == p) ? np_ : prior[q];
-          const double ne = (double)tp + cdm_likelihood<G, RICIAN>(io, sproto, P, FixP, tau, gm);
+          const double ne = (double)tp + cdm_likelihood<Gw, RICIAN>(io, sproto, P, FixP, tau, gm);
           if (expf((float)(energy - ne)) > d.uniform) {
             accepted = true;
             energy = ne;
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
 #pragma unroll
           for (int p = 0; p < kNP; p++)  // fixed parameters: their input value, in double
             dst[(size_t)p * a.nsamples] =
-                L.fixed[p] ? a.params[(size_t)v * kNP + p] : (double)(float)P[p];
+                lim.fixed[p] ? a.params[(size_t)v * kNP + p] : (double)(float)P[p];
           if (RICIAN && a.tau_samples) a.tau_samples[(size_t)v * a.nsamples + s] = (double)tau;
         }
       }
@@ -299,6 +299,6 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
   if (lane == 0) {
 #pragma unroll
     for (int p = 0; p < kNP; p++)
-      if (!L.fixed[p]) a.params[(size_t)v * kNP + p] = (double)(float)P[p];
+      if (!lim.fixed[p]) a.params[(size_t)v * kNP + p] = (double)(float)P[p];
   }
 }

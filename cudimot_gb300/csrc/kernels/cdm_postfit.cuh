@@ -190,19 +190,19 @@ __global__ void cdm_prep_protocol_kernel(const double* __restrict__ cfp, int nme
   }
 }
 
-// Signals: [nvox][nmeas] double -> [nchunk][nvox][G] float, so that the G
+// Signals: [nvox][nmeas] double -> [nchunk][nvox][Gw] float, so that the Gw
 // lanes of consecutive groups read one contiguous line per chunk.
-template <int G>
+template <int Gw>
 __global__ void cdm_pack_signals_kernel(const double* __restrict__ meas, int nvox, int nmeas,
                                         int nchunk, float* __restrict__ out) {
-  const size_t total = (size_t)nchunk * nvox * G;
+  const size_t total = (size_t)nchunk * nvox * Gw;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
-    const int j = (int)(i % G);
-    const size_t rest = i / G;
+    const int j = (int)(i % Gw);
+    const size_t rest = i / Gw;
     const int v = (int)(rest % nvox);
     const int c = (int)(rest / nvox);
-    const int m = c * G + j;
+    const int m = c * Gw + j;
     out[i] = m < nmeas ? (float)meas[(size_t)v * nmeas + m] : 0.0f;
   }
 }

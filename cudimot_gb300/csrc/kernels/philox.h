@@ -33,21 +33,21 @@ CDM_RNG_HD void cdm_mulhilo32(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo
 // Ten rounds of the Philox S-box; round multipliers and Weyl key increments
 // are the ones published with the generator.
 CDM_RNG_HD cdm_u32x4 cdm_philox4x32_10(cdm_u32x4 c, uint32_t k0, uint32_t k1) {
-  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
-  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+  const uint32_t kPhiloxM0 = 0xD2511F53u, kPhiloxM1 = 0xCD9E8D57u;
+  const uint32_t kPhiloxW0 = 0x9E3779B9u, kPhiloxW1 = 0xBB67AE85u;
 #pragma unroll
   for (int r = 0; r < 10; r++) {
     uint32_t hi0, lo0, hi1, lo1;
-    cdm_mulhilo32(M0, c.x, hi0, lo0);
-    cdm_mulhilo32(M1, c.z, hi1, lo1);
+    cdm_mulhilo32(kPhiloxM0, c.x, hi0, lo0);
+    cdm_mulhilo32(kPhiloxM1, c.z, hi1, lo1);
     cdm_u32x4 n;
     n.x = hi1 ^ c.y ^ k0;
     n.y = lo1;
     n.z = hi0 ^ c.w ^ k1;
     n.w = lo0;
     c = n;
-    k0 += W0;
-    k1 += W1;
+    k0 += kPhiloxW0;
+    k1 += kPhiloxW1;
   }
   return c;
 }

@@ -203,7 +203,9 @@ cdm_status cdm_fit_host(cdm_ctx* ctx, int nvox, int nmeas, const double* meas,
  * wait can never complete. The wait gives up after limit_ms (1..2000) and
  * records a device error, which the next cdm_synchronize on this context
  * reports as CDM_TIMEOUT and clears; the context stays usable. Every wait in
- * the fitting kernels takes the same path with a 2 s limit. */
+ * the fitting kernels takes the same path with a 2 s limit. With ctx NULL
+ * the error goes to the no-allocation error word of the current device
+ * (reported by cdm_noalloc_status). */
 cdm_status cdm_selftest_wait_timeout(cdm_ctx* ctx, int limit_ms, void* stream);
 
 /* dMRI_Data::remove_NonPositive_entries (dMRI_Data.cu:15-30), applied by
@@ -286,17 +288,31 @@ cdm_status cdm_get_stats(cdm_ctx* ctx, cdm_stats* stats);
  * framework that owns all device memory through its own pool), since
  * allocation can fail under such budgets and can synchronise the device.
  * Same arguments and results as cdm_levmar, but no context: the fit
- * options come from cfg, and the working memory (protocol table, packed
+ * options come from cfg (lanes_levmar = 0 picks the lane count by
+ * cdm_levmar's rule), and the working memory (protocol table, packed
  * signals, error word) is a fixed 16 MiB array in the library that every
  * GPU loading it holds until exit. Calls needing more than 16 MiB
  * (about nvox * nmeas * 4 bytes plus the protocol) return CDM_BAD_ARG;
- * split the voxels into parts. The first call on a device looks up the
- * array's device address (make it before any stream capture). All calls
- * share the array: calls that overlap on the GPU (different streams, or
- * different host threads) race and must be serialised by the caller. */
+ * split the voxels into parts. The protocol limit is cdm_levmar's (its
+ * staged table must fit in shared memory). The first call on a device
+ * looks up the array's device address and clears its error word (make it
+ * before any stream capture). All calls share the array: calls that
+ * overlap on the GPU (different streams, or different host threads) race
+ * and must be serialised by the caller.
+ * A bounded device wait that runs out (2 s) leaves that call's params at
+ * their start values and sets the device's error word; the call itself
+ * has already returned CDM_OK, so check cdm_noalloc_status. */
 cdm_status cdm_levmar_noalloc(const cdm_model_cfg* cfg, int nvox, int nmeas, int CFP_size,
                               int FixP_size, const double* meas, double* params,
                               const double* CFP, const double* FixP, void* stream);
+
+/* Error word of cdm_levmar_noalloc on the current device (no CUDIMOT
+ * counterpart). Waits for `stream`, then returns CDM_TIMEOUT if a bounded
+ * device wait of any no-allocation call ran out since the last check (and
+ * clears the word), CDM_OK otherwise. Allocates nothing. The word is shared
+ * by all callers on the device: a check races with calls still running on
+ * other streams. */
+cdm_status cdm_noalloc_status(void* stream);
 
 #ifdef __cplusplus
 }

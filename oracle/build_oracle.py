@@ -22,6 +22,16 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
+# Where this recipe looks for CUDIMOT's source tree unless CUDIMOT_REFERENCE
+# names another (the tree exists only on the build machine).
+DEFAULT_REFERENCE = "/root/reference"
+
+
+def reference_tree():
+    """CUDIMOT's source tree if it is present (CUDIMOT_REFERENCE, else the
+    default location), else None."""
+    ref = os.environ.get("CUDIMOT_REFERENCE", DEFAULT_REFERENCE)
+    return ref if ref and os.path.isdir(os.path.join(ref, "mymodels")) else None
 PRELUDE = os.path.join(ROOT, "cudimot_gb300", "csrc", "prelude")
 KERNELS = os.path.join(ROOT, "cudimot_gb300", "csrc", "kernels")
 INCLUDE = os.path.join(ROOT, "include")

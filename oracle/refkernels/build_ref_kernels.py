@@ -1,6 +1,6 @@
 """Build CUDIMOT's own GPU kernels for the GB300 (test infrastructure).
 
-    python oracle/refkernels/build_ref_kernels.py --reference /root/reference [--models ...]
+    python oracle/refkernels/build_ref_kernels.py --reference CUDIMOT_TREE [--models ...]
 
 Where the CUDIMOT source tree is present: compiles GridSearch.cu,
 Levenberg_Marquardt.cu, MCMC.cu, BIC_AIC.cu and getPredictedSignal.cu of the

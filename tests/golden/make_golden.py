@@ -1,6 +1,6 @@
 """Generate the golden fixtures that pin the oracle to CUDIMOT's own plugins.
 
-    python oracle/build_oracle.py --reference /root/reference
+    python oracle/build_oracle.py --reference CUDIMOT_TREE
     python tests/golden/make_golden.py
 
 Runs CUDIMOT's unchanged plugins, compiled for the host into oracle/_ref/
