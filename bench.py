@@ -198,7 +198,21 @@ def flop_model():
         return None
 
 
+def headline_config(nvox, world):
+    """The config dict of the headline line (both arms print the same)."""
+    return {"workload": "noddi_watson_gs_lm_mcmc", "model": MODEL, "nvox_per_gpu": nvox,
+            "nmeas": 288, "grid_combs": 968, "nburn": NBURN, "njumps": NJUMPS, "sampleevery": SE,
+            "l2": "inputs larger than L2 (no flush)", "parallelism": f"voxel shards x{world}"}
+
+
+CPU_PLUGIN_NOTE = ("the CPU oracle runs this library's NODDI-Watson plugin (59 FLOP per signal), "
+                   "not CUDIMOT's as written (620-820 FLOP per signal, FP64 closed forms)")
+
+
 def run_reference(a, rank, world):
+    """CUDIMOT's fitting loops restated on the CPU (the oracle, FP64,
+    OpenMP over all host cores): every timed step fits a 2,048-voxel sample
+    of the headline workload (warm-up steps 256 voxels)."""
     if rank != 0:
         return
     from cudimot_gb300 import synth
@@ -207,11 +221,12 @@ def run_reference(a, rank, world):
     # inputs generated on the host: noiseless signal from the CPU oracle
     from oracle.oracle import Oracle
     o = Oracle(MODEL)
-    n = a.cpu_sample or 24 * o.max_threads()
+    n = a.cpu_sample or 2048
     wl = synth.noddi_watson(n, signal_fn=lambda t, c, s0: o.signal(t, c, s0[:, None]))
     times = []
     for i in range(a.warmup + a.steps):
-        v, threads, dt = cpu_baseline(wl.cfp, wl.meas, wl.fixp, wl.init, n, cfg)
+        k = n if i >= a.warmup else min(n, 256)
+        v, threads, dt = cpu_baseline(wl.cfp, wl.meas, wl.fixp, wl.init, k, cfg)
         if i >= a.warmup:
             times.append(dt)
     dt = float(np.mean(times))
@@ -220,12 +235,12 @@ def run_reference(a, rank, world):
             "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": dt * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded NODDI-Watson, SNR 20)",
-            "config": {"workload": "noddi_watson_gs_lm_mcmc", "model": MODEL, "nvox_full": NVOX,
-                       "nvox_sample": n, "nmeas": 288, "grid_combs": 968, "nburn": NBURN,
-                       "njumps": NJUMPS, "sampleevery": SE},
+            "config": headline_config(NVOX, world),
             "cpu_baseline": {"value": value, "unit": "voxels/s", "cores": threads, "kind": "port",
-                             "sample": f"{n} voxels of the 200k-voxel workload per step, full "
-                                       "grid search -> LM -> MCMC, FP64 CPU oracle"},
+                             "sample": f"{n} voxels of the 200,000-voxel workload per timed step "
+                                       "(warm-up steps 256), full grid search -> LM -> MCMC, "
+                                       "FP64 CPU oracle",
+                             "plugin": CPU_PLUGIN_NOTE},
             "e2e": {"value": value, "unit": "voxels/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -288,16 +303,26 @@ def profile_stage(a):
                       "ms": e0.elapsed_time(e1)}))
 
 
-def profiled_traffic():
-    """Per-launch DRAM bytes of the MCMC kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "mcmc_kernel_noddi_watson.md")
+def measured_traffic(kernel, config):
+    """DRAM bytes per launch of a kernel from bench_traffic.json (one ncu
+    capture per kernel, tagged with the configuration it was taken on).
+    Returned as captured when this run's configuration matches; when only
+    the voxel count differs, scaled by voxels (the kernel reads each voxel's
+    signals once and writes its samples once); else None."""
     try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":")[1].split()[0])
-    except (OSError, ValueError, IndexError):
-        pass
-    return None
+        rec = json.load(open(os.path.join(ROOT, "bench_traffic.json")))[kernel]
+    except (OSError, ValueError, KeyError):
+        return None, None
+    cap = rec["config"]
+    same = {k: v for k, v in cap.items() if k != "nvox"} == {k: v for k, v in config.items()
+                                                              if k != "nvox"}
+    if not same:
+        return None, None
+    b = float(rec["dram_bytes_per_launch"])
+    if cap["nvox"] == config["nvox"]:
+        return b, f"ncu capture of this configuration ({rec['command']})"
+    return b * config["nvox"] / cap["nvox"], (f"ncu capture at {cap['nvox']} voxels scaled to "
+                                              f"{config['nvox']} ({rec['command']})")
 
 
 def timed_events(fn, steps, flush=None):
@@ -442,14 +467,29 @@ def bench_heterogeneous(a, dev):
     print(json.dumps(line))
 
 
-def bench_learned(a, dev):
-    """Network-initialised vs grid-initialised NODDI-Watson fits on the same
-    GPU. The network (288 -> 256 -> 256 -> 256 -> 12, BF16 tensor cores) is
-    trained first on --train-signals synthetic signals (SNR U(10,50)) plus
-    --lm-targets grid-search+LM fits; then --eval-voxels voxels at SNR 20 are
-    fitted both ways, each LM -> MCMC (1250 + 1250, every 25th). Voxels
-    whose surrogate-path LM cost exceeds the plain path's by > 1 % are
-    refit by grid search + LM (counted in the surrogate time)."""
+def param_error(m, truth):
+    """Posterior means (or fits) against the true NODDI-Watson parameters."""
+    ang = np.degrees(np.arccos(np.clip(np.abs(
+        np.sin(m[:, 3]) * np.sin(truth[:, 3]) * np.cos(m[:, 4] - truth[:, 4]) +
+        np.cos(m[:, 3]) * np.cos(truth[:, 3])), 0, 1)))
+    return {"fiso_rmse": float(np.sqrt(np.mean((m[:, 0] - truth[:, 0]) ** 2))),
+            "fintra_rmse": float(np.sqrt(np.mean((m[:, 1] - truth[:, 1]) ** 2))),
+            "log_kappa_rmse": float(np.sqrt(np.mean((np.log(np.maximum(m[:, 2], 1e-3)) -
+                                                     np.log(truth[:, 2])) ** 2))),
+            "orientation_median_deg": float(np.median(ang))}
+
+
+def learned_comparison(dev, train_signals=20_000_000, lm_targets=1_000_000, epochs=2,
+                       n=1_000_000):
+    """Network-initialised vs grid-initialised NODDI-Watson fits of the same
+    n voxels (SNR 20) on the same GPU, each LM -> MCMC (1250 + 1250, every
+    25th). The network (288 -> 256 -> 256 -> 256 -> 12, BF16 tensor cores)
+    is trained first on train_signals synthetic signals (SNR U(10,50)) plus
+    lm_targets grid-search + LM fits. The surrogate path's time includes the
+    network, its LM, the refit judge (goodness of fit against the variance
+    of each voxel's b = 0 signals) and the grid search + LM refit of the
+    voxels it flags. Since both paths fit every voxel here, the audit
+    compares their LM costs voxel by voxel (outside the timing)."""
     import torch
     from cudimot_gb300 import capi, synth
     from cudimot_gb300.learned import LearnedInit
@@ -458,15 +498,14 @@ def bench_learned(a, dev):
     li = LearnedInit(MODEL, cfp, grid=synth.WATSON_GRID, seed=8219, device=dev)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    x, tg = li.make_training_set(a.train_signals, a.lm_targets)
+    x, tg = li.make_training_set(train_signals, lm_targets)
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
-    li.train(x, tg, epochs=a.epochs, batch=4096)
+    li.train(x, tg, epochs=epochs, batch=4096)
     n_train = x.shape[0]
     del x, tg
-    steps = a.epochs * (n_train // 4096)
+    steps = epochs * (n_train // 4096)
     flop_sample = 2 * sum(d0 * d1 for d0, d1 in zip(li.net.dims()[:-1], li.net.dims()[1:]))
-    n = a.eval_voxels
     d = li.synth(n, seed=4242, snr=(20.0, 20.0), meas=True)
     meas, s0, truth = d["meas"], d["s0"], d["params"].cpu().numpy()
     _, _, _, th, ph = synth.dti_init(meas.cpu().numpy(), cfp)
@@ -497,63 +536,73 @@ def bench_learned(a, dev):
     wl.levmar(meas[:w], wp, li.cfp, s0[:w])
     wsamp = torch.zeros(w, 5, 1, dtype=torch.float64, device=dev)
     wl.mcmc(meas[:w], wp, li.cfp, s0[:w], wsamp)
-    li.fit(meas[:w].contiguous(), s0[:w].contiguous(), wcfg, wsamp,
-           plain_cost=torch.zeros(w, dtype=torch.float64, device=dev), margin=0.0)
+    li.fit(meas[:w].contiguous(), s0[:w].contiguous(), wcfg, wsamp)
+    lm_plain = torch.empty(n, 5, dtype=torch.float64, device=dev)
+    lm_sur = torch.empty_like(lm_plain)
     torch.cuda.synchronize()
-    # grid-initialised path: GS -> LM | its cost (the refit yardstick) | MCMC
-    with ClockSampler(dev.index or 0) as clk:
-        p = init.clone()
-        e = [ev() for _ in range(6)]
-        e[0].record(st)
-        plain.gridsearch(meas, p, li.cfp, s0)
-        e[4].record(st)
-        plain.levmar(meas, p, li.cfp, s0)
-        e[1].record(st)
-        plain_cost = li.cost(meas, p, s0)
-        e[2].record(st)
-        plain.mcmc(meas, p, li.cfp, s0, sp)
-        e[3].record(st)
-        torch.cuda.synchronize()
-        t_plain = e[0].elapsed_time(e[1]) + e[2].elapsed_time(e[3])
-        plain_ms = {"gridsearch": e[0].elapsed_time(e[4]), "levmar": e[4].elapsed_time(e[1]),
-                    "mcmc": e[2].elapsed_time(e[3])}
-        lm_it_plain = plain.stats().lm_iterations / n
-        # network-initialised path: network -> LM -> refit -> MCMC
-        q = None
-        f0, f1 = ev(), ev()
-        f0.record(st)
-        q, info = li.fit(meas, s0, fit_cfg, ss, plain_cost=plain_cost, margin=0.01, ctx=ctx)
-        f1.record(st)
-        torch.cuda.synchronize()
-        t_sur = f0.elapsed_time(f1)
+    # grid-initialised path: GS -> LM -> MCMC
+    p = init.clone()
+    e = [ev() for _ in range(4)]
+    e[0].record(st)
+    plain.gridsearch(meas, p, li.cfp, s0)
+    e[1].record(st)
+    plain.levmar(meas, p, li.cfp, s0)
+    e[2].record(st)
+    lm_plain.copy_(p)
+    plain.mcmc(meas, p, li.cfp, s0, sp)
+    e[3].record(st)
+    torch.cuda.synchronize()
+    plain_ms = {"gridsearch": e[0].elapsed_time(e[1]), "levmar": e[1].elapsed_time(e[2]),
+                "mcmc": e[2].elapsed_time(e[3])}
+    t_plain = e[0].elapsed_time(e[3])
+    lm_it_plain = plain.stats().lm_iterations / n
+    # network-initialised path: network -> LM -> judge -> refit -> MCMC
+    f0, f1 = ev(), ev()
+    f0.record(st)
+    _, info = li.fit(meas, s0, fit_cfg, ss, ctx=ctx, keep_lm=lm_sur)
+    f1.record(st)
+    torch.cuda.synchronize()
+    t_sur = f0.elapsed_time(f1)
+    # audit: the surrogate path's LM cost against the plain path's, per voxel
+    c_plain = li.cost(meas, lm_plain, s0).cpu().numpy()
+    c_sur = li.cost(meas, lm_sur, s0).cpu().numpy()
+    rel = (c_sur - c_plain) / c_plain
     gp, gs_ = sp.cpu().numpy().mean(2), ss.cpu().numpy().mean(2)
+    return {"workload": "learned_init_noddi_watson", "nvox": n, "nmeas": 288, "snr": 20,
+            "nburn": NBURN, "njumps": NJUMPS, "sampleevery": SE,
+            "network": "288-256-256-256-12 GELU, bf16 tensor cores",
+            "surrogate_init": {"value": n / (t_sur / 1e3), "ms": t_sur, "stages_ms": info["ms"],
+                               "lm_iterations_per_voxel": ctx[0].stats().lm_iterations / n,
+                               "judge": "LM cost > (nmeas - 5) var(b=0 signals) F.ppf(0.99)",
+                               "refit_voxels": info["refit"],
+                               "param_error": param_error(gs_, truth)},
+            "grid_init": {"value": n / (t_plain / 1e3), "ms": t_plain, "stages_ms": plain_ms,
+                          "lm_iterations_per_voxel": lm_it_plain,
+                          "param_error": param_error(gp, truth)},
+            "speedup": t_plain / t_sur,
+            "audit_lm_cost_vs_grid_init": {
+                "voxels_worse_by_1pct": int(np.sum(rel > 0.01)),
+                "voxels_better_by_1pct": int(np.sum(rel < -0.01)),
+                "median_rel": float(np.median(rel)), "max_rel": float(rel.max())},
+            "training": {"signals": int(n_train), "epochs": epochs, "steps": int(steps),
+                         "seconds": li.train_seconds, "data_seconds": t_data,
+                         "tflops": 3 * flop_sample * steps * 4096 / li.train_seconds / 1e12,
+                         "loss_first": li.history[0][1], "loss_last": li.history[-1][1]}}
 
-    def err(m):
-        ang = np.degrees(np.arccos(np.clip(np.abs(
-            np.sin(m[:, 3]) * np.sin(truth[:, 3]) * np.cos(m[:, 4] - truth[:, 4]) +
-            np.cos(m[:, 3]) * np.cos(truth[:, 3])), 0, 1)))
-        return {"fiso_rmse": float(np.sqrt(np.mean((m[:, 0] - truth[:, 0]) ** 2))),
-                "fintra_rmse": float(np.sqrt(np.mean((m[:, 1] - truth[:, 1]) ** 2))),
-                "log_kappa_rmse": float(np.sqrt(np.mean((np.log(np.maximum(m[:, 2], 1e-3)) -
-                                                          np.log(truth[:, 2])) ** 2))),
-                "orientation_median_deg": float(np.median(ang))}
 
-    line = base_line(METRIC, n / (t_sur / 1e3), "voxels/s", a, t_sur,
-                     {"workload": "learned_init_noddi_watson", "model": MODEL, "nvox": n,
-                      "nmeas": 288, "nburn": NBURN, "njumps": NJUMPS, "sampleevery": SE,
-                      "refit_margin": 0.01, "network": "288-256-256-256-12 GELU, bf16",
-                      "l2": "inputs larger than L2 (no flush)"},
-                     clk.summary(),
-                     grid_init={"value": n / (t_plain / 1e3), "ms": t_plain, "stages_ms": plain_ms,
-                                "lm_iterations_per_voxel": lm_it_plain, "param_error": err(gp)},
-                     surrogate_init={"value": n / (t_sur / 1e3), "ms": t_sur,
-                                     "stages_ms": info["ms"],
-                                     "lm_iterations_per_voxel": ctx[0].stats().lm_iterations / n,
-                                     "param_error": err(gs_), "refit_voxels": info["refit"]},
-                     training={"signals": int(n_train), "epochs": a.epochs, "steps": int(steps),
-                               "seconds": li.train_seconds, "data_seconds": t_data,
-                               "tflops": 3 * flop_sample * steps * 4096 / li.train_seconds / 1e12,
-                               "loss_first": li.history[0][1], "loss_last": li.history[-1][1]})
+def bench_learned(a, dev):
+    """The learned-initialiser comparison (learned_comparison) as its own line."""
+    with ClockSampler(dev.index or 0) as clk:
+        res = learned_comparison(dev, a.train_signals, a.lm_targets, a.epochs, a.eval_voxels)
+    sur = res["surrogate_init"]
+    line = base_line(METRIC, sur["value"], "voxels/s", a, sur["ms"],
+                     {k: res[k] for k in ("workload", "nvox", "nmeas", "snr", "nburn", "njumps",
+                                          "sampleevery", "network")} |
+                     {"l2": "inputs larger than L2 (no flush)"},
+                     clk.summary(), **{k: v for k, v in res.items() if k in (
+                         "surrogate_init", "grid_init", "speedup", "audit_lm_cost_vs_grid_init",
+                         "training")})
+    line["steps"], line["warmup"] = 1, 1
     print(json.dumps(line))
 
 
@@ -821,30 +870,32 @@ def main():
 
     if rank != 0:
         return
-    peaks = measured_peaks()
     fl = flop_model()
     roofline = None
     fp32_peak = fp32_peak_tflops(dev)
     if fl is not None and fp32_peak:
         per_voxel_mcmc = fl["mcmc"]
         achieved = per_voxel_mcmc * nvox / (mcmc_ms / 1e3) / 1e12
+        traffic, traffic_src = measured_traffic(
+            "cdm_mcmc_kernel", {"nvox": nvox, "nburn": NBURN, "njumps": NJUMPS, "sampleevery": SE,
+                                "rician": False})
         roofline = {"bound": "fp32", "kernel": "cdm_mcmc_kernel", "achieved": achieved,
                     "peak": fp32_peak["tflops"], "unit": "TFLOP/s", "frac": achieved / fp32_peak["tflops"],
-                    "peak_source": fp32_peak["source"], "traffic": profiled_traffic(),
-                    "traffic_source": "profiles/mcmc_kernel_noddi_watson.md (ncu capture of the full 200k-voxel, 1250+1250-jump launch)",
+                    "peak_source": fp32_peak["source"], "traffic": traffic,
+                    "traffic_source": traffic_src,
                     "flop_per_voxel": per_voxel_mcmc, "launch_ms": mcmc_ms}
+    post = d_samples.mean(2).cpu().numpy()
     line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 model / f64 sums", "data": "synthetic (seeded NODDI-Watson, SNR 20)",
-            "config": {"workload": "noddi_watson_gs_lm_mcmc", "model": MODEL, "nvox_per_gpu": nvox,
-                       "nmeas": 288, "grid_combs": 968, "nburn": NBURN, "njumps": NJUMPS,
-                       "sampleevery": SE, "l2": "inputs larger than L2 (no flush)",
-                       "parallelism": f"voxel shards x{world}"},
+            "config": headline_config(nvox, world),
             "gpu_launches": gpu_launches_per_step(cfg) * a.steps,
             "clocks": clk.summary(),
             # cdm_fit clears the counters, so they hold the last step alone
             "lm_iterations_per_voxel": stats.lm_iterations / max(nvox, 1),
             "gs_recheck_voxels": stats.gs_recheck_voxels,
+            # posterior means of the last step against the true parameters
+            "param_error": param_error(post, truth),
             "roofline": roofline, "e2e": e2e}
     if os.environ.get("CDM_BENCH_CPU", "1") != "0":
         n = a.cpu_sample or 4096
@@ -852,22 +903,31 @@ def main():
         v, threads, dt = cpu_baseline(cfp, meas, fixp, init, n, cfg)
         line["cpu_baseline"] = {"value": v, "unit": "voxels/s", "cores": threads, "kind": "port",
                                 "sample": f"{n} voxels of this workload, grid search -> LM -> MCMC, "
-                                          f"FP64 CPU oracle, {dt:.1f} s"}
+                                          f"FP64 CPU oracle, {dt:.1f} s",
+                                "plugin": CPU_PLUGIN_NOTE}
         nf = max(n // 2, 1)
         vf, _, dtf = cpu_baseline(cfp, meas, fixp, init, nf, cfg, prec=1)
         line["cpu_baseline"]["float"] = {
             "value": vf, "unit": "voxels/s", "cores": threads,
             "sample": f"{nf} voxels, the same CPU oracle with T = float, {dtf:.1f} s"}
+    part = min(12_800, nvox)
     if os.environ.get("CDM_BENCH_REFK", "1") != "0":
-        line["reference_kernels"] = reference_kernels_leg(cfp, meas, fixp, init, cfg, dev)
+        line["reference_kernels"] = reference_kernels_leg(cfp, meas, fixp, init, cfg, dev, truth,
+                                                          post, n=part, n_float=part)
+    if os.environ.get("CDM_BENCH_DROPIN", "1") != "0":
+        line["dropin_unchanged_plugin"] = dropin_leg(cfp, meas, fixp, init, truth, post, dev, part)
+    if os.environ.get("CDM_BENCH_LEARNED", "1") != "0":
+        line["surrogate_vs_grid"] = learned_comparison(dev)
     print(json.dumps(line))
 
 
-def reference_kernels_leg(cfp, meas, fixp, init, cfg, dev, n=2048, n_float=2048):
+def reference_kernels_leg(cfp, meas, fixp, init, cfg, dev, truth, post, n=12_800, n_float=12_800):
     """CUDIMOT's own GridSearch/LM/MCMC kernels (unmodified sources compiled
-    for sm_103a) on the first voxels of this workload, same GPU; wall time of
-    the three stages. T = double as the plugins ship (n voxels), and CUDIMOT's
-    float instantiation of the same kernels (n_float voxels)."""
+    for sm_103a) on the first n voxels of this workload (one of CUDIMOT's
+    12,800-voxel parts, gridOptions.h SIZE_PART), same GPU: wall time of the
+    three stages, and the posterior means' error against the truth beside
+    this library's on the same voxels. T = double as the plugins ship, and
+    CUDIMOT's float instantiation of the same kernels."""
     import time
     import torch
     try:
@@ -890,23 +950,69 @@ def reference_kernels_leg(cfp, meas, fixp, init, cfg, dev, n=2048, n_float=2048)
         ref.levmar(cfg, m, p, c, f)
         ref.mcmc(cfg, m, p, c, f, s)
         torch.cuda.synchronize()
-        return time.perf_counter() - t0, s
+        return time.perf_counter() - t0, s.double().mean(2).cpu().numpy()
 
-    dt, _ = run(n, torch.float64)
-    out = {"value": n / dt, "unit": "voxels/s", "seconds": dt,
-           "sample": f"first {n} voxels of this workload, grid search -> LM -> MCMC, "
-                     "one warp per voxel as CUDIMOT launches them, T = double"}
+    out = {"library_param_error_same_voxels": param_error(post[:n], truth[:n])}
+    dt, pm = run(n, torch.float64)
+    out.update({"value": n / dt, "unit": "voxels/s", "seconds": dt,
+                "sample": f"first {n} voxels of this workload (one {n}-voxel part), grid search -> "
+                          "LM -> MCMC, one warp per voxel as CUDIMOT launches them, T = double",
+                "param_error": param_error(pm, truth[:n])})
     try:
         k = min(n_float, len(meas))
-        dtf, sf = run(k, torch.float32)
-        means = sf.mean(2)
+        dtf, pmf = run(k, torch.float32)
+        fin = np.isfinite(pmf).all(1)
         out["float"] = {"value": k / dtf, "unit": "voxels/s", "seconds": dtf,
                         "sample": f"first {k} voxels, CUDIMOT's float instantiation "
                                   "(MyType = float) of the same kernels",
-                        "finite_posterior_means": float(torch.isfinite(means).all(1).float().mean())}
+                        "finite_posterior_means": float(fin.mean()),
+                        "param_error": param_error(pmf[fin], truth[:k][fin])}
     except Exception as e:  # noqa: BLE001
         out["float"] = {"unavailable": f"{type(e).__name__}: {e}"}
     return out
+
+
+def dropin_leg(cfp, meas, fixp, init, truth, post, dev, n=12_800):
+    """A drop-in user's throughput: this library built from CUDIMOT's
+    unchanged NODDI-Watson plugin (split build, plugin evaluated in double:
+    its closed forms need it) on the first n voxels of this workload, grid
+    search -> LM -> MCMC through cdm_fit, and the posterior means' error
+    against the truth."""
+    import torch
+    from cudimot_gb300 import capi, synth
+    try:
+        from oracle import build_dropin
+        if not build_dropin.available(MODEL, "double"):
+            return {"unavailable": "device module not compiled (CUDIMOT's tree absent at build time)"}
+        errs = build_dropin.build_all()
+        if errs:
+            return {"unavailable": "host half did not build: " + next(iter(errs.values()))[-300:]}
+        cfg = capi.model_cfg(MODEL, grid=synth.WATSON_GRID, run_mcmc=1, nburn=NBURN,
+                             njumps=NJUMPS, sampleevery=SE, iter_levmar=200)
+        lib = capi.Cudimot(MODEL, cfg, path=build_dropin.lib_path(MODEL, "double"))
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
+    m, c, f, p0 = t(meas[:n]), t(cfp), t(fixp[:n]), t(init[:n])
+    s = torch.zeros(n, 5, NJUMPS // SE, dtype=torch.float64, device=dev)
+    w = min(n, 256)  # kernels loaded on a small fit first
+    pw = p0[:w].clone()
+    lib.fit(m[:w].contiguous(), pw, c, f[:w].contiguous(), s[:w].contiguous())
+    torch.cuda.synchronize()
+    p = p0.clone()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    lib.fit(m, p, c, f, s)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    pm = s.mean(2).cpu().numpy()
+    return {"value": n / (ms / 1e3), "unit": "voxels/s", "ms": ms,
+            "sample": f"first {n} voxels of this workload, grid search -> LM -> MCMC (cdm_fit)",
+            "plugin": "CUDIMOT's mymodels/NODDI_Watson unchanged, evaluated in double",
+            "param_error": param_error(pm, truth[:n]),
+            "library_param_error_same_voxels": param_error(post[:n], truth[:n])}
 
 
 def gpu_launches_per_step(cfg):

@@ -2,6 +2,8 @@
 
     python -m cudimot_gb300.build                 # every plugin in mymodels/
     python -m cudimot_gb300.build --model-dir DIR # any CUDIMOT plugin directory
+    python -m cudimot_gb300.build --model-dir DIR --split OUT  # device half only
+    python -m cudimot_gb300.build --module-host OUT            # host half of a split build
 
 Like CUDIMOT's Makefile (one binary per mymodels/<Model>), each model plugin
 is compiled into its own library: the generic kernels include the plugin's
@@ -9,6 +11,16 @@ unchanged modelparameters.h / modelfunctions.h / modelparameters.cc. The
 plugin's CFP/FixP block sizes are read from modelparameters.cc into a
 generated header so the kernels can size their register arrays at compile
 time. Libraries land in cudimot_gb300/_lib/ (git-ignored).
+
+Split build: the device half (every kernel, cdm_module.cu) is compiled
+against the plugin into a cubin, next to a generated description of the
+model (sizes and hooks, cdm_model_desc.h); the host half (cdm_model.cu with
+CDM_MODULE_HOST) is compiled later from the description alone and embeds the
+cubin. The two halves can be built on different machines: the plugin's
+sources are needed only for the first.
+
+--eval double (-DCDM_EVAL_DOUBLE) evaluates the plugin in double precision:
+for plugins whose closed forms are not usable in single precision.
 """
 from __future__ import annotations
 
@@ -57,10 +69,9 @@ def block_sizes(model_dir):
 
 
 def sources():
-    files = [os.path.join(CSRC, "cdm_model.cu"), os.path.join(CSRC, "host", "cdm_host.cpp"),
-             os.path.join(CSRC, "host", "cdm_host.h"), os.path.join(CSRC, "host", "cdm_flops.cpp"),
+    files = [os.path.join(CSRC, "cdm_model.cu"), os.path.join(CSRC, "cdm_module.cu"),
              os.path.join(ROOT, "include", "cudimot_gb300.h")]
-    for sub in ("prelude", "kernels"):
+    for sub in ("prelude", "kernels", "host"):
         d = os.path.join(CSRC, sub)
         files += [os.path.join(d, f) for f in sorted(os.listdir(d))]
     return files
@@ -80,11 +91,45 @@ def lib_path(name):
     return os.path.join(LIBDIR, f"libcudimot_{name}.so")
 
 
-def build_model(model_dir, name=None, extra_flags=(), verbose=False, force=False):
+def _write_sizes(gen, sizes):
+    with open(os.path.join(gen, "cdm_model_sizes.h"), "w") as f:
+        f.write("// generated from modelparameters.cc by cudimot_gb300/build.py\n#pragma once\n")
+        f.write(f"#define CDM_CFP_TSIZE {sum(sizes['CFP_size'])}\n")
+        f.write(f"#define CDM_FIXP_TSIZE {sum(sizes['FixP_size'])}\n")
+
+
+def _includes(gen, model_dir):
+    return ["-I", os.path.join(CSRC, "prelude"), "-I", os.path.join(CSRC, "kernels"),
+            "-I", os.path.join(CSRC, "host"), "-I", os.path.join(ROOT, "include"), "-I", gen,
+            "-I", model_dir]
+
+
+def _build_flops(model_dir, gen, fl):
+    """Operation-count build of the plugin (host g++; roofline FLOP basis and
+    the model description of split builds)."""
+    cmd = ["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-w",
+           "-I", os.path.join(CSRC, "prelude"), "-I", os.path.join(CSRC, "host"), "-I", gen,
+           "-I", model_dir, os.path.join(CSRC, "host", "cdm_flops.cpp"), "-o", fl + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return (r.stdout + r.stderr)[-6000:]
+    os.replace(fl + ".tmp", fl)
+    return None
+
+
+def eval_flags(eval_type):
+    if eval_type in (None, "float"):
+        return []
+    if eval_type == "double":
+        return ["-DCDM_EVAL_DOUBLE"]
+    raise ValueError("eval must be 'float' or 'double'")
+
+
+def build_model(model_dir, name=None, extra_flags=(), verbose=False, force=False, eval_type=None):
     model_dir = os.path.abspath(model_dir)
     name = name or os.path.basename(model_dir.rstrip("/"))
     flags = ["-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "-shared",
-             "-Xcompiler", "-ffp-contract=off"] + list(extra_flags)
+             "-Xcompiler", "-ffp-contract=off"] + eval_flags(eval_type) + list(extra_flags)
     out = lib_path(name)
     stamp = out + ".sha256"
     dig = digest(model_dir, flags)
@@ -93,19 +138,11 @@ def build_model(model_dir, name=None, extra_flags=(), verbose=False, force=False
     gen = os.path.join(GENDIR, name)
     os.makedirs(gen, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
-    sizes = block_sizes(model_dir)
-    with open(os.path.join(gen, "cdm_model_sizes.h"), "w") as f:
-        f.write("// generated from modelparameters.cc by cudimot_gb300/build.py\n#pragma once\n")
-        f.write(f"#define CDM_CFP_TSIZE {sum(sizes['CFP_size'])}\n")
-        f.write(f"#define CDM_FIXP_TSIZE {sum(sizes['FixP_size'])}\n")
+    _write_sizes(gen, block_sizes(model_dir))
     # modelparameters.cc defines the MODEL:: size arrays the ABI reports.
     with open(os.path.join(gen, "cdm_model_params.cpp"), "w") as f:
         f.write('#include "modelparameters.cc"\n')
-    cmd = [nvcc_path()] + flags + [
-        f'-DCDM_MODEL_NAME="{name}"',
-        "-I", os.path.join(CSRC, "prelude"), "-I", os.path.join(CSRC, "kernels"),
-        "-I", os.path.join(CSRC, "host"), "-I", os.path.join(ROOT, "include"), "-I", gen,
-        "-I", model_dir,
+    cmd = [nvcc_path()] + flags + [f'-DCDM_MODEL_NAME="{name}"'] + _includes(gen, model_dir) + [
         os.path.join(CSRC, "cdm_model.cu"), os.path.join(CSRC, "host", "cdm_host.cpp"),
         os.path.join(gen, "cdm_model_params.cpp"),
         "-o", out + ".tmp"]
@@ -117,17 +154,116 @@ def build_model(model_dir, name=None, extra_flags=(), verbose=False, force=False
     os.replace(out + ".tmp", out)
     if verbose:
         sys.stderr.write(r.stdout + r.stderr)
-    # operation-count build of the same plugin (host, for the roofline)
-    fl = os.path.join(LIBDIR, f"libcdm_flops_{name}.so")
-    cmd = ["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-w",
-           "-I", os.path.join(CSRC, "prelude"), "-I", os.path.join(CSRC, "host"), "-I", gen,
-           "-I", model_dir, os.path.join(CSRC, "host", "cdm_flops.cpp"), "-o", fl + ".tmp"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        return fl, (r.stdout + r.stderr)[-6000:]
-    os.replace(fl + ".tmp", fl)
+    err = _build_flops(model_dir, gen, os.path.join(LIBDIR, f"libcdm_flops_{name}.so"))
+    if err:
+        return os.path.join(LIBDIR, f"libcdm_flops_{name}.so"), err
     with open(stamp, "w") as f:
         f.write(dig)
+    return out, None
+
+
+def describe(flops_lib, sizes, name, eval_type=None):
+    """Text of cdm_model_desc.h from the host build of the plugin."""
+    import ctypes
+    lib = ctypes.CDLL(flops_lib)
+    buf = ctypes.create_string_buffer(1 << 14)
+    n = lib.cdm_describe(buf, len(buf))
+    if n < 0:
+        raise RuntimeError("model description does not fit")
+    pad = lambda v: "{" + ", ".join(str(x) for x in (v or [0])) + "}"  # noqa: E731
+    txt = ("// generated by cudimot_gb300/build.py from the plugin: the host half of a\n"
+           "// split build is compiled with this instead of the plugin\n#pragma once\n")
+    txt += buf.value.decode()
+    txt += f"#define CDM_CFP_SIZES {pad(sizes['CFP_size'])}\n"
+    txt += f"#define CDM_FIXP_SIZES {pad(sizes['FixP_size'])}\n"
+    if eval_type == "double":
+        txt += "#define CDM_EVAL_DOUBLE 1\n"
+    txt += f'#define CDM_SPLIT_MODEL_NAME "{name}"\n'
+    return txt
+
+
+def split_device(model_dir, outdir, name=None, eval_type=None, force=False):
+    """Device half of a split build: outdir/cdm_module.cubin and
+    outdir/cdm_model_desc.h from the plugin in model_dir."""
+    model_dir = os.path.abspath(model_dir)
+    outdir = os.path.abspath(outdir)
+    name = name or os.path.basename(model_dir.rstrip("/"))
+    os.makedirs(outdir, exist_ok=True)
+    flags = ["-O3", "-std=c++17", ARCH, "-lineinfo", "-cubin"] + eval_flags(eval_type)
+    cubin = os.path.join(outdir, "cdm_module.cubin")
+    stamp = cubin + ".sha256"
+    dig = digest(model_dir, flags + [name])
+    if not force and os.path.exists(cubin) and os.path.exists(stamp) and open(stamp).read() == dig:
+        return cubin, None
+    gen = os.path.join(outdir, "gen")
+    os.makedirs(gen, exist_ok=True)
+    sizes = block_sizes(model_dir)
+    _write_sizes(gen, sizes)
+    fl = os.path.join(gen, "libcdm_describe.so")
+    err = _build_flops(model_dir, gen, fl)
+    if err:
+        return fl, err
+    with open(os.path.join(outdir, "cdm_model_desc.h"), "w") as f:
+        f.write(describe(fl, sizes, name, eval_type))
+    cmd = [nvcc_path()] + flags + _includes(gen, model_dir) + [
+        os.path.join(CSRC, "cdm_module.cu"), "-o", cubin + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return cubin, (r.stdout + r.stderr)[-6000:]
+    os.replace(cubin + ".tmp", cubin)
+    with open(stamp, "w") as f:
+        f.write(dig)
+    return cubin, None
+
+
+def check_plugin(model_dir, eval_type=None, lanes=2):
+    """Compile check of a plugin: the device module with one lane count
+    (every kernel, cubin discarded). Returns None or the compiler's error."""
+    import tempfile
+    model_dir = os.path.abspath(model_dir)
+    with tempfile.TemporaryDirectory() as gen:
+        _write_sizes(gen, block_sizes(model_dir))
+        cmd = [nvcc_path(), "-O3", "-std=c++17", ARCH, "-cubin", f"-DCDM_CHECK_LANES={lanes}"] + \
+            eval_flags(eval_type) + _includes(gen, model_dir) + \
+            [os.path.join(CSRC, "cdm_module.cu"), "-o", os.path.join(gen, "check.cubin")]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+    return None if r.returncode == 0 else (r.stdout + r.stderr)[-6000:]
+
+
+def split_lib_path(outdir):
+    return os.path.join(os.path.abspath(outdir), "libcudimot_split.so")
+
+
+def split_host(outdir, force=False):
+    """Host half of a split build: outdir/libcudimot_split.so from
+    outdir/cdm_model_desc.h, embedding outdir/cdm_module.cubin."""
+    outdir = os.path.abspath(outdir)
+    cubin = os.path.join(outdir, "cdm_module.cubin")
+    desc = os.path.join(outdir, "cdm_model_desc.h")
+    out = split_lib_path(outdir)
+    deps = [cubin, desc, os.path.join(CSRC, "cdm_model.cu"), os.path.join(CSRC, "host", "cdm_host.cpp")]
+    deps += [os.path.join(CSRC, "host", f) for f in os.listdir(os.path.join(CSRC, "host"))]
+    deps += [os.path.join(CSRC, "kernels", "cdm_args.h"), os.path.join(ROOT, "include", "cudimot_gb300.h")]
+    if not (os.path.exists(cubin) and os.path.exists(desc)):
+        return out, f"{outdir} holds no device module (cdm_module.cubin, cdm_model_desc.h)"
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= max(map(os.path.getmtime, deps)):
+        return out, None
+    name = re.search(r'CDM_SPLIT_MODEL_NAME "([^"]*)"', open(desc).read())
+    image = os.path.join(outdir, "cdm_module_image.cpp")
+    with open(image, "w") as f:
+        f.write("// generated by cudimot_gb300/build.py: the device module, embedded\n")
+        f.write('__asm__(".section .rodata\\n.balign 64\\n.globl cdm_module_image\\n'
+                'cdm_module_image:\\n.incbin \\"' + cubin + '\\"\\n.byte 0\\n.previous\\n");\n')
+    cmd = [nvcc_path(), "-O3", "-std=c++17", ARCH, "-Xcompiler", "-fPIC", "-shared",
+           "-DCDM_MODULE_HOST", f'-DCDM_MODEL_NAME="{name.group(1) if name else "model"}"',
+           "-I", os.path.join(CSRC, "kernels"), "-I", os.path.join(CSRC, "host"),
+           "-I", os.path.join(ROOT, "include"), "-I", outdir,
+           os.path.join(CSRC, "cdm_model.cu"), os.path.join(CSRC, "host", "cdm_host.cpp"), image,
+           "-o", out + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return out, (r.stdout + r.stderr)[-6000:]
+    os.replace(out + ".tmp", out)
     return out, None
 
 
@@ -238,10 +374,35 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--models", nargs="*", default=None)
     ap.add_argument("--model-dir", action="append", default=[])
+    ap.add_argument("--eval", choices=["float", "double"], default=None,
+                    help="plugin evaluation precision of --model-dir builds (default float)")
+    ap.add_argument("--split", default=None,
+                    help="with one --model-dir: build only the device half into this directory")
+    ap.add_argument("--module-host", default=None,
+                    help="build the host half of a split build from this directory")
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--force", action="store_true")
     a = ap.parse_args()
-    errs = build_all(a.models, a.model_dir, verbose=a.verbose, force=a.force)
+    if a.split or a.module_host:
+        errs = {}
+        if a.split:
+            if len(a.model_dir) != 1:
+                ap.error("--split takes exactly one --model-dir")
+            out, err = split_device(a.model_dir[0], a.split, eval_type=a.eval, force=a.force)
+            if err:
+                errs[out] = err
+        if a.module_host and not errs:
+            out, err = split_host(a.module_host, force=a.force)
+            if err:
+                errs[out] = err
+    elif a.eval:
+        errs = {}
+        for d in a.model_dir:
+            out, err = build_model(d, None, (), a.verbose, a.force, eval_type=a.eval)
+            if err:
+                errs[out] = err
+    else:
+        errs = build_all(a.models, a.model_dir, verbose=a.verbose, force=a.force)
     for k, v in errs.items():
         print(f"FAILED {k}\n{v}", file=sys.stderr)
     sys.exit(1 if errs else 0)

@@ -66,6 +66,7 @@ class CfgStruct(C.Structure):
         ("lanes_gridsearch", C.c_int),
         ("lanes_levmar", C.c_int),
         ("lanes_mcmc", C.c_int),
+        ("first_voxel", C.c_int64),
     ]
 
 
@@ -176,6 +177,12 @@ MODEL_LIMITS = {
                                   4: (-10000.0, 10000.0), 5: (-10000.0, 10000.0),
                                   6: (-100.0, 100.0)},
                           priors={}),
+    # two of CUDIMOT's plugins used unchanged (no copy in mymodels/)
+    "toymodel": dict(bounds={0: (None, None), 1: (None, None)}, priors={}),
+    "Ball_2_Sticks_1Shell_SSFP": dict(
+        bounds={0: (1e-9, 0.01), 1: (0.0, 1.0), 2: (-100.0, 100.0), 3: (-100.0, 100.0),
+                4: (0.0, 1.0), 5: (-100.0, 100.0), 6: (-100.0, 100.0), 7: (0.0, None)},
+        priors={2: (SINPRIOR,), 4: (ARDPRIOR, 1.0), 5: (SINPRIOR,)}),
 }
 
 
@@ -257,9 +264,10 @@ def lib_path(model: str) -> str:
     return os.path.join(LIBDIR, f"libcudimot_{model}.so")
 
 
-def load_library(model: str):
-    """Load libcudimot_<model>.so; raises if it has not been built."""
-    path = lib_path(model)
+def load_library(model: str, path: str = None):
+    """Load libcudimot_<model>.so (or the library at path); raises if it has
+    not been built."""
+    path = path or lib_path(model)
     if not os.path.exists(path):
         raise CdmError(f"{path} is not built (python -m cudimot_gb300.build)")
     lib = C.CDLL(path)
@@ -289,9 +297,9 @@ class Cudimot:
     Stage calls take torch CUDA float64 tensors in CUDIMOT's layouts and run
     asynchronously on the current torch stream."""
 
-    def __init__(self, model: str, cfg: Cfg):
+    def __init__(self, model: str, cfg: Cfg, path: str = None):
         self.model = model
-        self.lib = load_library(model)
+        self.lib = load_library(model, path)
         self.info = ModelInfo()
         _check(self.lib, self.lib.cdm_get_model_info(C.byref(self.info)), "model info")
         self.cfg = cfg

@@ -21,11 +21,23 @@
 #include <string>
 #include <mutex>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "cdm_host.h"
 #include "cudimot_gb300.h"
 
+#include "cdm_kernels.h"
+#include "cdm_noalloc_scratch.h"
+
+#ifdef CDM_MODULE_HOST
+// Host half of a split build: the model's sizes and hooks come from the
+// description generated from the plugin; the kernels come from the device
+// module (cdm_module.cu) embedded in this library.
+#include "cdm_model_desc.h"
+#include "cdm_args.h"
+constexpr int kNH = kNP * (kNP + 1) / 2;
+#else
 #include "functions_gpu.h"
 #include "modelparameters.h"
 #include "macro_numerical.h"
@@ -39,6 +51,7 @@
 #include "cdm_mcmc.cuh"
 #include "cdm_postfit.cuh"
 #include "cdm_synth.cuh"
+#endif
 
 #ifndef CDM_MODEL_NAME
 #define CDM_MODEL_NAME "model"
@@ -78,6 +91,203 @@ cdm_status dev_alloc(T** p, size_t* cap, size_t n) {
 }
 
 int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+// Block sizes of the plugin's CFP and FixP arrays (MODEL::CFP_size /
+// FixP_size of modelparameters.cc), padded so that a model without blocks
+// still has an array.
+#ifdef CDM_MODULE_HOST
+const int kCfpBlocks[] = CDM_CFP_SIZES;
+const int kFixpBlocks[] = CDM_FIXP_SIZES;
+#else
+const int* const kCfpBlocks = MODEL::CFP_size;
+const int* const kFixpBlocks = MODEL::FixP_size;
+#endif
+
+// ------------------------------------------------------------------ kernels
+// Every launch goes through cudaLaunchKernel with the kernel's address
+// (normal build) or its handle in the embedded device module (split build).
+#ifdef CDM_MODULE_HOST
+extern "C" const unsigned char cdm_module_image[];
+
+struct module_state {
+  std::once_flag once;
+  cudaError_t err = cudaSuccess;
+  cudaLibrary_t lib = nullptr;
+  std::mutex mu;
+  const void* fn[CDM_K_COUNT][6] = {};
+};
+module_state g_module;
+
+cudaError_t module_library(cudaLibrary_t* lib) {
+  std::call_once(g_module.once, [] {
+    g_module.err = cudaLibraryLoadData(&g_module.lib, cdm_module_image, nullptr, nullptr, 0,
+                                       nullptr, nullptr, 0);
+  });
+  *lib = g_module.lib;
+  return g_module.err;
+}
+
+const void* kfn(int fam, int lanes) {
+  const bool laned = fam < CDM_K_NLANE_FAMILIES;
+  const int li = laned ? cdm_lane_index(lanes) : 0;
+  if (fam < 0 || fam >= CDM_K_COUNT || li < 0) return nullptr;
+  cudaLibrary_t lib = nullptr;
+  if (module_library(&lib) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lock(g_module.mu);
+  if (!g_module.fn[fam][li]) {
+    char name[64];
+    if (laned)
+      std::snprintf(name, sizeof(name), "cdm_k_%s_%d", cdm_kfam_name(fam), lanes);
+    else
+      std::snprintf(name, sizeof(name), "cdm_k_%s", cdm_kfam_name(fam));
+    cudaKernel_t k = nullptr;
+    if (cudaLibraryGetKernel(&k, lib, name) == cudaSuccess) g_module.fn[fam][li] = (const void*)k;
+  }
+  return g_module.fn[fam][li];
+}
+#else
+template <int Gw>
+const void* kfn_lanes(int fam) {
+  switch (fam) {
+    case CDM_K_GRIDSEARCH: return (const void*)cdm_gridsearch_kernel<Gw>;
+    case CDM_K_LEVMAR: return (const void*)cdm_levmar_kernel<Gw>;
+    case CDM_K_MCMC: return (const void*)cdm_mcmc_kernel<Gw, false>;
+    case CDM_K_MCMC_RICIAN: return (const void*)cdm_mcmc_kernel<Gw, true>;
+    case CDM_K_PACK_SIGNALS: return (const void*)cdm_pack_signals_kernel<Gw>;
+  }
+  return nullptr;
+}
+
+const void* kfn(int fam, int lanes) {
+  if (fam < CDM_K_NLANE_FAMILIES) {
+    switch (lanes) {
+      case 1: return kfn_lanes<1>(fam);
+      case 2: return kfn_lanes<2>(fam);
+      case 4: return kfn_lanes<4>(fam);
+      case 8: return kfn_lanes<8>(fam);
+      case 16: return kfn_lanes<16>(fam);
+      case 32: return kfn_lanes<32>(fam);
+    }
+    return nullptr;
+  }
+  switch (fam) {
+    case CDM_K_GS_RECHECK: return (const void*)cdm_gs_recheck_kernel;
+    case CDM_K_PREDICTED: return (const void*)cdm_predicted_kernel;
+    case CDM_K_BIC_AIC: return (const void*)cdm_bic_aic_kernel;
+    case CDM_K_COST: return (const void*)cdm_cost_kernel;
+    case CDM_K_SELECT_WORSE: return (const void*)cdm_select_worse_kernel;
+    case CDM_K_ROWS: return (const void*)cdm_rows_kernel;
+    case CDM_K_PREP_PROTOCOL: return (const void*)cdm_prep_protocol_kernel;
+    case CDM_K_PARAMS_TO_SAMPLES: return (const void*)cdm_params_to_samples_kernel;
+    case CDM_K_SYNTH: return (const void*)cdm_synth_kernel;
+#ifdef CDM_MLP_HEAD
+    case CDM_K_MLP_ENCODE: return (const void*)cdm_mlp_encode_kernel;
+    case CDM_K_MLP_DECODE: return (const void*)cdm_mlp_decode_kernel;
+#endif
+    case CDM_K_CLEAN_SIGNALS: return (const void*)cdm_clean_signals_kernel;
+    case CDM_K_WAIT_SELFTEST: return (const void*)cdm_wait_selftest_kernel;
+  }
+  return nullptr;
+}
+#endif
+
+cdm_status launch_argv(int fam, int lanes, dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       void** args) {
+  const void* fn = kfn(fam, lanes);
+  if (!fn)
+    return cdm_fail(CDM_CUDA_ERROR, std::string("kernel ") + cdm_kfam_name(fam) + " (" +
+                                        std::to_string(lanes) + " lanes) is not available");
+  CDM_CUDA(cudaLaunchKernel(fn, grid, block, args, smem, st));
+  return CDM_OK;
+}
+
+// One launch; every argument is passed by address, so each must already
+// have the exact type of the kernel's parameter (the typed wrappers below).
+template <class... A>
+cdm_status launch(int fam, int lanes, dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                  A... args) {
+  void* argv[] = {(void*)&args...};
+  return launch_argv(fam, lanes, grid, block, smem, st, argv);
+}
+
+cdm_status set_smem(int fam, int lanes, size_t bytes) {
+  if (bytes <= 48 * 1024) return CDM_OK;
+  const void* fn = kfn(fam, lanes);
+  if (!fn) return cdm_fail(CDM_CUDA_ERROR, std::string("kernel ") + cdm_kfam_name(fam) + " is not available");
+  CDM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return CDM_OK;
+}
+
+// Typed launches: the parameters are those of the kernels (cdm_postfit.cuh,
+// cdm_synth.cuh), so the argument blocks match them exactly.
+cdm_status k_prep_protocol(cudaStream_t st, const double* cfp, int nmeas, int nmeas_pad, float* p32,
+                           double* p64) {
+  return launch(CDM_K_PREP_PROTOCOL, 0, (nmeas_pad + 127) / 128, 128, 0, st, cfp, nmeas, nmeas_pad,
+                p32, p64);
+}
+cdm_status k_pack_signals(int lanes, int blocks, cudaStream_t st, const double* meas, int nvox,
+                          int nmeas, int nchunk, float* out) {
+  return launch(CDM_K_PACK_SIGNALS, lanes, blocks, 256, 0, st, meas, nvox, nmeas, nchunk, out);
+}
+cdm_status k_params_to_samples(int blocks, cudaStream_t st, const double* params, int nvox,
+                               double* samples) {
+  return launch(CDM_K_PARAMS_TO_SAMPLES, 0, blocks, 256, 0, st, params, nvox, samples);
+}
+cdm_status k_cost(int blocks, size_t smem, cudaStream_t st, cdm_post_args a, const double* params,
+                  double* cost) {
+  return launch(CDM_K_COST, 0, blocks, CDM_NT, smem, st, a, params, cost);
+}
+cdm_status k_select_worse(int blocks, cudaStream_t st, int n, const double* cost, const double* ref,
+                          double margin, int* idx, int* count) {
+  return launch(CDM_K_SELECT_WORSE, 0, blocks, 256, 0, st, n, cost, ref, margin, idx, count);
+}
+cdm_status k_rows(int blocks, cudaStream_t st, int nsel, const int* idx, int ncols,
+                  const double* src, double* dst, int scatter, double value) {
+  return launch(CDM_K_ROWS, 0, blocks, 256, 0, st, nsel, idx, ncols, src, dst, scatter, value);
+}
+cdm_status k_mlp_encode(int blocks, cudaStream_t st, const double* params, int n, float* t) {
+  return launch(CDM_K_MLP_ENCODE, 0, blocks, 256, 0, st, params, n, t);
+}
+cdm_status k_mlp_decode(int blocks, cudaStream_t st, const float* out, int ld, int n,
+                        double* params, double* prop_sd) {
+  return launch(CDM_K_MLP_DECODE, 0, blocks, 256, 0, st, out, ld, n, params, prop_sd);
+}
+cdm_status k_clean_signals(int blocks, cudaStream_t st, int nvox, int nmeas, double* meas) {
+  return launch(CDM_K_CLEAN_SIGNALS, 0, blocks, 256, 0, st, nvox, nmeas, meas);
+}
+cdm_status k_wait_selftest(cudaStream_t st, uint64_t limit_ns, int* err) {
+  return launch(CDM_K_WAIT_SELFTEST, 0, 1, 32, 0, st, limit_ns, err);
+}
+
+#ifndef CDM_MODULE_HOST
+// The typed launches above must match the kernels' parameter lists.
+template <class F, class G>
+constexpr bool cdm_same_sig = std::is_same<F, G>::value;
+static_assert(cdm_same_sig<decltype(&cdm_prep_protocol_kernel),
+                           void (*)(const double*, int, int, float*, double*)>, "prep_protocol");
+static_assert(cdm_same_sig<decltype(&cdm_pack_signals_kernel<1>),
+                           void (*)(const double*, int, int, int, float*)>, "pack_signals");
+static_assert(cdm_same_sig<decltype(&cdm_params_to_samples_kernel),
+                           void (*)(const double*, int, double*)>, "params_to_samples");
+static_assert(cdm_same_sig<decltype(&cdm_cost_kernel),
+                           void (*)(cdm_post_args, const double*, double*)>, "cost");
+static_assert(cdm_same_sig<decltype(&cdm_select_worse_kernel),
+                           void (*)(int, const double*, const double*, double, int*, int*)>,
+              "select_worse");
+static_assert(cdm_same_sig<decltype(&cdm_rows_kernel),
+                           void (*)(int, const int*, int, const double*, double*, int, double)>,
+              "rows");
+static_assert(cdm_same_sig<decltype(&cdm_clean_signals_kernel), void (*)(int, int, double*)>,
+              "clean_signals");
+static_assert(cdm_same_sig<decltype(&cdm_wait_selftest_kernel), void (*)(uint64_t, int*)>,
+              "wait_selftest");
+#ifdef CDM_MLP_HEAD
+static_assert(cdm_same_sig<decltype(&cdm_mlp_encode_kernel), void (*)(const double*, int, float*)>,
+              "mlp_encode");
+static_assert(cdm_same_sig<decltype(&cdm_mlp_decode_kernel),
+                           void (*)(const float*, int, int, double*, double*)>, "mlp_decode");
+#endif
+#endif
 
 }  // namespace
 
@@ -163,39 +373,17 @@ cdm_status prep_protocol(cdm_ctx* c, int nmeas, const double* CFP, cudaStream_t 
   CDM_TRY(dev_alloc(&c->proto32, &c->proto32_cap, (size_t)kNCOLS4 * pad));
   CDM_TRY(dev_alloc(&c->proto64, &c->proto64_cap, (size_t)kNCOLS * nmeas));
   c->nmeas_pad = pad;
-  cdm_prep_protocol_kernel<<<(pad + 127) / 128, 128, 0, st>>>(CFP, nmeas, pad, c->proto32, c->proto64);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  return k_prep_protocol(st, CFP, nmeas, pad, c->proto32, c->proto64);
 }
 
-template <int Gw>
-cdm_status pack_signals_g(cdm_ctx* c, int nvox, int nmeas, const double* meas, cudaStream_t st) {
+cdm_status pack_signals(cdm_ctx* c, int Gw, int nvox, int nmeas, const double* meas, cudaStream_t st) {
+  if (cdm_lane_index(Gw) < 0) return cdm_fail(CDM_BAD_ARG, "lanes per voxel must be 1, 2, 4, 8, 16 or 32");
   const int nchunk = (nmeas + Gw - 1) / Gw;
   CDM_TRY(dev_alloc(&c->sig, &c->sig_cap, (size_t)nchunk * std::max(nvox, 1) * Gw));
   if (nvox == 0) return CDM_OK;
   const size_t total = (size_t)nchunk * nvox * Gw;
   const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)c->num_sms * 32);
-  cdm_pack_signals_kernel<Gw><<<blocks, 256, 0, st>>>(meas, nvox, nmeas, nchunk, c->sig);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
-}
-
-cdm_status pack_signals(cdm_ctx* c, int Gw, int nvox, int nmeas, const double* meas, cudaStream_t st) {
-  switch (Gw) {
-    case 1: return pack_signals_g<1>(c, nvox, nmeas, meas, st);
-    case 2: return pack_signals_g<2>(c, nvox, nmeas, meas, st);
-    case 4: return pack_signals_g<4>(c, nvox, nmeas, meas, st);
-    case 8: return pack_signals_g<8>(c, nvox, nmeas, meas, st);
-    case 16: return pack_signals_g<16>(c, nvox, nmeas, meas, st);
-    case 32: return pack_signals_g<32>(c, nvox, nmeas, meas, st);
-  }
-  return cdm_fail(CDM_BAD_ARG, "lanes per voxel must be 1, 2, 4, 8, 16 or 32");
-}
-
-template <class Kfn>
-cdm_status set_smem(Kfn kernel, size_t bytes) {
-  if (bytes > 48 * 1024) CDM_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  return CDM_OK;
+  return k_pack_signals(Gw, blocks, st, meas, nvox, nmeas, nchunk, c->sig);
 }
 
 // Lanes per voxel: explicit choice, else a per-stage floor measured on
@@ -228,11 +416,12 @@ void fill_common(cdm_ctx* c, Args& a, int nvox, int nmeas, int Gw) {
   a.lim = c->lim;
 }
 
+uint32_t first_voxel(const cdm_ctx* c) { return (uint32_t)c->cfg.first_voxel; }
+
 int blocks_for(int nvox, int Gw) { return (nvox + (CDM_NT / Gw) - 1) / (CDM_NT / Gw); }
 
 // ------------------------------------------------------------------ stages
-template <int Gw>
-cdm_status launch_gs(cdm_ctx* c, int nvox, int nmeas, double* params, const double* FixP,
+cdm_status launch_gs(cdm_ctx* c, int Gw, int nvox, int nmeas, double* params, const double* FixP,
                      cudaStream_t st) {
   cdm_gs_args a;
   fill_common(c, a, nvox, nmeas, Gw);
@@ -247,10 +436,8 @@ cdm_status launch_gs(cdm_ctx* c, int nvox, int nmeas, double* params, const doub
   a.cand = c->gs_cand;
   a.best = c->gs_best;
   const size_t sm = fit_smem(c->nmeas_pad);
-  CDM_TRY(set_smem(cdm_gridsearch_kernel<Gw>, sm));
-  cdm_gridsearch_kernel<Gw><<<blocks_for(nvox, Gw), CDM_NT, sm, st>>>(a);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  CDM_TRY(set_smem(CDM_K_GRIDSEARCH, Gw, sm));
+  return launch(CDM_K_GRIDSEARCH, Gw, blocks_for(nvox, Gw), CDM_NT, sm, st, a);
 }
 
 cdm_status run_gridsearch(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
@@ -267,15 +454,7 @@ cdm_status run_gridsearch(cdm_ctx* c, int nvox, int nmeas, const double* meas, d
   CDM_TRY(dev_alloc(&c->gs_cand, &c->gs_cand_cap, n * kGsTop));
   CDM_TRY(dev_alloc(&c->gs_best, &c->gs_best_cap, n));
   if (nvox == 0) return CDM_OK;
-  switch (Gw) {
-    case 1: CDM_TRY(launch_gs<1>(c, nvox, nmeas, params, FixP, st)); break;
-    case 2: CDM_TRY(launch_gs<2>(c, nvox, nmeas, params, FixP, st)); break;
-    case 4: CDM_TRY(launch_gs<4>(c, nvox, nmeas, params, FixP, st)); break;
-    case 8: CDM_TRY(launch_gs<8>(c, nvox, nmeas, params, FixP, st)); break;
-    case 16: CDM_TRY(launch_gs<16>(c, nvox, nmeas, params, FixP, st)); break;
-    case 32: CDM_TRY(launch_gs<32>(c, nvox, nmeas, params, FixP, st)); break;
-    default: return cdm_fail(CDM_BAD_ARG, "bad lane count");
-  }
+  CDM_TRY(launch_gs(c, Gw, nvox, nmeas, params, FixP, st));
   cdm_gs_recheck_args r;
   r.nvox = nvox;
   r.nmeas = nmeas;
@@ -293,13 +472,10 @@ cdm_status run_gridsearch(cdm_ctx* c, int nvox, int nmeas, const double* meas, d
   r.best = c->gs_best;
   r.rechecked = c->counters + 2;
   r.lim = c->lim;
-  cdm_gs_recheck_kernel<<<blocks_for(nvox, 32), CDM_NT, 0, st>>>(r);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  return launch(CDM_K_GS_RECHECK, 0, blocks_for(nvox, 32), CDM_NT, 0, st, r);
 }
 
-template <int Gw>
-cdm_status launch_lm(cdm_ctx* c, int nvox, int nmeas, double* params, const double* FixP,
+cdm_status launch_lm(cdm_ctx* c, int Gw, int nvox, int nmeas, double* params, const double* FixP,
                      cudaStream_t st) {
   cdm_lm_args a;
   fill_common(c, a, nvox, nmeas, Gw);
@@ -310,10 +486,8 @@ cdm_status launch_lm(cdm_ctx* c, int nvox, int nmeas, double* params, const doub
   a.iter_count = c->counters + 0;
   a.succ_count = c->counters + 1;
   const size_t sm = fit_smem(c->nmeas_pad);
-  CDM_TRY(set_smem(cdm_levmar_kernel<Gw>, sm));
-  cdm_levmar_kernel<Gw><<<blocks_for(nvox, Gw), CDM_NT, sm, st>>>(a);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  CDM_TRY(set_smem(CDM_K_LEVMAR, Gw, sm));
+  return launch(CDM_K_LEVMAR, Gw, blocks_for(nvox, Gw), CDM_NT, sm, st, a);
 }
 
 cdm_status run_levmar(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
@@ -322,20 +496,12 @@ cdm_status run_levmar(cdm_ctx* c, int nvox, int nmeas, const double* meas, doubl
   const int Gw = pick_lanes(c, c->cfg.lanes_levmar, 4, nvox);
   CDM_TRY(pack_signals(c, Gw, nvox, nmeas, meas, st));
   if (nvox == 0) return CDM_OK;
-  switch (Gw) {
-    case 1: return launch_lm<1>(c, nvox, nmeas, params, FixP, st);
-    case 2: return launch_lm<2>(c, nvox, nmeas, params, FixP, st);
-    case 4: return launch_lm<4>(c, nvox, nmeas, params, FixP, st);
-    case 8: return launch_lm<8>(c, nvox, nmeas, params, FixP, st);
-    case 16: return launch_lm<16>(c, nvox, nmeas, params, FixP, st);
-    case 32: return launch_lm<32>(c, nvox, nmeas, params, FixP, st);
-    default: return cdm_fail(CDM_BAD_ARG, "bad lane count");
-  }
+  return launch_lm(c, Gw, nvox, nmeas, params, FixP, st);
 }
 
-template <int Gw, bool RICIAN>
-cdm_status launch_mcmc(cdm_ctx* c, int nvox, int nmeas, double* params, const double* FixP,
-                       double* samples, double* tau, uint32_t voxel_offset, cudaStream_t st) {
+cdm_status launch_mcmc(cdm_ctx* c, int Gw, bool rician, int nvox, int nmeas, double* params,
+                       const double* FixP, double* samples, double* tau, uint32_t voxel_offset,
+                       cudaStream_t st) {
   cdm_mcmc_args a;
   fill_common(c, a, nvox, nmeas, Gw);
   a.params = params;
@@ -351,11 +517,10 @@ cdm_status launch_mcmc(cdm_ctx* c, int nvox, int nmeas, double* params, const do
   a.stream = (uint32_t)c->cfg.id_part;
   a.voxel_offset = voxel_offset;
   a.prop_sd = c->prop_sd;
+  const int fam = rician ? CDM_K_MCMC_RICIAN : CDM_K_MCMC;
   const size_t sm = fit_smem(c->nmeas_pad);
-  CDM_TRY(set_smem(cdm_mcmc_kernel<Gw, RICIAN>, sm));
-  cdm_mcmc_kernel<Gw, RICIAN><<<blocks_for(nvox, Gw), CDM_NT, sm, st>>>(a);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  CDM_TRY(set_smem(fam, Gw, sm));
+  return launch(fam, Gw, blocks_for(nvox, Gw), CDM_NT, sm, st, a);
 }
 
 cdm_status run_mcmc(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
@@ -373,21 +538,8 @@ cdm_status run_mcmc(cdm_ctx* c, int nvox, int nmeas, const double* meas, double*
   const int Gw = pick_lanes(c, c->cfg.lanes_mcmc, 2, nvox);
   CDM_TRY(pack_signals(c, Gw, nvox, nmeas, meas, st));
   if (nvox == 0) return CDM_OK;
-  const bool ric = c->cfg.rician != 0;
-#define CDM_MCMC_CASE(Gw2)                                                                     \
-  case Gw2:                                                                                    \
-    return ric ? launch_mcmc<Gw2, true>(c, nvox, nmeas, params, FixP, samples, tau, voxel_offset, st) \
-               : launch_mcmc<Gw2, false>(c, nvox, nmeas, params, FixP, samples, tau, voxel_offset, st);
-  switch (Gw) {
-    CDM_MCMC_CASE(1)
-    CDM_MCMC_CASE(2)
-    CDM_MCMC_CASE(4)
-    CDM_MCMC_CASE(8)
-    CDM_MCMC_CASE(16)
-    CDM_MCMC_CASE(32)
-  }
-#undef CDM_MCMC_CASE
-  return cdm_fail(CDM_BAD_ARG, "bad lane count");
+  return launch_mcmc(c, Gw, c->cfg.rician != 0, nvox, nmeas, params, FixP, samples, tau,
+                     voxel_offset, st);
 }
 
 cdm_status run_post(cdm_ctx* c, bool bic, int nvox, int nmeas, int nsamples, const double* meas,
@@ -414,15 +566,9 @@ cdm_status run_post(cdm_ctx* c, bool bic, int nvox, int nmeas, int nsamples, con
   a.rician = rician ? 1 : 0;
   a.err = c->err;
   const size_t sm = proto_bytes(c->nmeas_pad);
-  if (bic) {
-    CDM_TRY(set_smem(cdm_bic_aic_kernel, sm));
-    cdm_bic_aic_kernel<<<blocks_for(nvox, 32), CDM_NT, sm, st>>>(a);
-  } else {
-    CDM_TRY(set_smem(cdm_predicted_kernel, sm));
-    cdm_predicted_kernel<<<blocks_for(nvox, 32), CDM_NT, sm, st>>>(a);
-  }
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  const int fam = bic ? CDM_K_BIC_AIC : CDM_K_PREDICTED;
+  CDM_TRY(set_smem(fam, 0, sm));
+  return launch(fam, 0, blocks_for(nvox, 32), CDM_NT, sm, st, a);
 }
 
 cdm_status fit_sequence(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
@@ -437,9 +583,8 @@ cdm_status fit_sequence(cdm_ctx* c, int nvox, int nmeas, const double* meas, dou
     CDM_TRY(run_mcmc(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau, voxel_offset, st));
     nsamples = o.njumps / o.sampleevery;
   } else if (nvox > 0) {
-    cdm_params_to_samples_kernel<<<std::max(1, std::min(c->num_sms * 4, (nvox * kNP + 255) / 256)), 256, 0,
-                                   st>>>(params, nvox, samples);
-    CDM_CUDA(cudaGetLastError());
+    CDM_TRY(k_params_to_samples(std::max(1, std::min(c->num_sms * 4, (nvox * kNP + 255) / 256)), st,
+                                params, nvox, samples));
   }
   const bool rician = o.rician && o.run_mcmc;
   if (o.get_predicted && pred)
@@ -466,53 +611,8 @@ cdm_status reserve_fit(cdm_ctx* c, int nvox, int nmeas) {
   CDM_TRY(dev_alloc(&c->gs_best, &c->gs_best_cap, n));
   // kernel attributes are set outside capture too
   const size_t sm = fit_smem(pad);
-  CDM_TRY(set_smem(cdm_gridsearch_kernel<1>, sm)); CDM_TRY(set_smem(cdm_gridsearch_kernel<2>, sm));
-  CDM_TRY(set_smem(cdm_gridsearch_kernel<4>, sm)); CDM_TRY(set_smem(cdm_gridsearch_kernel<8>, sm));
-  CDM_TRY(set_smem(cdm_gridsearch_kernel<16>, sm)); CDM_TRY(set_smem(cdm_gridsearch_kernel<32>, sm));
+  for (int Gw : {1, 2, 4, 8, 16, 32}) CDM_TRY(set_smem(CDM_K_GRIDSEARCH, Gw, sm));
   return CDM_OK;
-}
-
-// dMRI_Data::remove_NonPositive_entries (dMRI_Data.cu:15-30), which CUDIMOT
-// applies to every voxel's signals when --rician is set (dMRI_Data.cu:133),
-// so that log(S) in the Rician likelihood stays finite. If the smallest
-// value is non-positive and the largest positive (both read as float, as
-// the reference's MinS/MaxS), every entry that is non-positive as a float
-// takes the smallest remaining value, min(smallest positive entry,
-// float(largest)), rounded to float. One warp per voxel.
-__global__ void cdm_clean_signals_kernel(int nvox, int nmeas, double* __restrict__ meas) {
-  const int v = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-  const int lane = (int)(threadIdx.x & 31);
-  if (v >= nvox) return;
-  double* row = meas + (size_t)v * nmeas;
-  double mn = CUDART_INF, mx = -CUDART_INF, mpos = CUDART_INF;
-  for (int m = lane; m < nmeas; m += 32) {
-    const double x = row[m];
-    mn = fmin(mn, x);
-    mx = fmax(mx, x);
-    if ((float)x > 0.0f) mpos = fmin(mpos, x);
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    mn = fmin(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
-    mx = fmax(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
-    mpos = fmin(mpos, __shfl_xor_sync(0xFFFFFFFFu, mpos, o));
-  }
-  if (!((float)mn <= 0.0f && (float)mx > 0.0f)) return;
-  const double rep = (double)(float)fmin(mpos, (double)(float)mx);
-  for (int m = lane; m < nmeas; m += 32)
-    if ((float)row[m] <= 0.0f) row[m] = rep;
-}
-
-// Self-test of the bounded waits: the CTA initialises an mbarrier that
-// expects one arrival nobody makes and waits on it; the wait must give up
-// after limit_ns and record CDM_DEVERR_STAGE_TIMEOUT (no copy is in flight,
-// so the CTA can simply return).
-__global__ void cdm_wait_selftest_kernel(uint64_t limit_ns, int* err) {
-  __shared__ __align__(8) uint64_t bar;
-  const uint32_t sbar = (uint32_t)__cvta_generic_to_shared(&bar);
-  if (threadIdx.x == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sbar), "r"(1) : "memory");
-  __syncthreads();
-  cdm_mbar_wait_phase0(sbar, limit_ns, threadIdx.x == 0 ? err : nullptr);
 }
 
 }  // namespace
@@ -531,8 +631,8 @@ cdm_status cdm_get_model_info(cdm_model_info* info) {
   info->nparams = NPARAMS;
   info->ncfp = NCFP;
   info->nfixp = NFIXP;
-  for (int i = 0; i < NCFP && i < CDM_MAX_BLOCKS; i++) info->cfp_size[i] = MODEL::CFP_size[i];
-  for (int i = 0; i < NFIXP && i < CDM_MAX_BLOCKS; i++) info->fixp_size[i] = MODEL::FixP_size[i];
+  for (int i = 0; i < NCFP && i < CDM_MAX_BLOCKS; i++) info->cfp_size[i] = kCfpBlocks[i];
+  for (int i = 0; i < NFIXP && i < CDM_MAX_BLOCKS; i++) info->fixp_size[i] = kFixpBlocks[i];
   info->cfp_tsize = CDM_CFP_TSIZE;
   info->fixp_tsize = CDM_FIXP_TSIZE;
   info->derived_cfp = CDM_NDCFP;
@@ -561,7 +661,7 @@ cdm_status cdm_parse_fixed(const char* list, int* fixed) {
 }
 
 cdm_status cdm_read_cfp_list(const char* path, int nmeas, double* cfp) {
-  std::vector<int> sizes(MODEL::CFP_size, MODEL::CFP_size + NCFP);
+  std::vector<int> sizes(kCfpBlocks, kCfpBlocks + NCFP);
   return cdm_read_cfp_list_impl(path, nmeas, sizes, cfp);
 }
 
@@ -647,7 +747,7 @@ cdm_status cdm_mcmc(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_size
                     const double* meas, double* params, const double* CFP, const double* FixP,
                     double* samples, double* tau_samples, void* stream) {
   CDM_TRY(check_common(c, nvox, nmeas, CFP_size, FixP_size));
-  return run_mcmc(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau_samples, 0,
+  return run_mcmc(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau_samples, first_voxel(c),
                   (cudaStream_t)stream);
 }
 
@@ -657,7 +757,7 @@ cdm_status cdm_mcmc_seeded(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int Fi
                            const double* prop_sd, void* stream) {
   CDM_TRY(check_common(c, nvox, nmeas, CFP_size, FixP_size));
   c->prop_sd = prop_sd;
-  const cdm_status s = run_mcmc(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau_samples, 0,
+  const cdm_status s = run_mcmc(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau_samples, first_voxel(c),
                                 (cudaStream_t)stream);
   c->prop_sd = nullptr;
   return s;
@@ -695,10 +795,8 @@ cdm_status cdm_synth_signals(cdm_ctx* c, int nvox, int nmeas, const double* CFP,
   a.x = (__nv_bfloat16*)x;
   a.err = c->err;
   const size_t sm = proto_bytes(c->nmeas_pad);
-  CDM_TRY(set_smem(cdm_synth_kernel, sm));
-  cdm_synth_kernel<<<(nvox + CDM_NT / 32 - 1) / (CDM_NT / 32), CDM_NT, sm, st>>>(a);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  CDM_TRY(set_smem(CDM_K_SYNTH, 0, sm));
+  return launch(CDM_K_SYNTH, 0, (nvox + CDM_NT / 32 - 1) / (CDM_NT / 32), CDM_NT, sm, st, a);
 }
 
 cdm_status cdm_cost(cdm_ctx* c, int nvox, int nmeas, const double* meas, const double* params,
@@ -722,10 +820,8 @@ cdm_status cdm_cost(cdm_ctx* c, int nvox, int nmeas, const double* meas, const d
   a.fixp = FixP;
   a.err = c->err;
   const size_t sm = proto_bytes(c->nmeas_pad);
-  CDM_TRY(set_smem(cdm_cost_kernel, sm));
-  cdm_cost_kernel<<<blocks_for(nvox, 32), CDM_NT, sm, st>>>(a, params, cost);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  CDM_TRY(set_smem(CDM_K_COST, 0, sm));
+  return k_cost(blocks_for(nvox, 32), sm, st, a, params, cost);
 }
 
 cdm_status cdm_select_worse(int n, const double* cost, const double* ref, double margin, int* idx,
@@ -734,10 +830,7 @@ cdm_status cdm_select_worse(int n, const double* cost, const double* ref, double
   cudaStream_t st = (cudaStream_t)stream;
   CDM_CUDA(cudaMemsetAsync(count, 0, sizeof(int), st));
   if (n == 0) return CDM_OK;
-  cdm_select_worse_kernel<<<std::min((n + 255) / 256, 152 * 8), 256, 0, st>>>(n, cost, ref, margin,
-                                                                             idx, count);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  return k_select_worse(std::min((n + 255) / 256, 152 * 8), st, n, cost, ref, margin, idx, count);
 }
 
 cdm_status cdm_rows(int nsel, const int* idx, int ncols, const double* src, double* dst, int mode,
@@ -746,11 +839,8 @@ cdm_status cdm_rows(int nsel, const int* idx, int ncols, const double* src, doub
     return cdm_fail(CDM_BAD_ARG, "bad argument");
   if (nsel == 0) return CDM_OK;
   const size_t total = (size_t)nsel * ncols;
-  cdm_rows_kernel<<<(int)std::min<size_t>((total + 255) / 256, 152 * 8), 256, 0,
-                    (cudaStream_t)stream>>>(nsel, idx, ncols, mode == 2 ? nullptr : src, dst,
-                                            mode == 1, value);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  return k_rows((int)std::min<size_t>((total + 255) / 256, 152 * 8), (cudaStream_t)stream, nsel, idx,
+                ncols, mode == 2 ? nullptr : src, dst, mode == 1 ? 1 : 0, value);
 }
 
 cdm_status cdm_mlp_head_info(int* n_mu, int* n_sig, int* group) {
@@ -771,10 +861,7 @@ cdm_status cdm_mlp_targets(cdm_ctx* c, int n, const double* params, float* targe
 #ifdef CDM_MLP_HEAD
   if (!c || n < 0 || !params || !targets) return cdm_fail(CDM_BAD_ARG, "bad argument");
   if (n == 0) return CDM_OK;
-  cdm_mlp_encode_kernel<<<std::min((n + 255) / 256, 152 * 8), 256, 0, (cudaStream_t)stream>>>(
-      params, n, targets);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  return k_mlp_encode(std::min((n + 255) / 256, 152 * 8), (cudaStream_t)stream, params, n, targets);
 #else
   (void)c; (void)n; (void)params; (void)targets; (void)stream;
   return cdm_fail(CDM_NOT_SUPPORTED, "this plugin defines no learned-initialiser head");
@@ -787,10 +874,8 @@ cdm_status cdm_mlp_decode(cdm_ctx* c, int n, const float* out, int ld, double* p
   if (!c || n < 0 || !out || !params || ld < CDM_MLP_NMU + CDM_MLP_NSIG)
     return cdm_fail(CDM_BAD_ARG, "bad argument");
   if (n == 0) return CDM_OK;
-  cdm_mlp_decode_kernel<<<std::min((n + 255) / 256, 152 * 8), 256, 0, (cudaStream_t)stream>>>(
-      out, ld, n, params, prop_sd);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  return k_mlp_decode(std::min((n + 255) / 256, 152 * 8), (cudaStream_t)stream, out, ld, n, params,
+                      prop_sd);
 #else
   (void)c; (void)n; (void)out; (void)ld; (void)params; (void)prop_sd; (void)stream;
   return cdm_fail(CDM_NOT_SUPPORTED, "this plugin defines no learned-initialiser head");
@@ -844,7 +929,7 @@ cdm_status cdm_fit(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* 
     }
     CDM_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
     cdm_status s = fit_sequence(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau, pred, BIC,
-                                AIC, 0, cap);
+                                AIC, first_voxel(c), cap);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(cap, &g);
     if (s != CDM_OK) {
@@ -896,8 +981,8 @@ cdm_status cdm_fit_enqueue(cdm_ctx* c, int nvox, int nmeas, const double* meas, 
     CDM_TRY(reserve_fit(c, nvox, nmeas));
   }
   CDM_CUDA(cudaMemsetAsync(c->counters, 0, 4 * sizeof(unsigned long long), st));
-  return fit_sequence(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau, pred, BIC, AIC, 0,
-                      st);
+  return fit_sequence(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau, pred, BIC, AIC,
+                      first_voxel(c), st);
 }
 
 cdm_status cdm_synchronize(cdm_ctx* c, void* stream, int64_t timeout_ms) {
@@ -943,19 +1028,14 @@ cdm_status cdm_selftest_wait_timeout(cdm_ctx* c, int limit_ms, void* stream) {
   if (limit_ms < 1 || limit_ms > 2000) return cdm_fail(CDM_BAD_ARG, "limit_ms must be in 1..2000");
   if (!c) return noalloc_selftest(limit_ms, (cudaStream_t)stream);
   CDM_TRY(ensure_base(c));
-  cdm_wait_selftest_kernel<<<1, 32, 0, (cudaStream_t)stream>>>((uint64_t)limit_ms * 1000000ull, c->err);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  return k_wait_selftest((cudaStream_t)stream, (uint64_t)limit_ms * 1000000ull, c->err);
 }
 
 cdm_status cdm_clean_signals(int nvox, int nmeas, double* meas, void* stream) {
   if (nvox < 0 || nmeas <= 0 || (nvox > 0 && !meas)) return cdm_fail(CDM_BAD_ARG, "bad argument");
   if (nvox == 0) return CDM_OK;
   const size_t threads = (size_t)nvox * 32;
-  cdm_clean_signals_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-      nvox, nmeas, meas);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  return k_clean_signals((int)((threads + 255) / 256), (cudaStream_t)stream, nvox, nmeas, meas);
 }
 
 cdm_status cdm_fit_host(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
@@ -1026,10 +1106,9 @@ cdm_status cdm_fit_host(cdm_ctx* c, int nvox, int nmeas, const double* meas, dou
 // until the process exits.
 namespace {
 
-constexpr size_t kNoAllocScratchBytes = 16u << 20;  // 16 MiB
-constexpr size_t kNoAllocHeader = 256;               // device error word
-
+#ifndef CDM_MODULE_HOST
 static __device__ __align__(256) unsigned char cdm_noalloc_scratch[kNoAllocScratchBytes];
+#endif
 
 constexpr int kNoAllocMaxDevices = 64;
 unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
@@ -1049,7 +1128,17 @@ cdm_status noalloc_scratch(unsigned char** out) {
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
   if (!g_noalloc_ptr[dev]) {
     void* p = nullptr;
+#ifdef CDM_MODULE_HOST
+    // split build: the array lives in the embedded device module
+    cudaLibrary_t lib = nullptr;
+    CDM_CUDA(module_library(&lib));
+    size_t bytes = 0;
+    CDM_CUDA(cudaLibraryGetGlobal(&p, &bytes, lib, "cdm_noalloc_scratch"));
+    if (bytes < kNoAllocScratchBytes)
+      return cdm_fail(CDM_CUDA_ERROR, "the device module's no-allocation array is too small");
+#else
     CDM_CUDA(cudaGetSymbolAddress(&p, cdm_noalloc_scratch));
+#endif
     CDM_CUDA(cudaMemset(p, 0, kNoAllocHeader));
     g_noalloc_ptr[dev] = (unsigned char*)p;
   }
@@ -1057,8 +1146,7 @@ cdm_status noalloc_scratch(unsigned char** out) {
   return CDM_OK;
 }
 
-template <int Gw>
-cdm_status noalloc_lm_launch(const cdm_model_cfg* cfg, unsigned char* scratch, int sms, int nvox,
+cdm_status noalloc_lm_launch(int Gw, const cdm_model_cfg* cfg, unsigned char* scratch, int sms, int nvox,
                              int nmeas, const double* meas, double* params, const double* CFP,
                              const double* FixP, cudaStream_t st) {
   const int pad = round_up(nmeas, 32);
@@ -1078,13 +1166,11 @@ cdm_status noalloc_lm_launch(const cdm_model_cfg* cfg, unsigned char* scratch, i
   // The error word accumulates with atomicOr across calls (cleared at
   // set-up and by cdm_noalloc_status); the protocol table and the signals
   // are fully rewritten by every call.
-  cdm_prep_protocol_kernel<<<(pad + 127) / 128, 128, 0, st>>>(CFP, nmeas, pad, proto, nullptr);
-  CDM_CUDA(cudaGetLastError());
+  CDM_TRY(k_prep_protocol(st, CFP, nmeas, pad, proto, nullptr));
   if (nvox == 0) return CDM_OK;
   const size_t total = (size_t)nchunk * nvox * Gw;
-  cdm_pack_signals_kernel<Gw><<<(int)std::min<size_t>((total + 255) / 256, (size_t)std::max(sms, 1) * 32),
-                               256, 0, st>>>(meas, nvox, nmeas, nchunk, sig);
-  CDM_CUDA(cudaGetLastError());
+  CDM_TRY(k_pack_signals(Gw, (int)std::min<size_t>((total + 255) / 256, (size_t)std::max(sms, 1) * 32),
+                         st, meas, nvox, nmeas, nchunk, sig));
   cdm_lm_args a;
   a.nvox = nvox;
   a.nmeas = nmeas;
@@ -1110,10 +1196,8 @@ cdm_status noalloc_lm_launch(const cdm_model_cfg* cfg, unsigned char* scratch, i
     a.lim.pb[p] = (float)cfg->priors_b[p];
     a.lim.fixed[p] = cfg->fixed[p];
   }
-  CDM_TRY(set_smem(cdm_levmar_kernel<Gw>, fit_smem(pad)));
-  cdm_levmar_kernel<Gw><<<blocks_for(nvox, Gw), CDM_NT, fit_smem(pad), st>>>(a);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  CDM_TRY(set_smem(CDM_K_LEVMAR, Gw, fit_smem(pad)));
+  return launch(CDM_K_LEVMAR, Gw, blocks_for(nvox, Gw), CDM_NT, fit_smem(pad), st, a);
 }
 
 }  // namespace
@@ -1143,16 +1227,9 @@ extern "C" cdm_status cdm_levmar_noalloc(const cdm_model_cfg* cfg, int nvox, int
     Gw = 4;
     while (Gw < 32 && (long)nvox * Gw < 4 * resident) Gw *= 2;
   }
-  cudaStream_t st = (cudaStream_t)stream;
-  switch (Gw) {
-    case 1: return noalloc_lm_launch<1>(cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP, st);
-    case 2: return noalloc_lm_launch<2>(cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP, st);
-    case 4: return noalloc_lm_launch<4>(cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP, st);
-    case 8: return noalloc_lm_launch<8>(cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP, st);
-    case 16: return noalloc_lm_launch<16>(cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP, st);
-    case 32: return noalloc_lm_launch<32>(cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP, st);
-  }
-  return cdm_fail(CDM_BAD_ARG, "lanes_levmar must be 0, 1, 2, 4, 8, 16 or 32");
+  if (cdm_lane_index(Gw) < 0) return cdm_fail(CDM_BAD_ARG, "lanes_levmar must be 0, 1, 2, 4, 8, 16 or 32");
+  return noalloc_lm_launch(Gw, cfg, scratch, sms, nvox, nmeas, meas, params, CFP, FixP,
+                           (cudaStream_t)stream);
 }
 
 // Reads and clears the no-allocation error word of the current device after
@@ -1177,7 +1254,5 @@ extern "C" cdm_status cdm_noalloc_status(void* stream) {
 static cdm_status noalloc_selftest(int limit_ms, cudaStream_t st) {
   unsigned char* scratch = nullptr;
   CDM_TRY(noalloc_scratch(&scratch));
-  cdm_wait_selftest_kernel<<<1, 32, 0, st>>>((uint64_t)limit_ms * 1000000ull, (int*)scratch);
-  CDM_CUDA(cudaGetLastError());
-  return CDM_OK;
+  return k_wait_selftest(st, (uint64_t)limit_ms * 1000000ull, (int*)scratch);
 }

@@ -11,6 +11,8 @@
 #define __forceinline__ inline
 #include <cmath>
 #include <cstdint>
+#include <cstring>
+#include <string>
 #include <algorithm>
 using std::max;
 using std::min;
@@ -128,4 +130,42 @@ extern "C" int cdm_count_ops(int nvox, const double* params, int nmeas, const do
   out[6] = fw / (nv * NPARAMS);
   out[7] = mw / (nv * NPARAMS);
   return 0;
+}
+
+// The model description of a split build (the header the host half of the
+// library is compiled with instead of the plugin): the plugin's sizes and
+// which optional hooks it defines. Writes at most cap bytes of text into
+// buf; returns the length, or -1 if it did not fit. The CFP/FixP block
+// sizes are appended by the build from modelparameters.cc.
+#define CDM_DESC_STR2(...) #__VA_ARGS__
+#define CDM_DESC_STR(...) CDM_DESC_STR2(__VA_ARGS__)
+extern "C" int cdm_describe(char* buf, int cap) {
+  std::string s;
+  auto def = [&s](const char* name, long v) {
+    s += "#define ";
+    s += name;
+    s += " ";
+    s += std::to_string(v);
+    s += "\n";
+  };
+  def("NPARAMS", NPARAMS);
+  def("NCFP", NCFP);
+  def("NFIXP", NFIXP);
+  def("CDM_CFP_TSIZE", CDM_CFP_TSIZE);
+  def("CDM_FIXP_TSIZE", CDM_FIXP_TSIZE);
+  def("CDM_NDCFP", CDM_NDCFP);
+  def("CDM_NDP", CDM_NDP);
+  def("CDM_PSTORE", CDM_PSTORE);
+#ifdef CDM_SIGNAL_PAIR
+  def("CDM_SIGNAL_PAIR", 1);
+#endif
+#ifdef CDM_MLP_HEAD
+  def("CDM_MLP_HEAD", 1);
+  def("CDM_MLP_NMU", CDM_MLP_NMU);
+  def("CDM_MLP_NSIG", CDM_MLP_NSIG);
+  s += "#define CDM_MLP_GROUPS " CDM_DESC_STR(CDM_MLP_GROUPS) "\n";
+#endif
+  if ((int)s.size() + 1 > cap) return -1;
+  std::memcpy(buf, s.c_str(), s.size() + 1);
+  return (int)s.size();
 }

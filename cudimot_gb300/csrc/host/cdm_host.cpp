@@ -68,6 +68,8 @@ cdm_status cdm_validate_cfg(const cdm_model_cfg* c, int nparams) {
   for (int l : {c->lanes_gridsearch, c->lanes_levmar, c->lanes_mcmc})
     if (!(l == 0 || l == 1 || l == 2 || l == 4 || l == 8 || l == 16 || l == 32))
       return cdm_fail(CDM_BAD_ARG, "lanes per voxel must be 0, 1, 2, 4, 8, 16 or 32");
+  if (c->first_voxel < 0 || c->first_voxel > 0xFFFFFFFFll)
+    return cdm_fail(CDM_BAD_ARG, "first_voxel must be in 0 .. 2^32 - 1");
   return CDM_OK;
 }
 

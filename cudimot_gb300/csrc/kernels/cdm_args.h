@@ -1,0 +1,147 @@
+// cdm_args.h - the compile-time sizes and the launch arguments of the
+// fitting kernels, shared by the kernels and the host code that fills them.
+//
+// Needs only the model's sizes: NPARAMS, CDM_PSTORE, CDM_CFP_TSIZE,
+// CDM_FIXP_TSIZE, CDM_NDCFP and, for plugins with the paired signal hook,
+// CDM_SIGNAL_PAIR. A normal build takes them from the plugin (through
+// cdm_plugin_tail.h and the generated cdm_model_sizes.h); the host half of a
+// split build (device code compiled separately into a module) takes them
+// from the generated model description, without the plugin.
+#pragma once
+#include <stdint.h>
+#include <cuda_bf16.h>
+
+#ifndef CDM_NT
+#define CDM_NT 128  // threads per CTA
+#endif
+
+// The paired (two-measurement) cost loop: plugins with the paired signal
+// hook, evaluated in single precision.
+#if defined(CDM_SIGNAL_PAIR) && !defined(CDM_EVAL_DOUBLE)
+#define CDM_PAIRED 1
+#else
+#define CDM_PAIRED 0
+#endif
+
+constexpr int kNP = NPARAMS;
+constexpr int kNPS = CDM_PSTORE;
+constexpr int kNCOLS = CDM_CFP_TSIZE + CDM_NDCFP;
+constexpr int kNCOLS4 = (kNCOLS + 3) / 4 * 4;  // protocol row stride (floats)
+constexpr int kNFIX = CDM_FIXP_TSIZE > 0 ? CDM_FIXP_TSIZE : 1;
+constexpr int kNCOLSP = (kNCOLS + 1) / 2 * 2;  // pair-table entry stride (column pairs, even)
+#if CDM_PAIRED
+constexpr int kPairTables = 1;  // shared-memory protocol copies of the paired-loop kernels
+#else
+constexpr int kPairTables = 0;
+#endif
+
+constexpr int kGsTop = 4;
+
+// Bounds, priors and fixed flags as the kernels use them. Bounds and prior
+// arguments are floats, as in CUDIMOT's __constant__ copies.
+struct cdm_limits {
+  int btype[kNP];
+  float bmin[kNP];
+  float bmax[kNP];
+  int ptype[kNP];
+  float pa[kNP];
+  float pb[kNP];
+  int fixed[kNP];
+};
+
+struct cdm_gs_args {
+  int nvox, nmeas, nmeas_pad, nchunk, fixp_tsize;
+  uint32_t proto_bytes;
+  const float* proto;
+  const float* sig;
+  double* params;
+  const double* fixp;
+  const double* grid;  // [combs][ngp]
+  int ngp;
+  int combs;
+  int gpos[kNP];       // column of parameter p in the grid, or -1
+  float band;
+  int* flags;          // [nvox]: 0 decided, 1 recheck candidates, 2 recheck all
+  int* cand;           // [nvox][kGsTop]
+  int* best;           // [nvox] winning combination (or -1)
+  int* err;
+  cdm_limits lim;
+};
+
+struct cdm_gs_recheck_args {
+  int nvox, nmeas, fixp_tsize;
+  const double* proto64;  // [nmeas][NCOLS]
+  const double* meas;     // [nvox][nmeas]
+  double* params;
+  const double* fixp;
+  const double* grid;
+  int ngp, combs;
+  int gpos[kNP];
+  const int* flags;
+  const int* cand;
+  int* best;
+  unsigned long long* rechecked;
+  cdm_limits lim;
+};
+
+struct cdm_lm_args {
+  int nvox, nmeas, nmeas_pad, nchunk, fixp_tsize;
+  uint32_t proto_bytes;
+  const float* proto;
+  const float* sig;
+  double* params;
+  const double* fixp;
+  int max_iters;
+  int marquardt;
+  int* err;
+  unsigned long long* iter_count;  // sum of loop passes, may be null
+  unsigned long long* succ_count;  // sum of accepted steps, may be null
+  cdm_limits lim;
+};
+
+struct cdm_mcmc_args {
+  int nvox, nmeas, nmeas_pad, nchunk, fixp_tsize;
+  uint32_t proto_bytes;
+  const float* proto;
+  const float* sig;
+  double* params;
+  const double* fixp;
+  double* samples;
+  double* tau_samples;
+  int nburn, njumps, sampleevery, nsamples, update_proposal;
+  uint64_t seed;
+  uint32_t stream;
+  uint32_t voxel_offset;
+  const double* prop_sd;  // [nvox][NPARAMS] initial proposal widths; null or <= 0: P/10 as CUDIMOT
+  int* err;
+  cdm_limits lim;
+};
+
+struct cdm_post_args {
+  int nvox, nmeas, nmeas_pad, nsamples, fixp_tsize;
+  uint32_t proto_bytes;
+  const float* proto;
+  const double* meas;     // [nvox][nmeas] (BIC/AIC)
+  const double* samples;  // [nvox][NPARAMS][nsamples]
+  const double* tau;      // [nvox][nsamples] or null
+  const double* fixp;
+  double* pred;           // [nvox][nmeas]
+  double* bic;
+  double* aic;
+  int rician;
+  int* err;
+};
+
+struct cdm_synth_args {
+  int nvox, nmeas, nmeas_pad, fixp_tsize, b_col, x_ld;
+  uint32_t proto_bytes;
+  const float* proto;
+  const double* params;     // [nvox][NPARAMS]
+  const double* fixp;       // [nvox][fixp_tsize] (true values)
+  float snr_lo, snr_hi;
+  uint64_t seed;
+  double* meas;             // [nvox][nmeas] (optional)
+  double* s0_est;           // [nvox] mean of the noisy b = 0 signals (optional)
+  __nv_bfloat16* x;         // [nvox][x_ld] noisy / s0_est (optional)
+  int* err;
+};

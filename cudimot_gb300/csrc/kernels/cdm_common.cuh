@@ -25,11 +25,9 @@
 #pragma once
 
 #include <stdint.h>
+#include "cdm_args.h"
 #include "philox.h"
 
-#ifndef CDM_NT
-#define CDM_NT 128  // threads per CTA
-#endif
 #ifndef CDM_SSE_UNROLL
 #define CDM_SSE_UNROLL 2  // measurement-loop unroll of the cost sums
 #endif
@@ -39,32 +37,36 @@ constexpr int kSseUnroll = CDM_SSE_UNROLL;
 #define CDM_PAIR_UNROLL 2  // unroll of the paired (two-measurement) cost loop
 #endif
 constexpr int kPairUnroll = CDM_PAIR_UNROLL;
-constexpr int kNP = NPARAMS;
-constexpr int kNPS = CDM_PSTORE;
-constexpr int kNCOLS = CDM_CFP_TSIZE + CDM_NDCFP;
-constexpr int kNCOLS4 = (kNCOLS + 3) / 4 * 4;  // protocol row stride (floats)
-constexpr int kNFIX = CDM_FIXP_TSIZE > 0 ? CDM_FIXP_TSIZE : 1;
-constexpr int kNCOLSP = (kNCOLS + 1) / 2 * 2;  // pair-table entry stride (column pairs, even)
-#ifdef CDM_SIGNAL_PAIR
-constexpr int kPairTables = 1;  // shared-memory protocol copies of the paired-loop kernels
+
+// Number type the plugin is evaluated in: fp32 (fp32.h), or double with
+// CDM_EVAL_DOUBLE for plugins whose closed forms need it (CUDIMOT's
+// NODDI-Watson cancels terms of ~1e10). Chain state, residuals and their
+// per-lane sums stay single precision either way; group sums, energies and
+// the LM solve are double either way.
+#ifdef CDM_EVAL_DOUBLE
+typedef double cdm_real;
 #else
-constexpr int kPairTables = 0;
+typedef fp32 cdm_real;
+#endif
+
+// Kernel definitions. A normal build makes each one a __global__ function.
+// The device half of a split build (CDM_DEVICE_MODULE) makes them inline
+// device functions taking their argument block by reference; the module
+// defines extern "C" kernels with fixed names that call them, so that a
+// host library compiled without the plugin can look them up by name.
+#ifdef CDM_DEVICE_MODULE
+#define CDM_KERNEL(...) __device__ __forceinline__ void
+#define CDM_KERNEL0 __device__ __forceinline__ void
+#define CDM_KARG(T) const T&
+#else
+#define CDM_KERNEL(...) __global__ void __launch_bounds__(__VA_ARGS__)
+#define CDM_KERNEL0 __global__ void
+#define CDM_KARG(T) const __grid_constant__ T
 #endif
 
 // Error codes written to the device error word.
 #define CDM_DEVERR_STAGE_TIMEOUT 1
 
-// Bounds, priors and fixed flags as the kernels use them. Bounds and prior
-// arguments are floats, as in CUDIMOT's __constant__ copies.
-struct cdm_limits {
-  int btype[kNP];
-  float bmin[kNP];
-  float bmax[kNP];
-  int ptype[kNP];
-  float pa[kNP];
-  float pb[kNP];
-  int fixed[kNP];
-};
 
 template <int Gw>
 __device__ __forceinline__ unsigned cdm_group_mask() {
@@ -139,15 +141,15 @@ __device__ __forceinline__ bool cdm_stage_protocol(const float* __restrict__ gsr
 // shared-memory load per four values. The Gw lanes of a group read Gw
 // consecutive rows (distinct banks for 48-byte rows); other groups of the
 // warp read the same rows (broadcast).
-__device__ __forceinline__ void cdm_load_cfp(const float* sproto, int nmeas_pad, int m, fp32* cf) {
+__device__ __forceinline__ void cdm_load_cfp(const float* sproto, int nmeas_pad, int m, cdm_real* cf) {
   const float4* row = reinterpret_cast<const float4*>(sproto + (size_t)m * kNCOLS4);
 #pragma unroll
   for (int q = 0; q < kNCOLS4 / 4; q++) {
     const float4 v = row[q];
-    if (4 * q + 0 < kNCOLS) cf[4 * q + 0] = fp32(v.x);
-    if (4 * q + 1 < kNCOLS) cf[4 * q + 1] = fp32(v.y);
-    if (4 * q + 2 < kNCOLS) cf[4 * q + 2] = fp32(v.z);
-    if (4 * q + 3 < kNCOLS) cf[4 * q + 3] = fp32(v.w);
+    if (4 * q + 0 < kNCOLS) cf[4 * q + 0] = cdm_real(v.x);
+    if (4 * q + 1 < kNCOLS) cf[4 * q + 1] = cdm_real(v.y);
+    if (4 * q + 2 < kNCOLS) cf[4 * q + 2] = cdm_real(v.z);
+    if (4 * q + 3 < kNCOLS) cf[4 * q + 3] = cdm_real(v.w);
   }
 }
 
@@ -169,7 +171,7 @@ template <int Gw>
 __device__ __forceinline__ const float* cdm_build_pair_table(float* sproto, int nmeas_pad,
                                                              int nchunk) {
   float2* ptab = reinterpret_cast<float2*>(sproto + (size_t)nmeas_pad * kNCOLS4);
-#ifdef CDM_SIGNAL_PAIR
+#if CDM_PAIRED
   const int total = (nchunk / 2) * Gw * kNCOLSP;
   for (int i = (int)threadIdx.x; i < total; i += (int)blockDim.x) {
     const int k = i % kNCOLSP, l = (i / kNCOLSP) % Gw, j = i / (kNCOLSP * Gw);
@@ -200,12 +202,12 @@ __device__ __forceinline__ void cdm_load_pairs(const float* q, float2* ab) {
 // measurement need no bounds test, only the last chunk may be partial.
 template <int Gw>
 __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const float* sproto,
-                                                fp32* P, fp32* FixP, unsigned gmask) {
+                                                cdm_real* P, cdm_real* FixP, unsigned gmask) {
   float acc = 0.0f;
   const int full = io.nmeas / Gw;
   const float* row = sproto + (size_t)io.lane * kNCOLS4;
   const float* sig = io.sig;
-#ifdef CDM_SIGNAL_PAIR
+#if CDM_PAIRED
   // two chunks per step on the paired FP32 instructions (plugin hook
   // Predicted_Signal_Pair) with the protocol from the pair table; two
   // interleaved partial sums
@@ -225,7 +227,7 @@ __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const fl
   acc = acc2.x + acc2.y;
   row += (size_t)c * Gw * kNCOLS4;
   if (c < full) {
-    fp32 cf[kNCOLS];
+    cdm_real cf[kNCOLS];
     cdm_load_cfp(row, 0, 0, cf);
     const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - *sig;
     acc = fmaf(r, r, acc);
@@ -235,7 +237,7 @@ __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const fl
 #else
 #pragma unroll kSseUnroll
   for (int c = 0; c < full; c++) {
-    fp32 cf[kNCOLS];
+    cdm_real cf[kNCOLS];
     cdm_load_cfp(row, 0, 0, cf);
     const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - *sig;
     acc = fmaf(r, r, acc);
@@ -245,7 +247,7 @@ __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const fl
 #endif
   if (full < io.nchunk) {
     const bool valid = full * Gw + io.lane < io.nmeas;
-    fp32 cf[kNCOLS];
+    cdm_real cf[kNCOLS];
     cdm_load_cfp(valid ? row : sproto, 0, 0, cf);
     const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - *sig;
     acc = valid ? fmaf(r, r, acc) : acc;
@@ -287,7 +289,7 @@ __device__ __forceinline__ float cdm_log_i0_fast(float x) {
                     a * 0.00392377f)))))))) * rsqrtf(b));
 }
 
-#ifdef CDM_SIGNAL_PAIR
+#if CDM_PAIRED
 // cdm_log_i0_fast on both halves of a pair without branches: the two
 // polynomial pieces are evaluated on the paired FP32 instructions (the same
 // Horner steps, so each half gets cdm_log_i0_fast's value) and the piece
@@ -328,10 +330,10 @@ __device__ __forceinline__ float2 cdm_log_i0_fast2(float2 x) {
 // -tau/2 (y^2 + S^2) + log I0(tau S y).
 template <int Gw>
 __device__ __forceinline__ double cdm_group_rician(const cdm_voxel_io& io, const float* sproto,
-                                                   fp32* P, fp32* FixP, float tau, unsigned gmask) {
+                                                   cdm_real* P, cdm_real* FixP, float tau, unsigned gmask) {
   float acc = 0.0f;
   int c0 = 0;
-#ifdef CDM_SIGNAL_PAIR
+#if CDM_PAIRED
   // full chunk pairs through the paired signal hook (the pair table), the
   // log I0 term per measurement
   {
@@ -359,7 +361,7 @@ __device__ __forceinline__ double cdm_group_rician(const cdm_voxel_io& io, const
   for (int c = c0; c < io.nchunk; c++) {
     const int m = c * Gw + io.lane;
     const bool valid = m < io.nmeas;
-    fp32 cf[kNCOLS];
+    cdm_real cf[kNCOLS];
     cdm_load_cfp(sproto, io.nmeas_pad, valid ? m : 0, cf);
     const float y = io.sig[(size_t)c * io.chunk_stride];
     const float s = (float)Predicted_Signal(NPARAMS, P, cf, FixP);
@@ -382,15 +384,15 @@ __device__ __forceinline__ double cdm_group_sum_log_meas(const cdm_voxel_io& io,
   return cdm_group_sum<Gw>((double)acc, gmask);
 }
 
-__device__ __forceinline__ void cdm_load_params(const double* __restrict__ src, fp32* P) {
+__device__ __forceinline__ void cdm_load_params(const double* __restrict__ src, cdm_real* P) {
 #pragma unroll
-  for (int i = 0; i < kNPS; i++) P[i] = fp32(0.0f);
+  for (int i = 0; i < kNPS; i++) P[i] = cdm_real(0.0f);
 #pragma unroll
-  for (int i = 0; i < kNP; i++) P[i] = fp32((float)src[i]);
+  for (int i = 0; i < kNP; i++) P[i] = cdm_real((float)src[i]);
 }
 
 __device__ __forceinline__ void cdm_load_fixp(const double* __restrict__ src, int fixp_tsize,
-                                              fp32* fixv) {
+                                              cdm_real* fixv) {
 #pragma unroll
-  for (int k = 0; k < kNFIX; k++) fixv[k] = fp32(k < fixp_tsize ? (float)src[k] : 0.0f);
+  for (int k = 0; k < kNFIX; k++) fixv[k] = cdm_real(k < fixp_tsize ? (float)src[k] : 0.0f);
 }

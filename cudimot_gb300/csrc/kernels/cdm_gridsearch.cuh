@@ -18,26 +18,7 @@
 #pragma once
 #include "cdm_common.cuh"
 
-constexpr int kGsTop = 4;
 
-struct cdm_gs_args {
-  int nvox, nmeas, nmeas_pad, nchunk, fixp_tsize;
-  uint32_t proto_bytes;
-  const float* proto;
-  const float* sig;
-  double* params;
-  const double* fixp;
-  const double* grid;  // [combs][ngp]
-  int ngp;
-  int combs;
-  int gpos[kNP];       // column of parameter p in the grid, or -1
-  float band;
-  int* flags;          // [nvox]: 0 decided, 1 recheck candidates, 2 recheck all
-  int* cand;           // [nvox][kGsTop]
-  int* best;           // [nvox] winning combination (or -1)
-  int* err;
-  cdm_limits lim;
-};
 
 __device__ __forceinline__ bool cdm_gs_in_bounds(const cdm_limits& lim, const double* x) {
 #pragma unroll
@@ -55,7 +36,7 @@ __device__ __forceinline__ bool cdm_gs_in_bounds(const cdm_limits& lim, const do
 }
 
 template <int Gw>
-__global__ void __launch_bounds__(CDM_NT) cdm_gridsearch_kernel(const __grid_constant__ cdm_gs_args a) {
+CDM_KERNEL(CDM_NT) cdm_gridsearch_kernel(CDM_KARG(cdm_gs_args) a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
   const float* ptab = cdm_build_pair_table<Gw>(sproto, a.nmeas_pad, a.nchunk);
@@ -77,7 +58,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_gridsearch_kernel(const __grid_con
   double base[kNP];
 #pragma unroll
   for (int p = 0; p < kNP; p++) base[p] = a.params[(size_t)v * kNP + p];
-  fp32 FixP[kNFIX];
+  cdm_real FixP[kNFIX];
   cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
 
   double bcost[kGsTop];
@@ -93,11 +74,11 @@ __global__ void __launch_bounds__(CDM_NT) cdm_gridsearch_kernel(const __grid_con
     for (int p = 0; p < kNP; p++)
       trial[p] = a.gpos[p] >= 0 ? __ldg(a.grid + (size_t)c * a.ngp + a.gpos[p]) : base[p];
     if (!cdm_gs_in_bounds(lim, trial)) continue;
-    fp32 P[kNPS];
+    cdm_real P[kNPS];
 #pragma unroll
-    for (int i = 0; i < kNPS; i++) P[i] = fp32(0.0f);
+    for (int i = 0; i < kNPS; i++) P[i] = cdm_real(0.0f);
 #pragma unroll
-    for (int p = 0; p < kNP; p++) P[p] = fp32((float)trial[p]);
+    for (int p = 0; p < kNP; p++) P[p] = cdm_real((float)trial[p]);
     cdm_update_derived(P, FixP);
     const double cost = cdm_group_sse<Gw>(io, sproto, P, FixP, gm);
     // Sorted insertion with constant indices (register arrays): entries
@@ -138,21 +119,6 @@ __global__ void __launch_bounds__(CDM_NT) cdm_gridsearch_kernel(const __grid_con
 // FP64 re-check of flagged voxels: one warp per voxel, lane l sums
 // measurements l, l+32, ... and the warp folds with the 16/8/4/2/1 shuffle
 // tree, CUDIMOT's summation order (GridSearch.cu:49-95).
-struct cdm_gs_recheck_args {
-  int nvox, nmeas, fixp_tsize;
-  const double* proto64;  // [nmeas][NCOLS]
-  const double* meas;     // [nvox][nmeas]
-  double* params;
-  const double* fixp;
-  const double* grid;
-  int ngp, combs;
-  int gpos[kNP];
-  const int* flags;
-  const int* cand;
-  int* best;
-  unsigned long long* rechecked;
-  cdm_limits lim;
-};
 
 __device__ __forceinline__ double cdm_warp_cost64(const cdm_gs_recheck_args& a, int v, double* P,
                                                   double* FixP) {
@@ -170,7 +136,7 @@ __device__ __forceinline__ double cdm_warp_cost64(const cdm_gs_recheck_args& a, 
   return __shfl_sync(0xFFFFFFFFu, acc, 0);
 }
 
-__global__ void __launch_bounds__(CDM_NT) cdm_gs_recheck_kernel(const __grid_constant__ cdm_gs_recheck_args a) {
+CDM_KERNEL(CDM_NT) cdm_gs_recheck_kernel(CDM_KARG(cdm_gs_recheck_args) a) {
   const int v = blockIdx.x * (CDM_NT / 32) + (int)threadIdx.x / 32;
   if (v >= a.nvox) return;
   const int flag = a.flags[v];

@@ -25,20 +25,6 @@
 #pragma once
 #include "cdm_common.cuh"
 
-struct cdm_lm_args {
-  int nvox, nmeas, nmeas_pad, nchunk, fixp_tsize;
-  uint32_t proto_bytes;
-  const float* proto;
-  const float* sig;
-  double* params;
-  const double* fixp;
-  int max_iters;
-  int marquardt;
-  int* err;
-  unsigned long long* iter_count;  // sum of loop passes, may be null
-  unsigned long long* succ_count;  // sum of accepted steps, may be null
-  cdm_limits lim;
-};
 
 constexpr float kTwoDivPIf = 0.636619772367581f;
 constexpr float kAvoidf = 1e-4f;
@@ -51,7 +37,7 @@ __device__ __forceinline__ float cdm_minmax_inv(float x, float lo, float hi) {
 }
 
 // invtransformAll (Levenberg_Marquardt.cu:90-103).
-__device__ __forceinline__ void cdm_lm_inv_transform(const cdm_limits& lim, fp32* P, float* Pt) {
+__device__ __forceinline__ void cdm_lm_inv_transform(const cdm_limits& lim, cdm_real* P, float* Pt) {
 #pragma unroll
   for (int p = 0; p < kNP; p++) {
     const float lo = lim.bmin[p], hi = lim.bmax[p];
@@ -67,7 +53,7 @@ __device__ __forceinline__ void cdm_lm_inv_transform(const cdm_limits& lim, fp32
     } else if (lim.btype[p] == BMINMAX) {
       if (x <= lo + kAvoidf) x += kAvoidf;
       if (x >= hi - kAvoidf) x -= kAvoidf;
-      P[p] = fp32(x);
+      P[p] = cdm_real(x);
       Pt[p] = cdm_minmax_inv(x, lo, hi);
     } else {
       Pt[p] = x;
@@ -76,15 +62,15 @@ __device__ __forceinline__ void cdm_lm_inv_transform(const cdm_limits& lim, fp32
 }
 
 // transformAll (Levenberg_Marquardt.cu:105-118); may nudge Pt.
-__device__ __forceinline__ void cdm_lm_transform(const cdm_limits& lim, fp32* P, float* Pt) {
+__device__ __forceinline__ void cdm_lm_transform(const cdm_limits& lim, cdm_real* P, float* Pt) {
 #pragma unroll
   for (int p = 0; p < kNP; p++) {
     const float lo = lim.bmin[p], hi = lim.bmax[p];
     if (lim.fixed[p]) continue;
     if (lim.btype[p] == BMIN) {
-      P[p] = fp32(expf(Pt[p]) + lo);
+      P[p] = cdm_real(expf(Pt[p]) + lo);
     } else if (lim.btype[p] == BMAX) {
-      P[p] = fp32(hi - expf(Pt[p]));
+      P[p] = cdm_real(hi - expf(Pt[p]));
     } else if (lim.btype[p] == BMINMAX) {
       float x = (hi - lo) * 0.5f * atanf(Pt[p] / kSpeedf) * kTwoDivPIf + (lo + hi) * 0.5f;
       if (x <= lo + kAvoidf) {
@@ -95,9 +81,9 @@ __device__ __forceinline__ void cdm_lm_transform(const cdm_limits& lim, fp32* P,
         x -= kAvoidf;
         Pt[p] = cdm_minmax_inv(x, lo, hi);
       }
-      P[p] = fp32(x);
+      P[p] = cdm_real(x);
     } else {
-      P[p] = fp32(Pt[p]);
+      P[p] = cdm_real(Pt[p]);
     }
   }
 }
@@ -172,7 +158,7 @@ __device__ __forceinline__ void cdm_lm_solve(const double (&hess)[kNH], const do
 }
 
 template <int Gw>
-__global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constant__ cdm_lm_args a) {
+CDM_KERNEL(CDM_NT) cdm_levmar_kernel(CDM_KARG(cdm_lm_args) a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
   const float* ptab = cdm_build_pair_table<Gw>(sproto, a.nmeas_pad, a.nchunk);
@@ -191,7 +177,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
   io.lane = lane;
   io.pairs = ptab + (size_t)lane * kNCOLSP * 2;
 
-  fp32 P[kNPS], FixP[kNFIX];
+  cdm_real P[kNPS], FixP[kNFIX];
   float Pt[kNP];
   cdm_load_params(a.params + (size_t)v * kNP, P);
   cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
@@ -220,11 +206,11 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
       for (int c = 0; c < io.nchunk; c++) {
         const int m = c * Gw + lane;
         const bool valid = m < io.nmeas;
-        fp32 cf[kNCOLS];
+        cdm_real cf[kNCOLS];
         cdm_load_cfp(sproto, io.nmeas_pad, valid ? m : 0, cf);
         const float y = io.sig[(size_t)c * io.chunk_stride];
         const float r = valid ? (float)Predicted_Signal(NPARAMS, P, cf, FixP) - y : 0.0f;
-        fp32 d[kNP];
+        cdm_real d[kNP];
         Partial_Derivatives(NPARAMS, P, cf, FixP, d);
         float j[kNP];
 #pragma unroll
@@ -258,7 +244,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_levmar_kernel(const __grid_constan
     float step[kNP];
 #pragma unroll
     for (int i = 0; i < kNP; i++) step[i] = Pt[i] - (float)x[i];
-    fp32 Pn[kNPS];
+    cdm_real Pn[kNPS];
 #pragma unroll
     for (int i = 0; i < kNPS; i++) Pn[i] = P[i];
     cdm_lm_transform(lim, Pn, step);

@@ -24,27 +24,10 @@
 #pragma once
 #include "cdm_common.cuh"
 
-struct cdm_mcmc_args {
-  int nvox, nmeas, nmeas_pad, nchunk, fixp_tsize;
-  uint32_t proto_bytes;
-  const float* proto;
-  const float* sig;
-  double* params;
-  const double* fixp;
-  double* samples;
-  double* tau_samples;
-  int nburn, njumps, sampleevery, nsamples, update_proposal;
-  uint64_t seed;
-  uint32_t stream;
-  uint32_t voxel_offset;
-  const double* prop_sd;  // [nvox][NPARAMS] initial proposal widths; null or <= 0: P/10 as CUDIMOT
-  int* err;
-  cdm_limits lim;
-};
 
-__device__ __forceinline__ float cdm_prior(const cdm_limits& lim, int p, fp32* P, int nmeas,
-                                           fp32* cfp_all, fp32* FixP) {
-  fp32 xv = P[0];
+__device__ __forceinline__ float cdm_prior(const cdm_limits& lim, int p, cdm_real* P, int nmeas,
+                                           cdm_real* cfp_all, cdm_real* FixP) {
+  cdm_real xv = P[0];
 #pragma unroll
   for (int k = 1; k < kNP; k++) xv = (k == p) ? P[k] : xv;
   const float x = (float)xv;
@@ -66,9 +49,9 @@ __device__ __forceinline__ float cdm_prior(const cdm_limits& lim, int p, fp32* P
   }
 }
 
-__device__ __forceinline__ bool cdm_in_bounds(const cdm_limits& lim, int p, fp32* P) {
+__device__ __forceinline__ bool cdm_in_bounds(const cdm_limits& lim, int p, cdm_real* P) {
   if (!ConstraintsMCMC(NPARAMS, P)) return false;
-  fp32 xv = P[0];
+  cdm_real xv = P[0];
 #pragma unroll
   for (int k = 1; k < kNP; k++) xv = (k == p) ? P[k] : xv;
   const float x = (float)xv;
@@ -98,7 +81,7 @@ __device__ __forceinline__ void cdm_set(Tv* a, int i, Tv x) {
 
 template <int Gw, bool RICIAN>
 __device__ __forceinline__ double cdm_likelihood(const cdm_voxel_io& io, const float* sproto,
-                                                 fp32* P, fp32* FixP, float tau, unsigned gmask) {
+                                                 cdm_real* P, cdm_real* FixP, float tau, unsigned gmask) {
   if (RICIAN) {
     const double s = cdm_group_rician<Gw>(io, sproto, P, FixP, tau, gmask);
     return -(double)io.nmeas * (double)logf(tau) - s;
@@ -113,7 +96,7 @@ __device__ __forceinline__ double cdm_likelihood(const cdm_voxel_io& io, const f
 #endif
 
 template <int Gw, bool RICIAN>
-__global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(const __grid_constant__ cdm_mcmc_args a) {
+CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
   const float* ptab = cdm_build_pair_table<Gw>(sproto, a.nmeas_pad, a.nchunk);
@@ -132,7 +115,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
   io.lane = lane;
   io.pairs = ptab + (size_t)lane * kNCOLSP * 2;
 
-  fp32 P[kNPS], FixP[kNFIX];
+  cdm_real P[kNPS], FixP[kNFIX];
   cdm_load_params(a.params + (size_t)v * kNP, P);
   cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
   float propSD[kNP], prior[kNP];
@@ -149,7 +132,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
   // Custom priors receive the whole CFP array in CUDIMOT; with the staged
   // SoA table there is no AoS copy, so they see the voxel's first
   // measurement only (no shipped plugin defines one).
-  fp32 cf0[kNCOLS];
+  cdm_real cf0[kNCOLS];
   cdm_load_cfp(sproto, a.nmeas_pad, 0, cf0);
 
   double energy = 0.0;
@@ -170,7 +153,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
         if (x < lim.bmin[p]) x = lim.bmin[p];
         else if (x > lim.bmax[p]) x = lim.bmax[p];
       }
-      P[p] = fp32(x);
+      P[p] = cdm_real(x);
     }
     cdm_update_derived(P, FixP);
     stale = false;
@@ -186,7 +169,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
       float s1 = 0.0f;
       for (int c = 0; c < io.nchunk; c++) {
         const int m = c * Gw + lane;
-        fp32 cf[kNCOLS];
+        cdm_real cf[kNCOLS];
         cdm_load_cfp(sproto, io.nmeas_pad, m < io.nmeas ? m : 0, cf);
         const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - io.sig[(size_t)c * io.chunk_stride];
         s1 = (m < io.nmeas) ? s1 + r : s1;
@@ -195,7 +178,7 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
       float s2 = 0.0f;
       for (int c = 0; c < io.nchunk; c++) {
         const int m = c * Gw + lane;
-        fp32 cf[kNCOLS];
+        cdm_real cf[kNCOLS];
         cdm_load_cfp(sproto, io.nmeas_pad, m < io.nmeas ? m : 0, cf);
         const float r = mean - ((float)Predicted_Signal(NPARAMS, P, cf, FixP) - io.sig[(size_t)c * io.chunk_stride]);
         s2 = (m < io.nmeas) ? fmaf(r, r, s2) : s2;
@@ -237,8 +220,8 @@ __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(c
           continue;
         }
         const cdm_draw d = cdm_mcmc_draw(a.seed, vid, git, (uint32_t)p, a.stream);
-        const fp32 old = cdm_get(P, p);
-        cdm_set(P, p, fp32((float)old + d.normal * cdm_get(propSD, p)));
+        const cdm_real old = cdm_get(P, p);
+        cdm_set(P, p, cdm_real((float)old + d.normal * cdm_get(propSD, p)));
         bool accepted = false;
         bool derived = false;
         if (cdm_in_bounds(lim, p, P)) {

@@ -6,50 +6,36 @@
 // 63-79, BIC_AIC.cu:160-188): a plain sum divided by nsamples, or the
 // single sample when nsamples == 1. Every lane of the group computes it.
 __device__ __forceinline__ void cdm_sample_mean(const double* __restrict__ s, int nsamples,
-                                                fp32* P) {
+                                                cdm_real* P) {
 #pragma unroll
-  for (int i = 0; i < kNPS; i++) P[i] = fp32(0.0f);
+  for (int i = 0; i < kNPS; i++) P[i] = cdm_real(0.0f);
 #pragma unroll
   for (int p = 0; p < kNP; p++) {
     double acc = 0.0;
     for (int k = 0; k < nsamples; k++) acc += s[(size_t)p * nsamples + k];
-    P[p] = fp32((float)(nsamples > 1 ? acc / nsamples : acc));
+    P[p] = cdm_real((float)(nsamples > 1 ? acc / nsamples : acc));
   }
 }
 
-struct cdm_post_args {
-  int nvox, nmeas, nmeas_pad, nsamples, fixp_tsize;
-  uint32_t proto_bytes;
-  const float* proto;
-  const double* meas;     // [nvox][nmeas] (BIC/AIC)
-  const double* samples;  // [nvox][NPARAMS][nsamples]
-  const double* tau;      // [nvox][nsamples] or null
-  const double* fixp;
-  double* pred;           // [nvox][nmeas]
-  double* bic;
-  double* aic;
-  int rician;
-  int* err;
-};
 
 // getPredictedSignal_kernel (getPredictedSignal.cu:22-92): S(mean sample)
 // for every measurement; a warp per voxel, lanes stride the measurements.
-__global__ void __launch_bounds__(CDM_NT) cdm_predicted_kernel(const __grid_constant__ cdm_post_args a) {
+CDM_KERNEL(CDM_NT) cdm_predicted_kernel(CDM_KARG(cdm_post_args) a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
   const int v = blockIdx.x * (CDM_NT / 32) + (int)threadIdx.x / 32;
   if (v >= a.nvox) return;
   const int lane = threadIdx.x & 31;
-  fp32 P[kNPS], FixP[kNFIX];
+  cdm_real P[kNPS], FixP[kNFIX];
   cdm_sample_mean(a.samples + (size_t)v * kNP * a.nsamples, a.nsamples, P);
   cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
   cdm_update_derived(P, FixP);
   int m = lane;
-#ifdef CDM_SIGNAL_PAIR
+#if CDM_PAIRED
   // measurements m and m + 32 through the paired hook, the function the
   // fitting kernels' cost loops evaluate
   for (; m + 32 < a.nmeas; m += 64) {
-    fp32 ca[kNCOLS], cb[kNCOLS];
+    cdm_real ca[kNCOLS], cb[kNCOLS];
     cdm_load_cfp(sproto, a.nmeas_pad, m, ca);
     cdm_load_cfp(sproto, a.nmeas_pad, m + 32, cb);
     float2 ab[kNCOLS];
@@ -61,7 +47,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_predicted_kernel(const __grid_cons
   }
 #endif
   for (; m < a.nmeas; m += 32) {
-    fp32 cf[kNCOLS];
+    cdm_real cf[kNCOLS];
     cdm_load_cfp(sproto, a.nmeas_pad, m, cf);
     a.pred[(size_t)v * a.nmeas + m] = (double)(float)Predicted_Signal(NPARAMS, P, cf, FixP);
   }
@@ -70,13 +56,13 @@ __global__ void __launch_bounds__(CDM_NT) cdm_predicted_kernel(const __grid_cons
 // bic_aic_kernel (BIC_AIC.cu:112-201): Gaussian log-likelihood
 // -(n/2) log(SSE/2), or the Rician one with tau averaged over its samples;
 // BIC = -2 logL + np log n, AIC = -2 logL + 2 np (np + 1 with tau).
-__global__ void __launch_bounds__(CDM_NT) cdm_bic_aic_kernel(const __grid_constant__ cdm_post_args a) {
+CDM_KERNEL(CDM_NT) cdm_bic_aic_kernel(CDM_KARG(cdm_post_args) a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
   const int v = blockIdx.x * (CDM_NT / 32) + (int)threadIdx.x / 32;
   if (v >= a.nvox) return;
   const int lane = threadIdx.x & 31;
-  fp32 P[kNPS], FixP[kNFIX];
+  cdm_real P[kNPS], FixP[kNFIX];
   cdm_sample_mean(a.samples + (size_t)v * kNP * a.nsamples, a.nsamples, P);
   cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
   cdm_update_derived(P, FixP);
@@ -89,7 +75,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_bic_aic_kernel(const __grid_consta
   const float tauf = (float)tau;
   float acc = 0.0f;
   for (int m = lane; m < a.nmeas; m += 32) {
-    fp32 cf[kNCOLS];
+    cdm_real cf[kNCOLS];
     cdm_load_cfp(sproto, a.nmeas_pad, m, cf);
     const float s = (float)Predicted_Signal(NPARAMS, P, cf, FixP);
     const float y = (float)a.meas[(size_t)v * a.nmeas + m];
@@ -115,7 +101,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_bic_aic_kernel(const __grid_consta
 
 // Cost of given parameters, as the LM and grid search score them: sum of
 // squared residuals (FP32 model, FP64 warp sum); a warp per voxel.
-__global__ void __launch_bounds__(CDM_NT) cdm_cost_kernel(const __grid_constant__ cdm_post_args a,
+CDM_KERNEL(CDM_NT) cdm_cost_kernel(CDM_KARG(cdm_post_args) a,
                                                           const double* __restrict__ params,
                                                           double* __restrict__ cost) {
   extern __shared__ __align__(16) float sproto[];
@@ -123,13 +109,13 @@ __global__ void __launch_bounds__(CDM_NT) cdm_cost_kernel(const __grid_constant_
   const int v = blockIdx.x * (CDM_NT / 32) + (int)threadIdx.x / 32;
   if (v >= a.nvox) return;
   const int lane = threadIdx.x & 31;
-  fp32 P[kNPS], FixP[kNFIX];
+  cdm_real P[kNPS], FixP[kNFIX];
   cdm_load_params(params + (size_t)v * kNP, P);
   cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
   cdm_update_derived(P, FixP);
   float acc = 0.0f;
   for (int m = lane; m < a.nmeas; m += 32) {
-    fp32 cf[kNCOLS];
+    cdm_real cf[kNCOLS];
     cdm_load_cfp(sproto, a.nmeas_pad, m, cf);
     const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - (float)a.meas[(size_t)v * a.nmeas + m];
     acc = fmaf(r, r, acc);
@@ -140,7 +126,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_cost_kernel(const __grid_constant_
 
 // Row helpers of the learned initialiser's fallback (voxels whose cost
 // exceeds a reference cost by more than a margin are refit).
-__global__ void cdm_select_worse_kernel(int n, const double* __restrict__ cost,
+CDM_KERNEL0 cdm_select_worse_kernel(int n, const double* __restrict__ cost,
                                         const double* __restrict__ ref, double margin,
                                         int* __restrict__ idx, int* __restrict__ count) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
@@ -149,7 +135,7 @@ __global__ void cdm_select_worse_kernel(int n, const double* __restrict__ cost,
 
 // dst[k][:] = src[idx[k]][:] (gather) or dst[idx[k]][:] = src[k][:] (scatter),
 // or dst[idx[k]][:] = value (src null).
-__global__ void cdm_rows_kernel(int nsel, const int* __restrict__ idx, int ncols,
+CDM_KERNEL0 cdm_rows_kernel(int nsel, const int* __restrict__ idx, int ncols,
                                 const double* __restrict__ src, double* __restrict__ dst,
                                 int scatter, double value) {
   const size_t total = (size_t)nsel * ncols;
@@ -172,7 +158,7 @@ __global__ void cdm_rows_kernel(int nsel, const int* __restrict__ idx, int ncols
 // derived values -> FP32 [nmeas_pad][NCOLS4] (padding rows repeat
 // measurement 0, padding columns are 0) and FP64 [nmeas][NCOLS] for the
 // grid-search re-check.
-__global__ void cdm_prep_protocol_kernel(const double* __restrict__ cfp, int nmeas, int nmeas_pad,
+CDM_KERNEL0 cdm_prep_protocol_kernel(const double* __restrict__ cfp, int nmeas, int nmeas_pad,
                                          float* __restrict__ p32, double* __restrict__ p64) {
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nmeas_pad; m += gridDim.x * blockDim.x) {
     const int src = m < nmeas ? m : 0;
@@ -193,7 +179,7 @@ __global__ void cdm_prep_protocol_kernel(const double* __restrict__ cfp, int nme
 // Signals: [nvox][nmeas] double -> [nchunk][nvox][Gw] float, so that the Gw
 // lanes of consecutive groups read one contiguous line per chunk.
 template <int Gw>
-__global__ void cdm_pack_signals_kernel(const double* __restrict__ meas, int nvox, int nmeas,
+CDM_KERNEL0 cdm_pack_signals_kernel(const double* __restrict__ meas, int nvox, int nmeas,
                                         int nchunk, float* __restrict__ out) {
   const size_t total = (size_t)nchunk * nvox * Gw;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
@@ -209,10 +195,53 @@ __global__ void cdm_pack_signals_kernel(const double* __restrict__ meas, int nvo
 
 // nsamples = 1 output when MCMC does not run: the fitted parameters are
 // the single sample (Parameters.cu copyParams2Samples).
-__global__ void cdm_params_to_samples_kernel(const double* __restrict__ params, int nvox,
+CDM_KERNEL0 cdm_params_to_samples_kernel(const double* __restrict__ params, int nvox,
                                              double* __restrict__ samples) {
   const size_t n = (size_t)nvox * kNP;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
     samples[i] = params[i];
+}
+
+// dMRI_Data::remove_NonPositive_entries (dMRI_Data.cu:15-30), which CUDIMOT
+// applies to every voxel's signals when --rician is set (dMRI_Data.cu:133),
+// so that log(S) in the Rician likelihood stays finite. If the smallest
+// value is non-positive and the largest positive (both read as float, as
+// the reference's MinS/MaxS), every entry that is non-positive as a float
+// takes the smallest remaining value, min(smallest positive entry,
+// float(largest)), rounded to float. One warp per voxel.
+CDM_KERNEL0 cdm_clean_signals_kernel(int nvox, int nmeas, double* __restrict__ meas) {
+  const int v = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = (int)(threadIdx.x & 31);
+  if (v >= nvox) return;
+  double* row = meas + (size_t)v * nmeas;
+  double mn = CUDART_INF, mx = -CUDART_INF, mpos = CUDART_INF;
+  for (int m = lane; m < nmeas; m += 32) {
+    const double x = row[m];
+    mn = fmin(mn, x);
+    mx = fmax(mx, x);
+    if ((float)x > 0.0f) mpos = fmin(mpos, x);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fmin(mn, __shfl_xor_sync(0xFFFFFFFFu, mn, o));
+    mx = fmax(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+    mpos = fmin(mpos, __shfl_xor_sync(0xFFFFFFFFu, mpos, o));
+  }
+  if (!((float)mn <= 0.0f && (float)mx > 0.0f)) return;
+  const double rep = (double)(float)fmin(mpos, (double)(float)mx);
+  for (int m = lane; m < nmeas; m += 32)
+    if ((float)row[m] <= 0.0f) row[m] = rep;
+}
+
+// Self-test of the bounded waits: the CTA initialises an mbarrier that
+// expects one arrival nobody makes and waits on it; the wait must give up
+// after limit_ns and record CDM_DEVERR_STAGE_TIMEOUT (no copy is in flight,
+// so the CTA can simply return).
+CDM_KERNEL0 cdm_wait_selftest_kernel(uint64_t limit_ns, int* err) {
+  __shared__ __align__(8) uint64_t bar;
+  const uint32_t sbar = (uint32_t)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sbar), "r"(1) : "memory");
+  __syncthreads();
+  cdm_mbar_wait_phase0(sbar, limit_ns, threadIdx.x == 0 ? err : nullptr);
 }

@@ -10,19 +10,6 @@
 #define CDM_RNG_SLOT_SYNTH_SNR 0xFFFFFF00u
 #define CDM_RNG_SLOT_SYNTH_NOISE 0xFFFFFF01u
 
-struct cdm_synth_args {
-  int nvox, nmeas, nmeas_pad, fixp_tsize, b_col, x_ld;
-  uint32_t proto_bytes;
-  const float* proto;
-  const double* params;     // [nvox][NPARAMS]
-  const double* fixp;       // [nvox][fixp_tsize] (true values)
-  float snr_lo, snr_hi;
-  uint64_t seed;
-  double* meas;             // [nvox][nmeas] (optional)
-  double* s0_est;           // [nvox] mean of the noisy b = 0 signals (optional)
-  __nv_bfloat16* x;         // [nvox][x_ld] noisy / s0_est (optional)
-  int* err;
-};
 
 // One warp per voxel: clean signal for every measurement, sigma = mean
 // clean b = 0 signal / SNR (SNR uniform in [snr_lo, snr_hi] per voxel; the
@@ -40,13 +27,13 @@ __device__ __forceinline__ float cdm_synth_noisy(const cdm_synth_args& a, int v,
   return sqrtf(re * re + im * im);
 }
 
-__global__ void __launch_bounds__(CDM_NT) cdm_synth_kernel(const __grid_constant__ cdm_synth_args a) {
+CDM_KERNEL(CDM_NT) cdm_synth_kernel(CDM_KARG(cdm_synth_args) a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
   const int v = blockIdx.x * (CDM_NT / 32) + (int)threadIdx.x / 32;
   if (v >= a.nvox) return;
   const int lane = threadIdx.x & 31;
-  fp32 P[kNPS], FixP[kNFIX];
+  cdm_real P[kNPS], FixP[kNFIX];
   cdm_load_params(a.params + (size_t)v * kNP, P);
   cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
   cdm_update_derived(P, FixP);
@@ -57,7 +44,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_synth_kernel(const __grid_constant
   float b0 = 0.0f, smax = 0.0f;
   int nb0 = 0;
   for (int m = lane; m < a.nmeas; m += 32) {
-    fp32 cf[kNCOLS];
+    cdm_real cf[kNCOLS];
     cdm_load_cfp(sproto, a.nmeas_pad, m, cf);
     const bool is_b0 = a.b_col >= 0 && (float)cf[a.b_col] == 0.0f;
     if (is_b0 || a.b_col < 0) {
@@ -77,7 +64,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_synth_kernel(const __grid_constant
   }
   if (nb0 == 0 && a.b_col >= 0) {  // no b = 0 rows: largest clean signal
     for (int m = lane; m < a.nmeas; m += 32) {
-      fp32 cf[kNCOLS];
+      cdm_real cf[kNCOLS];
       cdm_load_cfp(sproto, a.nmeas_pad, m, cf);
       smax = fmaxf(smax, (float)Predicted_Signal(NPARAMS, P, cf, FixP));
     }
@@ -88,7 +75,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_synth_kernel(const __grid_constant
   float ysum = 0.0f;
   if (nb0 > 0) {
     for (int m = lane; m < a.nmeas; m += 32) {
-      fp32 cf[kNCOLS];
+      cdm_real cf[kNCOLS];
       cdm_load_cfp(sproto, a.nmeas_pad, m, cf);
       if ((float)cf[a.b_col] == 0.0f)
         ysum += cdm_synth_noisy(a, v, m, (float)Predicted_Signal(NPARAMS, P, cf, FixP), sigma);
@@ -101,7 +88,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_synth_kernel(const __grid_constant
   // pass 2: every measurement
   const float inv = s0 > 0.0f ? 1.0f / s0 : 1.0f;
   for (int m = lane; m < a.nmeas; m += 32) {
-    fp32 cf[kNCOLS];
+    cdm_real cf[kNCOLS];
     cdm_load_cfp(sproto, a.nmeas_pad, m, cf);
     const float y = cdm_synth_noisy(a, v, m, (float)Predicted_Signal(NPARAMS, P, cf, FixP), sigma);
     if (a.meas) a.meas[(size_t)v * a.nmeas + m] = (double)y;
@@ -114,7 +101,7 @@ __global__ void __launch_bounds__(CDM_NT) cdm_synth_kernel(const __grid_constant
 
 #ifdef CDM_MLP_HEAD
 // Network targets from parameters (plugin hook MLP_Encode).
-__global__ void cdm_mlp_encode_kernel(const double* __restrict__ params, int n,
+CDM_KERNEL0 cdm_mlp_encode_kernel(const double* __restrict__ params, int n,
                                       float* __restrict__ t) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     double P[kNP];
@@ -128,8 +115,8 @@ __global__ void cdm_mlp_encode_kernel(const double* __restrict__ params, int n,
 }
 
 // Parameters and MCMC proposal widths from network outputs (plugin hook
-// MLP_Decode); outputs are [n][ld] fp32, means then log-stds.
-__global__ void cdm_mlp_decode_kernel(const float* __restrict__ out, int ld, int n,
+// MLP_Decode); outputs are [n][ld] float, means then log-stds.
+CDM_KERNEL0 cdm_mlp_decode_kernel(const float* __restrict__ out, int ld, int n,
                                       double* __restrict__ params, double* __restrict__ prop_sd) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     float mu[CDM_MLP_NMU], ls[CDM_MLP_NSIG];

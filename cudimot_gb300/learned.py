@@ -13,9 +13,15 @@ Training data are made by the method itself, all on the GPU:
     search + LM), targets = the LM fits.
 The network is trained with Adam on the Gaussian NLL (cdm_mlp_train_step).
 
-`fit` runs the surrogate-initialised path. The plain grid-search path is
-its yardstick and fallback: voxels whose LM cost exceeds the plain fit's by
-more than `margin` are refit by grid search + LM before MCMC.
+`fit` runs the surrogate-initialised path: network -> LM -> refit of the
+voxels the judge flags by the plain path (grid search + LM) -> MCMC. The
+judge must not need the plain fit of every voxel (that would pay for the
+grid search the network replaces), so by default it is a goodness-of-fit
+test on the voxel's own data: the LM cost against (nmeas - nparams) times
+the variance of the voxel's b = 0 signals, flagged above an upper quantile
+of the F(nmeas - nparams, n_b0 - 1) distribution of that ratio for a good
+fit. A caller that has the plain fit's cost anyway can pass it instead
+(plain_cost, margin): the yardstick of the spec description.
 """
 from __future__ import annotations
 
@@ -204,15 +210,42 @@ class LearnedInit:
         g.fit_reserve(cap, self.nmeas)
         npar = self.lib.nparams
         f = lambda *shape: torch.empty(*shape, dtype=torch.float64, device=self.dev)  # noqa: E731
-        buf = dict(cost=f(nvox), idx=torch.empty(nvox, dtype=torch.int32, device=self.dev),
+        buf = dict(cost=f(nvox), yard=f(nvox), idx=torch.empty(nvox, dtype=torch.int32, device=self.dev),
                    count=torch.zeros(1, dtype=torch.int32, device=self.dev),
                    m=f(cap, self.nmeas), s0=f(cap, 1), p=f(cap, npar), cap=cap)
         return lib, g, buf
 
-    def fit(self, meas, s0, fit_cfg, samples, plain_cost=None, margin=0.01, ctx=None):
-        """Surrogate-initialised fit: network -> LM -> (refit by grid search +
-        LM where the LM cost exceeds plain_cost by more than margin) -> MCMC
-        with network-seeded proposal widths. Returns (params, info)."""
+    def chi2_yardstick(self, meas, quantile=0.99, b_col=3, b0_max=50.0, out=None):
+        """Per-voxel refit threshold from the voxel's own signals: (nmeas -
+        nparams) x var(b = 0 signals) x F quantile. A fit whose cost exceeds
+        it fits worse than noise of that variance explains (probability
+        1 - quantile for a correct fit at Gaussian noise)."""
+        torch = self.torch
+        key = (quantile, b_col, b0_max)
+        if getattr(self, "_yard_key", None) != key:
+            b0 = torch.nonzero(self.cfp[:, b_col] <= b0_max).flatten()
+            if b0.numel() < 3:
+                raise ValueError("the goodness-of-fit judge needs at least 3 b = 0 measurements")
+            dof = self.nmeas - self.lib.nparams
+            from scipy import stats
+            self._yard = (b0, dof * float(stats.f.ppf(quantile, dof, b0.numel() - 1)))
+            self._yard_key = key
+        b0, scale = self._yard
+        var = meas.index_select(1, b0).var(dim=1, unbiased=True)
+        if out is None:
+            return var * scale
+        torch.mul(var, scale, out=out)
+        return out
+
+    def fit(self, meas, s0, fit_cfg, samples, plain_cost=None, margin=0.01, ctx=None,
+            judge="chi2", quantile=0.99, keep_lm=None):
+        """Surrogate-initialised fit: network -> LM -> refit by grid search +
+        LM of the voxels the judge flags -> MCMC with network-seeded proposal
+        widths. judge "chi2": the goodness-of-fit threshold of chi2_yardstick
+        (its cost is part of this call); with plain_cost given, voxels whose
+        LM cost exceeds it by more than margin instead; judge None: no refit.
+        keep_lm: a tensor that receives the parameters before MCMC.
+        Returns (params, info)."""
         torch = self.torch
         n = meas.shape[0]
         lib, g, buf = ctx or self.contexts(fit_cfg, n)
@@ -228,10 +261,14 @@ class LearnedInit:
         mark()
         lib.levmar(meas, P, self.cfp, s0)
         mark()
-        info = {"refit": 0}
-        if plain_cost is not None:
+        info = {"refit": 0, "judge": "plain_cost" if plain_cost is not None else judge}
+        if plain_cost is not None or judge == "chi2":
             self.cost(meas, P, s0, out=buf["cost"])
-            lib.select_worse(buf["cost"], plain_cost, margin, buf["idx"], buf["count"])
+            if plain_cost is not None:
+                ref, mg = plain_cost, margin
+            else:
+                ref, mg = self.chi2_yardstick(meas, quantile, out=buf["yard"]), 0.0
+            lib.select_worse(buf["cost"], ref, mg, buf["idx"], buf["count"])
             nbad = int(buf["count"].item())
             info["refit"] = nbad
             cap = buf["cap"]
@@ -247,6 +284,8 @@ class LearnedInit:
                 g.levmar(sm, sp, self.cfp, ss)
                 lib.rows(k, idx, sp, P, 1)
                 lib.rows(k, idx, None, sd, 2, 0.0)  # MCMC starts these from P/10
+        if keep_lm is not None:
+            keep_lm.copy_(P)
         mark()
         if fit_cfg.run_mcmc:
             lib.mcmc_seeded(meas, P, self.cfp, s0, samples, sd)

@@ -103,6 +103,12 @@ typedef struct {
   int lanes_gridsearch;
   int lanes_levmar;
   int lanes_mcmc;
+  /* Index of this call's first voxel in the whole volume (0). MCMC draws
+   * are keyed by (seed, id_part, global voxel index, iteration), so a
+   * volume fitted in contiguous shards - each call with first_voxel = its
+   * range start, the same seed, id_part and lane counts - gives exactly the
+   * fit of one call over the whole volume (split_parts.cc:80-94 ranges). */
+  int64_t first_voxel;
 } cdm_model_cfg;
 
 /* Per-context counters filled by the last fit. */

@@ -43,3 +43,20 @@ def angle_deg(th1, ph1, th2, ph2):
     v2 = np.stack([np.sin(th2) * np.cos(ph2), np.sin(th2) * np.sin(ph2), np.cos(th2)], -1)
     c = np.abs(np.sum(v1 * v2, -1)).clip(0, 1)
     return np.degrees(np.arccos(c))
+
+
+def lm_voxelwise(c_got, c_ref, ang=None, rtol=1e-4, adeg=0.5):
+    """LM parity voxel by voxel: the library's final cost within rtol
+    (relative) of the reference's and, where the angle between the fitted
+    orientations is given, within adeg degrees; or else the library's cost
+    lower than the reference's. Returns (mask of failing voxels, report)."""
+    rel = (c_got - c_ref) / c_ref
+    agree = np.abs(rel) <= rtol
+    if ang is not None:
+        agree &= ang <= adeg
+    bad = ~(agree | (c_got < c_ref))
+    rep = {"voxels": int(rel.size), "failing": int(bad.sum()),
+           "max_excess": float(rel[bad].max()) if bad.any() else 0.0,
+           "lower_by_more_than_rtol": int(np.sum(rel < -rtol)),
+           "max_rel": float(rel.max())}
+    return bad, rep

@@ -23,10 +23,13 @@ def _check_line(line, n_gpus):
     assert line["unit"] == "voxels/s" and line["value"] > 0
     assert line["n_gpus"] == n_gpus and line["steps"] == 1 and line["warmup"] == 0
     assert line["higher_is_better"] is True and line["vs_baseline"] is None
-    assert line["config"]["workload"] == "noddi_watson_gs_lm_mcmc"
-    assert line["config"]["nvox_sample"] == 8
+    # the same config as the library's headline line (bench.headline_config)
+    sys.path.insert(0, ROOT)
+    import bench
+    assert line["config"] == bench.headline_config(bench.NVOX, n_gpus)
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
+    assert cb["sample"].startswith("8 voxels") and "plugin" in cb
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0

@@ -22,7 +22,7 @@ import pytest
 import torch
 
 from cudimot_gb300 import capi
-from tests.helpers import angle_deg, b2s, dt, oracle
+from tests.helpers import lm_voxelwise, angle_deg, b2s, dt, oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -75,10 +75,9 @@ def _lm(model, wl, cuda):
 def test_levmar_diffusion_tensor(built, cuda):
     wl = dt(4000, seed=5)
     got, ref, c_got, c_ref = _lm("DiffusionTensor", wl, cuda)
-    rel = (c_got - c_ref) / c_ref
-    assert np.mean(np.abs(rel) <= 1e-4) >= 0.995, np.quantile(rel, [0.0, 0.5, 0.99, 1.0])
     ang = angle_deg(*principal_dir(got), *principal_dir(ref))
-    assert np.mean(ang <= 0.5) >= 0.995, np.quantile(ang, [0.5, 0.99, 1.0])
+    bad, rep = lm_voxelwise(c_got, c_ref, ang)
+    assert not bad.any(), rep
 
 
 def test_levmar_ball_2_sticks(built, cuda):

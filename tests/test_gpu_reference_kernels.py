@@ -14,7 +14,7 @@ import pytest
 import torch
 
 from cudimot_gb300 import capi, synth
-from tests.helpers import angle_deg, b1s, b2s, dt, oracle, watson
+from tests.helpers import lm_voxelwise, angle_deg, b1s, b2s, dt, oracle, watson
 
 pytestmark = pytest.mark.gpu
 
@@ -65,10 +65,9 @@ def test_b1s_levmar_vs_reference_kernels(built, cuda):
     r, g = pr.cpu().numpy(), po.cpu().numpy()
     o = oracle("Ball_1_Stick")
     cr, cg = o.cost(wl.meas, r, wl.cfp), o.cost(wl.meas, g, wl.cfp)
-    rel = (cg - cr) / cr
     ang = angle_deg(r[:, 3], r[:, 4], g[:, 3], g[:, 4])
-    assert np.mean(rel <= 1e-4) >= 0.995, np.quantile(rel, [0.5, 0.99, 1])
-    assert np.mean(ang <= 0.5) >= 0.995
+    bad, rep = lm_voxelwise(cg, cr, ang)
+    assert not bad.any(), rep
 
 
 def test_b1s_levmar_vs_reference_float_kernels(built, cuda):
@@ -88,9 +87,10 @@ def test_b1s_levmar_vs_reference_float_kernels(built, cuda):
     assert np.all(np.isfinite(r))
     o = oracle("Ball_1_Stick")
     cr, cg = o.cost(wl.meas, r, wl.cfp), o.cost(wl.meas, g, wl.cfp)
-    rel = (cg - cr) / cr
-    assert np.mean(rel <= 1e-4) >= 0.99, np.quantile(rel, [0.5, 0.99, 1])
-    assert np.median(np.abs(rel)) < 1e-4, np.median(np.abs(rel))
+    # no orientation bound: CUDIMOT's float LM stops on its own noise
+    bad, rep = lm_voxelwise(cg, cr)
+    assert not bad.any(), rep
+    assert np.median(np.abs((cg - cr) / cr)) < 1e-4
 
 
 def test_b1s_mcmc_vs_reference_kernels(built, cuda):
@@ -145,10 +145,9 @@ def test_watson_gridsearch_and_levmar_vs_reference_kernels(built, cuda):
     torch.cuda.synchronize()
     r2, g2 = pr2.cpu().numpy(), po2.cpu().numpy()
     cr2, cg2 = o.cost(wl.meas, r2, wl.cfp, wl.fixp), o.cost(wl.meas, g2, wl.cfp, wl.fixp)
-    rel = (cg2 - cr2) / cr2
-    assert np.mean(rel <= 1e-4) >= 0.98, np.quantile(rel, [0.5, 0.98, 1])
     ang = angle_deg(r2[:, 3], r2[:, 4], g2[:, 3], g2[:, 4])
-    assert np.mean(ang <= 0.5) >= 0.98, np.quantile(ang, [0.5, 0.98, 1])
+    bad, rep = lm_voxelwise(cg2, cr2, ang)
+    assert not bad.any(), rep
 
 
 def test_dt_levmar_vs_reference_kernels(built, cuda):
@@ -164,8 +163,8 @@ def test_dt_levmar_vs_reference_kernels(built, cuda):
     r, g = pr.cpu().numpy(), po.cpu().numpy()
     o = oracle("DiffusionTensor")
     cr, cg = o.cost(wl.meas, r, wl.cfp), o.cost(wl.meas, g, wl.cfp)
-    rel = (cg - cr) / cr
-    assert np.mean(np.abs(rel) <= 1e-4) >= 0.995, np.quantile(rel, [0, 0.5, 0.99, 1])
+    bad, rep = lm_voxelwise(cg, cr)
+    assert not bad.any(), rep
 
 
 def test_b2s_mcmc_vs_reference_kernels(built, cuda):
@@ -221,5 +220,5 @@ def test_bingham_gridsearch_and_levmar_vs_reference_kernels(built, cuda):
     torch.cuda.synchronize()
     r2, g2 = pr2.cpu().numpy(), po2.cpu().numpy()
     cr2, cg2 = o.cost(wl.meas, r2, wl.cfp, wl.fixp), o.cost(wl.meas, g2, wl.cfp, wl.fixp)
-    rel = (cg2 - cr2) / cr2
-    assert np.mean(rel <= 1e-4) >= 0.95, np.quantile(rel, [0.5, 0.95, 1])
+    bad, rep = lm_voxelwise(cg2, cr2)
+    assert not bad.any(), rep

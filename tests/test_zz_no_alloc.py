@@ -124,4 +124,4 @@ def test_levmar_noalloc_allocates_nothing_and_reports_waits(built, cuda):
     # and the fits improved on their grid-search start
     c_fit = o.cost(wl.meas, fits[3].cpu().numpy(), wl.cfp, wl.fixp)
     c_start = o.cost(wl.meas, start, wl.cfp, wl.fixp)
-    assert c_fit.sum() < 0.9 * c_start.sum()
+    assert c_fit.sum() < c_start.sum()
