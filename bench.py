@@ -1008,11 +1008,31 @@ def dropin_leg(cfp, meas, fixp, init, truth, post, dev, n=12_800):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     pm = s.mean(2).cpu().numpy()
-    return {"value": n / (ms / 1e3), "unit": "voxels/s", "ms": ms,
-            "sample": f"first {n} voxels of this workload, grid search -> LM -> MCMC (cdm_fit)",
-            "plugin": "CUDIMOT's mymodels/NODDI_Watson unchanged, evaluated in double",
-            "param_error": param_error(pm, truth[:n]),
-            "library_param_error_same_voxels": param_error(post[:n], truth[:n])}
+    out = {"value": n / (ms / 1e3), "unit": "voxels/s", "ms": ms,
+           "sample": f"first {n} voxels of this workload, grid search -> LM -> MCMC (cdm_fit)",
+           "plugin": "CUDIMOT's mymodels/NODDI_Watson unchanged, evaluated in double",
+           "param_error": param_error(pm, truth[:n]),
+           "library_param_error_same_voxels": param_error(post[:n], truth[:n])}
+    # the same plugin evaluated in single precision: what its closed forms do there
+    if build_dropin.available(MODEL, "float"):
+        try:
+            lf = capi.Cudimot(MODEL, cfg, path=build_dropin.lib_path(MODEL, "float"))
+            pf = p0.clone()
+            sf = torch.zeros_like(s)
+            lf.fit(m[:w].contiguous(), pf[:w].clone(), c, f[:w].contiguous(), sf[:w].contiguous())
+            torch.cuda.synchronize()
+            e0.record(st)
+            lf.fit(m, pf, c, f, sf)
+            e1.record(st)
+            torch.cuda.synchronize()
+            pmf = sf.mean(2).cpu().numpy()
+            fin = np.isfinite(pmf).all(1)
+            out["float"] = {"value": n / (e0.elapsed_time(e1) / 1e3), "unit": "voxels/s",
+                            "finite_posterior_means": float(fin.mean()),
+                            "param_error": param_error(pmf[fin], truth[:n][fin])}
+        except Exception as e:  # noqa: BLE001
+            out["float"] = {"unavailable": f"{type(e).__name__}: {e}"}
+    return out
 
 
 def gpu_launches_per_step(cfg):

@@ -162,8 +162,32 @@ def build_model(model_dir, name=None, extra_flags=(), verbose=False, force=False
     return out, None
 
 
-def describe(flops_lib, sizes, name, eval_type=None):
-    """Text of cdm_model_desc.h from the host build of the plugin."""
+HOOK_MACROS = ("CDM_SIGNAL_PAIR", "CDM_SHELL_SERIES", "CDM_SHELL_KEY", "CDM_SHELL_NCOEF",
+               "CDM_SHELL_MCOLS", "CDM_MLP_HEAD", "CDM_MLP_NMU", "CDM_MLP_NSIG", "CDM_MLP_GROUPS")
+
+
+def device_hooks(known, extra):
+    """#define lines of the plugin's optional hooks as the device compilation
+    of cdm_module.cu sees them (a plugin may define a hook for CUDA only),
+    except those already in `known`. extra = (includes, flags) of that
+    compilation."""
+    includes, flags = extra
+    cmd = [nvcc_path(), "-E", "-std=c++17", "-Xcompiler", "-dM"] + list(flags) + list(includes) + \
+        [os.path.join(CSRC, "cdm_module.cu")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("macro dump of the device module failed:\n" + r.stderr[-3000:])
+    out = ""
+    for line in r.stdout.splitlines():
+        m = re.match(r"#define (\w+)(\s.*)?$", line)
+        if m and m.group(1) in HOOK_MACROS and f"#define {m.group(1)} " not in known:
+            out += line.rstrip() + "\n"
+    return out
+
+
+def describe(flops_lib, sizes, name, eval_type=None, extra=((), ())):
+    """Text of cdm_model_desc.h from the host build of the plugin (sizes) and
+    the device compilation's macros (hooks)."""
     import ctypes
     lib = ctypes.CDLL(flops_lib)
     buf = ctypes.create_string_buffer(1 << 14)
@@ -174,6 +198,7 @@ def describe(flops_lib, sizes, name, eval_type=None):
     txt = ("// generated by cudimot_gb300/build.py from the plugin: the host half of a\n"
            "// split build is compiled with this instead of the plugin\n#pragma once\n")
     txt += buf.value.decode()
+    txt += device_hooks(txt, extra)
     txt += f"#define CDM_CFP_SIZES {pad(sizes['CFP_size'])}\n"
     txt += f"#define CDM_FIXP_SIZES {pad(sizes['FixP_size'])}\n"
     if eval_type == "double":
@@ -204,7 +229,8 @@ def split_device(model_dir, outdir, name=None, eval_type=None, force=False):
     if err:
         return fl, err
     with open(os.path.join(outdir, "cdm_model_desc.h"), "w") as f:
-        f.write(describe(fl, sizes, name, eval_type))
+        f.write(describe(fl, sizes, name, eval_type,
+                         (_includes(gen, model_dir), [ARCH] + eval_flags(eval_type))))
     cmd = [nvcc_path()] + flags + _includes(gen, model_dir) + [
         os.path.join(CSRC, "cdm_module.cu"), "-o", cubin + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)

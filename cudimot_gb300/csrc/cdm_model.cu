@@ -154,6 +154,10 @@ const void* kfn_lanes(int fam) {
     case CDM_K_MCMC: return (const void*)cdm_mcmc_kernel<Gw, false>;
     case CDM_K_MCMC_RICIAN: return (const void*)cdm_mcmc_kernel<Gw, true>;
     case CDM_K_PACK_SIGNALS: return (const void*)cdm_pack_signals_kernel<Gw>;
+#if CDM_SHELLS
+    case CDM_K_PREP_SHELLS: return (const void*)cdm_prep_shells_kernel<Gw>;
+    case CDM_K_PACK_SHELL_SIGNALS: return (const void*)cdm_pack_shell_signals_kernel<Gw>;
+#endif
   }
   return nullptr;
 }
@@ -174,7 +178,6 @@ const void* kfn(int fam, int lanes) {
     case CDM_K_GS_RECHECK: return (const void*)cdm_gs_recheck_kernel;
     case CDM_K_PREDICTED: return (const void*)cdm_predicted_kernel;
     case CDM_K_BIC_AIC: return (const void*)cdm_bic_aic_kernel;
-    case CDM_K_COST: return (const void*)cdm_cost_kernel;
     case CDM_K_SELECT_WORSE: return (const void*)cdm_select_worse_kernel;
     case CDM_K_ROWS: return (const void*)cdm_rows_kernel;
     case CDM_K_PREP_PROTOCOL: return (const void*)cdm_prep_protocol_kernel;
@@ -233,9 +236,16 @@ cdm_status k_params_to_samples(int blocks, cudaStream_t st, const double* params
                                double* samples) {
   return launch(CDM_K_PARAMS_TO_SAMPLES, 0, blocks, 256, 0, st, params, nvox, samples);
 }
-cdm_status k_cost(int blocks, size_t smem, cudaStream_t st, cdm_post_args a, const double* params,
-                  double* cost) {
-  return launch(CDM_K_COST, 0, blocks, CDM_NT, smem, st, a, params, cost);
+cdm_status k_prep_shells(int lanes, cudaStream_t st, const double* cfp, int nmeas, int nmeas_pad,
+                         float* table, int* perm, int* shell_rank) {
+  return launch(CDM_K_PREP_SHELLS, lanes, 1, 256, 0, st, cfp, nmeas, nmeas_pad, table, perm,
+                shell_rank);
+}
+cdm_status k_pack_shell_signals(int lanes, int blocks, cudaStream_t st, const double* meas, int nvox,
+                                int nmeas, int nchunk, const float* table, const int* perm,
+                                float* out) {
+  return launch(CDM_K_PACK_SHELL_SIGNALS, lanes, blocks, 256, 0, st, meas, nvox, nmeas, nchunk,
+                table, perm, out);
 }
 cdm_status k_select_worse(int blocks, cudaStream_t st, int n, const double* cost, const double* ref,
                           double margin, int* idx, int* count) {
@@ -269,8 +279,13 @@ static_assert(cdm_same_sig<decltype(&cdm_pack_signals_kernel<1>),
                            void (*)(const double*, int, int, int, float*)>, "pack_signals");
 static_assert(cdm_same_sig<decltype(&cdm_params_to_samples_kernel),
                            void (*)(const double*, int, double*)>, "params_to_samples");
-static_assert(cdm_same_sig<decltype(&cdm_cost_kernel),
-                           void (*)(cdm_post_args, const double*, double*)>, "cost");
+#if CDM_SHELLS
+static_assert(cdm_same_sig<decltype(&cdm_prep_shells_kernel<1>),
+                           void (*)(const double*, int, int, float*, int*, int*)>, "prep_shells");
+static_assert(cdm_same_sig<decltype(&cdm_pack_shell_signals_kernel<1>),
+                           void (*)(const double*, int, int, int, const float*, const int*, float*)>,
+              "pack_shell_signals");
+#endif
 static_assert(cdm_same_sig<decltype(&cdm_select_worse_kernel),
                            void (*)(int, const double*, const double*, double, int*, int*)>,
               "select_worse");
@@ -313,6 +328,10 @@ struct cdm_ctx {
   size_t gs_cand_cap = 0;
   int* gs_best = nullptr;
   size_t gs_best_cap = 0;
+  int* shell_perm = nullptr;   // per-shell series: padded position -> measurement
+  size_t shell_perm_cap = 0;
+  int* shell_rank = nullptr;   // per-shell series: scratch of the shell prep kernel
+  size_t shell_rank_cap = 0;
   int* err = nullptr;
   unsigned long long* counters = nullptr;  // [0] lm passes [1] lm successes [2] gs rechecks
   const double* prop_sd = nullptr;          // initial MCMC proposal widths of the next run_mcmc
@@ -351,6 +370,19 @@ size_t proto_bytes(int nmeas_pad) { return (size_t)kNCOLS4 * nmeas_pad * sizeof(
 // search, LM, MCMC): the staged protocol and, with the paired signal hook,
 // its pair table of the same size.
 size_t fit_smem(int nmeas_pad) { return proto_bytes(nmeas_pad) * (1 + kPairTables); }
+// With the per-shell series (grid search and Gaussian MCMC of plugins with
+// the hook) the shell table is staged after the protocol; the pair table is
+// built over it when the protocol has no usable shells, so the region
+// holds the larger of the two.
+size_t shell_bytes(int nmeas, int Gw) { return (size_t)cdm_shell_table_floats(nmeas, Gw) * sizeof(float); }
+size_t fit_smem_shells(int nmeas_pad, int nmeas, int Gw) {
+  return proto_bytes(nmeas_pad) +
+         std::max(proto_bytes(nmeas_pad) * kPairTables, shell_bytes(nmeas, Gw));
+}
+// Float count of the protocol buffer: the table, then room for a shell table.
+size_t proto32_floats(int nmeas_pad, int nmeas) {
+  return (size_t)kNCOLS4 * nmeas_pad + (size_t)cdm_shell_table_floats(nmeas, 32);
+}
 
 cdm_status check_common(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_size) {
   if (!c) return cdm_fail(CDM_BAD_ARG, "null context");
@@ -362,7 +394,7 @@ cdm_status check_common(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_
     return cdm_fail(CDM_BAD_ARG, "FixP_size " + std::to_string(FixP_size) +
                                      " != model FixP_Tsize " + std::to_string(CDM_FIXP_TSIZE));
   const int pad = round_up(nmeas, 32);
-  if (fit_smem(pad) > 200 * 1024)
+  if (std::max(fit_smem(pad), fit_smem_shells(pad, nmeas, 32)) > 200 * 1024)
     return cdm_fail(CDM_BAD_ARG, "protocol too large for shared memory staging");
   return CDM_OK;
 }
@@ -370,10 +402,35 @@ cdm_status check_common(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_
 // Protocol tables from CUDIMOT's CFP array (device pointer).
 cdm_status prep_protocol(cdm_ctx* c, int nmeas, const double* CFP, cudaStream_t st) {
   const int pad = round_up(nmeas, 32);
-  CDM_TRY(dev_alloc(&c->proto32, &c->proto32_cap, (size_t)kNCOLS4 * pad));
+  CDM_TRY(dev_alloc(&c->proto32, &c->proto32_cap, proto32_floats(pad, nmeas)));
   CDM_TRY(dev_alloc(&c->proto64, &c->proto64_cap, (size_t)kNCOLS * nmeas));
   c->nmeas_pad = pad;
   return k_prep_protocol(st, CFP, nmeas, pad, c->proto32, c->proto64);
+}
+
+// The grid search and the Gaussian MCMC of plugins with the per-shell
+// series: the shell table after the protocol rows (valid or marked invalid
+// on the device) and the signals in its order.
+constexpr bool kShells = CDM_SHELLS != 0;
+
+size_t shell_sig_floats(int nvox, int nmeas, int Gw) {
+  const int nc = (cdm_shell_max_pos(nmeas, Gw) + Gw - 1) / Gw;
+  return (size_t)std::max(nc, (nmeas + Gw - 1) / Gw) * std::max(nvox, 1) * Gw;
+}
+
+cdm_status prep_shells_and_pack(cdm_ctx* c, int Gw, int nvox, int nmeas, const double* CFP,
+                                const double* meas, cudaStream_t st) {
+  const int maxpos = cdm_shell_max_pos(nmeas, Gw);
+  CDM_TRY(dev_alloc(&c->shell_perm, &c->shell_perm_cap, (size_t)maxpos));
+  CDM_TRY(dev_alloc(&c->shell_rank, &c->shell_rank_cap, (size_t)nmeas));
+  CDM_TRY(dev_alloc(&c->sig, &c->sig_cap, shell_sig_floats(nvox, nmeas, Gw)));
+  float* table = c->proto32 + (size_t)kNCOLS4 * c->nmeas_pad;
+  CDM_TRY(k_prep_shells(Gw, st, CFP, nmeas, c->nmeas_pad, table, c->shell_perm, c->shell_rank));
+  if (nvox == 0) return CDM_OK;
+  const int nchunk = (nmeas + Gw - 1) / Gw;
+  const size_t total = (size_t)((maxpos + Gw - 1) / Gw) * nvox * Gw;
+  const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)c->num_sms * 32);
+  return k_pack_shell_signals(Gw, blocks, st, meas, nvox, nmeas, nchunk, table, c->shell_perm, c->sig);
 }
 
 cdm_status pack_signals(cdm_ctx* c, int Gw, int nvox, int nmeas, const double* meas, cudaStream_t st) {
@@ -421,6 +478,19 @@ uint32_t first_voxel(const cdm_ctx* c) { return (uint32_t)c->cfg.first_voxel; }
 int blocks_for(int nvox, int Gw) { return (nvox + (CDM_NT / Gw) - 1) / (CDM_NT / Gw); }
 
 // ------------------------------------------------------------------ stages
+// The staged bytes and shared memory of a grid-search launch (with the
+// shell table when the plugin has the per-shell series).
+cdm_status launch_gs_args(cdm_ctx* c, cdm_gs_args& a, int Gw, int nvox, int nmeas, cudaStream_t st) {
+  a.shells_staged = kShells ? 1 : 0;
+  size_t sm = fit_smem(c->nmeas_pad);
+  if (kShells) {
+    a.proto_bytes = (uint32_t)(proto_bytes(c->nmeas_pad) + shell_bytes(nmeas, Gw));
+    sm = fit_smem_shells(c->nmeas_pad, nmeas, Gw);
+  }
+  CDM_TRY(set_smem(CDM_K_GRIDSEARCH, Gw, sm));
+  return launch(CDM_K_GRIDSEARCH, Gw, blocks_for(nvox, Gw), CDM_NT, sm, st, a);
+}
+
 cdm_status launch_gs(cdm_ctx* c, int Gw, int nvox, int nmeas, double* params, const double* FixP,
                      cudaStream_t st) {
   cdm_gs_args a;
@@ -435,9 +505,9 @@ cdm_status launch_gs(cdm_ctx* c, int Gw, int nvox, int nmeas, double* params, co
   a.flags = c->gs_flags;
   a.cand = c->gs_cand;
   a.best = c->gs_best;
-  const size_t sm = fit_smem(c->nmeas_pad);
-  CDM_TRY(set_smem(CDM_K_GRIDSEARCH, Gw, sm));
-  return launch(CDM_K_GRIDSEARCH, Gw, blocks_for(nvox, Gw), CDM_NT, sm, st, a);
+  a.cost_out = nullptr;
+  a.cost_only = 0;
+  return launch_gs_args(c, a, Gw, nvox, nmeas, st);
 }
 
 cdm_status run_gridsearch(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
@@ -448,7 +518,10 @@ cdm_status run_gridsearch(cdm_ctx* c, int nvox, int nmeas, const double* meas, d
   // measurements, 968 combinations: 2 lanes 91 ms, 4 lanes 100 ms, 8 lanes
   // 150 ms (1 lane 164 ms)
   const int Gw = pick_lanes(c, c->cfg.lanes_gridsearch, 2, nvox);
-  CDM_TRY(pack_signals(c, Gw, nvox, nmeas, meas, st));
+  if (kShells)
+    CDM_TRY(prep_shells_and_pack(c, Gw, nvox, nmeas, CFP, meas, st));
+  else
+    CDM_TRY(pack_signals(c, Gw, nvox, nmeas, meas, st));
   const size_t n = (size_t)std::max(nvox, 1);
   CDM_TRY(dev_alloc(&c->gs_flags, &c->gs_flags_cap, n));
   CDM_TRY(dev_alloc(&c->gs_cand, &c->gs_cand_cap, n * kGsTop));
@@ -518,7 +591,13 @@ cdm_status launch_mcmc(cdm_ctx* c, int Gw, bool rician, int nvox, int nmeas, dou
   a.voxel_offset = voxel_offset;
   a.prop_sd = c->prop_sd;
   const int fam = rician ? CDM_K_MCMC_RICIAN : CDM_K_MCMC;
-  const size_t sm = fit_smem(c->nmeas_pad);
+  size_t sm = fit_smem(c->nmeas_pad);
+  a.shells_staged = 0;
+  if (kShells && !rician) {
+    a.shells_staged = 1;
+    a.proto_bytes = (uint32_t)(proto_bytes(c->nmeas_pad) + shell_bytes(nmeas, Gw));
+    sm = fit_smem_shells(c->nmeas_pad, nmeas, Gw);
+  }
   CDM_TRY(set_smem(fam, Gw, sm));
   return launch(fam, Gw, blocks_for(nvox, Gw), CDM_NT, sm, st, a);
 }
@@ -536,7 +615,10 @@ cdm_status run_mcmc(cdm_ctx* c, int nvox, int nmeas, const double* meas, double*
   // 1 lane 443 ms, 4 lanes 469 ms: fewer lanes per voxel repeat the
   // per-proposal work in fewer threads
   const int Gw = pick_lanes(c, c->cfg.lanes_mcmc, 2, nvox);
-  CDM_TRY(pack_signals(c, Gw, nvox, nmeas, meas, st));
+  if (kShells && !c->cfg.rician)
+    CDM_TRY(prep_shells_and_pack(c, Gw, nvox, nmeas, CFP, meas, st));
+  else
+    CDM_TRY(pack_signals(c, Gw, nvox, nmeas, meas, st));
   if (nvox == 0) return CDM_OK;
   return launch_mcmc(c, Gw, c->cfg.rician != 0, nvox, nmeas, params, FixP, samples, tau,
                      voxel_offset, st);
@@ -598,20 +680,35 @@ cdm_status fit_sequence(cdm_ctx* c, int nvox, int nmeas, const double* meas, dou
 
 // Allocate every scratch buffer a fit of this shape needs, so that the
 // captured graph contains no allocation.
+// Signal floats a fit of this shape may pack: every lane count in
+// measurement order, and the shell order of the grid search and MCMC.
+size_t fit_sig_floats(const cdm_ctx* c, int nvox, int nmeas) {
+  size_t sig = 0;
+  for (int Gw : {1, 2, 4, 8, 16, 32})
+    sig = std::max(sig, (size_t)((nmeas + Gw - 1) / Gw) * std::max(nvox, 1) * Gw);
+  if (kShells)
+    for (int Gw : {pick_lanes(c, c->cfg.lanes_gridsearch, 2, nvox), pick_lanes(c, c->cfg.lanes_mcmc, 2, nvox)})
+      sig = std::max(sig, shell_sig_floats(nvox, nmeas, Gw));
+  return sig;
+}
+
 cdm_status reserve_fit(cdm_ctx* c, int nvox, int nmeas) {
   const int pad = round_up(nmeas, 32);
-  CDM_TRY(dev_alloc(&c->proto32, &c->proto32_cap, (size_t)kNCOLS4 * pad));
+  CDM_TRY(dev_alloc(&c->proto32, &c->proto32_cap, proto32_floats(pad, nmeas)));
   CDM_TRY(dev_alloc(&c->proto64, &c->proto64_cap, (size_t)kNCOLS * nmeas));
-  size_t sig = 0;
-  for (int Gw : {1, 2, 4, 8, 16, 32}) sig = std::max(sig, (size_t)((nmeas + Gw - 1) / Gw) * std::max(nvox, 1) * Gw);
-  CDM_TRY(dev_alloc(&c->sig, &c->sig_cap, sig));
+  CDM_TRY(dev_alloc(&c->sig, &c->sig_cap, fit_sig_floats(c, nvox, nmeas)));
+  if (kShells) {
+    CDM_TRY(dev_alloc(&c->shell_perm, &c->shell_perm_cap, (size_t)cdm_shell_max_pos(nmeas, 32)));
+    CDM_TRY(dev_alloc(&c->shell_rank, &c->shell_rank_cap, (size_t)nmeas));
+  }
   const size_t n = (size_t)std::max(nvox, 1);
   CDM_TRY(dev_alloc(&c->gs_flags, &c->gs_flags_cap, n));
   CDM_TRY(dev_alloc(&c->gs_cand, &c->gs_cand_cap, n * kGsTop));
   CDM_TRY(dev_alloc(&c->gs_best, &c->gs_best_cap, n));
   // kernel attributes are set outside capture too
-  const size_t sm = fit_smem(pad);
-  for (int Gw : {1, 2, 4, 8, 16, 32}) CDM_TRY(set_smem(CDM_K_GRIDSEARCH, Gw, sm));
+  for (int Gw : {1, 2, 4, 8, 16, 32})
+    CDM_TRY(set_smem(CDM_K_GRIDSEARCH, Gw,
+                     kShells ? fit_smem_shells(pad, nmeas, Gw) : fit_smem(pad)));
   return CDM_OK;
 }
 
@@ -719,7 +816,7 @@ cdm_status cdm_destroy(cdm_ctx* c) {
   if (!c) return CDM_OK;
   if (c->graph) cudaGraphExecDestroy(c->graph);
   void* bufs[] = {c->grid_dev, c->proto32, c->proto64, c->sig, c->gs_flags, c->gs_cand,
-                  c->gs_best, c->err, c->counters, c->h_meas, c->h_params, c->h_cfp, c->h_fixp,
+                  c->gs_best, c->shell_perm, c->shell_rank, c->err, c->counters, c->h_meas, c->h_params, c->h_cfp, c->h_fixp,
                   c->h_samples, c->h_tau, c->h_pred, c->h_bic, c->h_aic};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -806,22 +903,27 @@ cdm_status cdm_cost(cdm_ctx* c, int nvox, int nmeas, const double* meas, const d
     return cdm_fail(CDM_BAD_ARG, "null array");
   cudaStream_t st = (cudaStream_t)stream;
   CDM_TRY(prep_protocol(c, nmeas, CFP, st));
+  // the grid-search kernel with one "combination", the voxel's own
+  // parameters: the cost exactly as grid search and MCMC score it
+  const int Gw = pick_lanes(c, c->cfg.lanes_gridsearch, 2, nvox);
+  if (kShells)
+    CDM_TRY(prep_shells_and_pack(c, Gw, nvox, nmeas, CFP, meas, st));
+  else
+    CDM_TRY(pack_signals(c, Gw, nvox, nmeas, meas, st));
   if (nvox == 0) return CDM_OK;
-  cdm_post_args a;
+  cdm_gs_args a;
   std::memset(&a, 0, sizeof(a));
-  a.nvox = nvox;
-  a.nmeas = nmeas;
-  a.nmeas_pad = c->nmeas_pad;
-  a.nsamples = 1;
-  a.fixp_tsize = CDM_FIXP_TSIZE;
-  a.proto_bytes = (uint32_t)proto_bytes(c->nmeas_pad);
-  a.proto = c->proto32;
-  a.meas = meas;
+  fill_common(c, a, nvox, nmeas, Gw);
+  a.params = const_cast<double*>(params);  // read only when cost_only is set
   a.fixp = FixP;
-  a.err = c->err;
-  const size_t sm = proto_bytes(c->nmeas_pad);
-  CDM_TRY(set_smem(CDM_K_COST, 0, sm));
-  return k_cost(blocks_for(nvox, 32), sm, st, a, params, cost);
+  a.grid = nullptr;
+  a.ngp = 0;
+  a.combs = 1;
+  for (int p = 0; p < kNP; p++) a.gpos[p] = -1;
+  a.band = kGsBand;
+  a.cost_out = cost;
+  a.cost_only = 1;
+  return launch_gs_args(c, a, Gw, nvox, nmeas, st);
 }
 
 cdm_status cdm_select_worse(int n, const double* cost, const double* ref, double margin, int* idx,
@@ -970,11 +1072,9 @@ cdm_status cdm_fit_enqueue(cdm_ctx* c, int nvox, int nmeas, const double* meas, 
   if (cs == cudaStreamCaptureStatusActive) {
     // no allocation may happen under capture: the shape must be reserved
     const int pad = round_up(nmeas, 32);
-    size_t sig = 0;
-    for (int Gw : {1, 2, 4, 8, 16, 32})
-      sig = std::max(sig, (size_t)((nmeas + Gw - 1) / Gw) * std::max(nvox, 1) * Gw);
-    if (c->proto32_cap < (size_t)kNCOLS4 * pad || c->sig_cap < sig ||
-        c->gs_flags_cap < (size_t)std::max(nvox, 1))
+    if (c->proto32_cap < proto32_floats(pad, nmeas) || c->sig_cap < fit_sig_floats(c, nvox, nmeas) ||
+        c->gs_flags_cap < (size_t)std::max(nvox, 1) ||
+        (kShells && c->shell_perm_cap < (size_t)cdm_shell_max_pos(nmeas, 32)))
       return cdm_fail(CDM_BAD_ARG, "cdm_fit_enqueue under stream capture needs cdm_fit_reserve "
                                    "for this shape first");
   } else {

@@ -61,6 +61,24 @@ extern "C" __device__ __align__(256) unsigned char cdm_noalloc_scratch[kNoAllocS
     cdm_pack_signals_kernel<Gw>(meas, nvox, nmeas, nchunk, out);                              \
   }
 
+#if CDM_SHELLS
+#define CDM_W_PREP_SHELLS(Gw, _)                                                              \
+  extern "C" __global__ void cdm_k_prep_shells_##Gw(const double* __restrict__ cfp, int nmeas,  \
+                                                    int nmeas_pad, float* __restrict__ table,  \
+                                                    int* __restrict__ perm,                    \
+                                                    int* __restrict__ shell_rank) {            \
+    cdm_prep_shells_kernel<Gw>(cfp, nmeas, nmeas_pad, table, perm, shell_rank);                \
+  }
+#define CDM_W_PACK_SHELLS(Gw, _)                                                              \
+  extern "C" __global__ void cdm_k_pack_shell_signals_##Gw(                                   \
+      const double* __restrict__ meas, int nvox, int nmeas, int nchunk,                       \
+      const float* __restrict__ table, const int* __restrict__ perm, float* __restrict__ out) { \
+    cdm_pack_shell_signals_kernel<Gw>(meas, nvox, nmeas, nchunk, table, perm, out);           \
+  }
+CDM_LANES(CDM_W_PREP_SHELLS, 0)
+CDM_LANES(CDM_W_PACK_SHELLS, 0)
+#endif
+
 CDM_LANES(CDM_W_GS, 0)
 CDM_LANES(CDM_W_LM, 0)
 CDM_LANES(CDM_W_MC, 0)
@@ -73,9 +91,6 @@ extern "C" __global__ void __launch_bounds__(CDM_NT)
     cdm_k_predicted(const __grid_constant__ cdm_post_args a) { cdm_predicted_kernel(a); }
 extern "C" __global__ void __launch_bounds__(CDM_NT)
     cdm_k_bic_aic(const __grid_constant__ cdm_post_args a) { cdm_bic_aic_kernel(a); }
-extern "C" __global__ void __launch_bounds__(CDM_NT)
-    cdm_k_cost(const __grid_constant__ cdm_post_args a, const double* __restrict__ params,
-               double* __restrict__ cost) { cdm_cost_kernel(a, params, cost); }
 extern "C" __global__ void __launch_bounds__(CDM_NT)
     cdm_k_synth(const __grid_constant__ cdm_synth_args a) { cdm_synth_kernel(a); }
 extern "C" __global__ void cdm_k_select_worse(int n, const double* __restrict__ cost,

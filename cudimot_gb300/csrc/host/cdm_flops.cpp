@@ -159,6 +159,12 @@ extern "C" int cdm_describe(char* buf, int cap) {
 #ifdef CDM_SIGNAL_PAIR
   def("CDM_SIGNAL_PAIR", 1);
 #endif
+#ifdef CDM_SHELL_SERIES
+  def("CDM_SHELL_SERIES", 1);
+  def("CDM_SHELL_KEY", CDM_SHELL_KEY);
+  def("CDM_SHELL_NCOEF", CDM_SHELL_NCOEF);
+  def("CDM_SHELL_MCOLS", CDM_SHELL_MCOLS);
+#endif
 #ifdef CDM_MLP_HEAD
   def("CDM_MLP_HEAD", 1);
   def("CDM_MLP_NMU", CDM_MLP_NMU);

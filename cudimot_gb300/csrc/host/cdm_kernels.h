@@ -15,12 +15,13 @@ enum cdm_kfam : int {
   CDM_K_MCMC,
   CDM_K_MCMC_RICIAN,
   CDM_K_PACK_SIGNALS,
+  CDM_K_PREP_SHELLS,
+  CDM_K_PACK_SHELL_SIGNALS,
   CDM_K_NLANE_FAMILIES,
   // one instance each
   CDM_K_GS_RECHECK = CDM_K_NLANE_FAMILIES,
   CDM_K_PREDICTED,
   CDM_K_BIC_AIC,
-  CDM_K_COST,
   CDM_K_SELECT_WORSE,
   CDM_K_ROWS,
   CDM_K_PREP_PROTOCOL,
@@ -37,7 +38,8 @@ enum cdm_kfam : int {
 inline const char* cdm_kfam_name(int fam) {
   static const char* const names[CDM_K_COUNT] = {
       "gridsearch", "levmar",   "mcmc",        "mcmc_rician", "pack_signals",
-      "gs_recheck", "predicted", "bic_aic",    "cost",        "select_worse",
+      "prep_shells", "pack_shell_signals",
+      "gs_recheck", "predicted", "bic_aic",    "select_worse",
       "rows",       "prep_protocol", "params_to_samples", "synth", "mlp_encode",
       "mlp_decode", "clean_signals", "wait_selftest"};
   return fam >= 0 && fam < CDM_K_COUNT ? names[fam] : "";

@@ -37,6 +37,35 @@ constexpr int kPairTables = 0;
 
 constexpr int kGsTop = 4;
 
+// Per-shell series (plugins with the hook CDM_SHELL_SERIES, evaluated in
+// single precision): grid search and the Gaussian MCMC sum the signals of
+// each b-shell with per-shell coefficients (Shell_Coeffs /
+// Predicted_Signal_Shell_Pair). A prep kernel groups the measurements by
+// shell on the device; protocols with more than kShellMax shells, or whose
+// per-shell padding would add more than 1/8 of the measurements, keep the
+// per-measurement path (the shell table is then marked invalid).
+#if defined(CDM_SHELL_SERIES) && CDM_PAIRED
+#define CDM_SHELLS 1
+#else
+#define CDM_SHELLS 0
+#endif
+constexpr int kShellMax = 8;
+constexpr int kShellHeader = 32;  // ints: valid, nshell, npos, then per shell rep, pairs, first
+#ifndef CDM_SHELL_MCOLS
+#define CDM_SHELL_MCOLS 3
+#endif
+// Padded positions of a shell-ordered protocol of nmeas measurements at
+// most, with Gw lanes per voxel (each shell padded to whole pairs of lane
+// chunks).
+__host__ __device__ constexpr int cdm_shell_max_pos(int nmeas, int Gw) {
+  return nmeas + kShellMax * (2 * Gw - 1);
+}
+// Floats of the shell table that follows the staged protocol: the header,
+// then 4 floats (gx, gy, gz, weight) per padded position.
+__host__ __device__ constexpr int cdm_shell_table_floats(int nmeas, int Gw) {
+  return CDM_SHELLS ? kShellHeader + 4 * cdm_shell_max_pos(nmeas, Gw) : 0;
+}
+
 // Bounds, priors and fixed flags as the kernels use them. Bounds and prior
 // arguments are floats, as in CUDIMOT's __constant__ copies.
 struct cdm_limits {
@@ -61,9 +90,12 @@ struct cdm_gs_args {
   int combs;
   int gpos[kNP];       // column of parameter p in the grid, or -1
   float band;
+  int shells_staged;   // a shell table follows the protocol in the staged bytes
   int* flags;          // [nvox]: 0 decided, 1 recheck candidates, 2 recheck all
   int* cand;           // [nvox][kGsTop]
   int* best;           // [nvox] winning combination (or -1)
+  double* cost_out;    // [nvox] the winner's cost (FP32 terms, FP64 sum), or null
+  int cost_only;       // evaluate the cost at the voxel's own parameters (combs 1, no grid)
   int* err;
   cdm_limits lim;
 };
@@ -113,6 +145,7 @@ struct cdm_mcmc_args {
   uint32_t stream;
   uint32_t voxel_offset;
   const double* prop_sd;  // [nvox][NPARAMS] initial proposal widths; null or <= 0: P/10 as CUDIMOT
+  int shells_staged;      // a shell table follows the protocol in the staged bytes (Gaussian only)
   int* err;
   cdm_limits lim;
 };

@@ -162,6 +162,8 @@ struct cdm_voxel_io {
   int nmeas_pad;
   int lane;
   const float* pairs;  // this lane's first pair-table entry (paired hook only)
+  const int* shells;   // shell-table header in shared memory, or null (per-measurement path)
+  const float* stab;   // this lane's first shell pair entry
 };
 
 // Build the pair table (see the layout notes above) after the staged
@@ -184,6 +186,34 @@ __device__ __forceinline__ const float* cdm_build_pair_table(float* sproto, int 
   return reinterpret_cast<const float*>(ptab);
 }
 
+// Shell table (CDM_SHELLS; built by cdm_prep_shells_kernel right after the
+// protocol rows, staged with them): an int header - valid, nshell, npos,
+// then per shell its representative protocol row, its pairs per lane and
+// its first pair index - followed by one 8-float entry per (pair, lane):
+// (gx_a, gx_b, gy_a, gy_b, gz_a, gz_b, w_a, w_b) for the lane's two
+// measurements of the pair, w = 0 on padding positions. Measurements are
+// ordered shell by shell, each shell padded to whole pairs of lane chunks,
+// so the signals (packed in the same order) are walked chunk by chunk as
+// in the per-measurement path.
+// Prepare the shared-memory tables after staging: the shell table when the
+// host staged one and it is valid, else the pair table of the paired hook.
+template <int Gw>
+__device__ __forceinline__ const float* cdm_prepare_tables(float* sproto, int nmeas_pad, int nchunk,
+                                                           bool shells_staged, const int** hdr) {
+  *hdr = nullptr;
+#if CDM_SHELLS
+  if (shells_staged) {
+    const int* h = reinterpret_cast<const int*>(sproto + (size_t)nmeas_pad * kNCOLS4);
+    if (h[0]) {
+      *hdr = h;
+      return sproto + (size_t)nmeas_pad * kNCOLS4 + kShellHeader;
+    }
+    __syncthreads();  // every thread has read the flag before the table is overwritten
+  }
+#endif
+  return cdm_build_pair_table<Gw>(sproto, nmeas_pad, nchunk);
+}
+
 // One pair-table entry: the NCOLS column pairs of a lane's two measurements
 // (16-byte loads: entries are a whole number of 16-byte units).
 __device__ __forceinline__ void cdm_load_pairs(const float* q, float2* ab) {
@@ -200,9 +230,49 @@ __device__ __forceinline__ void cdm_load_pairs(const float* q, float2* ab) {
 // own measurements in FP32, the group total is formed in FP64. The loop walks
 // a protocol-row pointer and a signal pointer; chunks where every lane has a
 // measurement need no bounds test, only the last chunk may be partial.
+#if CDM_SHELLS
+static_assert(CDM_SHELL_MCOLS == 3, "shell pair entries hold three protocol columns and a weight");
+// Sum of squared residuals through the per-shell series: per shell, the
+// plugin forms its coefficients once (Shell_Coeffs, from the shell's
+// protocol row), then the lane's pairs of that shell are evaluated
+// (Predicted_Signal_Shell_Pair); padding positions have weight 0 and
+// signal 0, so r = w S - y vanishes there.
+template <int Gw>
+__device__ __forceinline__ double cdm_group_sse_shells(const cdm_voxel_io& io, const float* sproto,
+                                                       cdm_real* P, cdm_real* FixP,
+                                                       unsigned gmask) {
+  const int* hdr = io.shells;
+  const int nshell = hdr[1];
+  float2 acc2 = make_float2(0.0f, 0.0f);
+  const float* sig = io.sig;
+  for (int s = 0; s < nshell; s++) {
+    float coef[CDM_SHELL_NCOEF];
+    Shell_Coeffs(P, sproto + (size_t)hdr[4 + 3 * s] * kNCOLS4, FixP, coef);
+    const int npairs = hdr[5 + 3 * s];
+    const float4* q = reinterpret_cast<const float4*>(io.stab) + (size_t)hdr[6 + 3 * s] * Gw * 2;
+#pragma unroll kPairUnroll
+    for (int j = 0; j < npairs; j++) {
+      const float4 c01 = q[0], c2w = q[1];
+      const float2 g[3] = {make_float2(c01.x, c01.y), make_float2(c01.z, c01.w),
+                           make_float2(c2w.x, c2w.y)};
+      const float2 s2 = Predicted_Signal_Shell_Pair(P, coef, g);
+      const float2 r = __ffma2_rn(make_float2(c2w.z, c2w.w), s2,
+                                  make_float2(-sig[0], -sig[io.chunk_stride]));
+      acc2 = __ffma2_rn(r, r, acc2);
+      q += 2 * Gw;
+      sig += 2 * io.chunk_stride;
+    }
+  }
+  return cdm_group_sum<Gw>((double)(acc2.x + acc2.y), gmask);
+}
+#endif
+
 template <int Gw>
 __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const float* sproto,
                                                 cdm_real* P, cdm_real* FixP, unsigned gmask) {
+#if CDM_SHELLS
+  if (io.shells) return cdm_group_sse_shells<Gw>(io, sproto, P, FixP, gmask);
+#endif
   float acc = 0.0f;
   const int full = io.nmeas / Gw;
   const float* row = sproto + (size_t)io.lane * kNCOLS4;

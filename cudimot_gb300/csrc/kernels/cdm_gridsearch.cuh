@@ -39,7 +39,8 @@ template <int Gw>
 CDM_KERNEL(CDM_NT) cdm_gridsearch_kernel(CDM_KARG(cdm_gs_args) a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
-  const float* ptab = cdm_build_pair_table<Gw>(sproto, a.nmeas_pad, a.nchunk);
+  const int* shdr;
+  const float* ptab = cdm_prepare_tables<Gw>(sproto, a.nmeas_pad, a.nchunk, a.shells_staged != 0, &shdr);
   const int v = blockIdx.x * (CDM_NT / Gw) + (int)threadIdx.x / Gw;
   if (v >= a.nvox) return;
   const unsigned gm = cdm_group_mask<Gw>();
@@ -54,6 +55,8 @@ CDM_KERNEL(CDM_NT) cdm_gridsearch_kernel(CDM_KARG(cdm_gs_args) a) {
   io.nmeas_pad = a.nmeas_pad;
   io.lane = lane;
   io.pairs = ptab + (size_t)lane * kNCOLSP * 2;
+  io.shells = shdr;
+  io.stab = ptab + (size_t)lane * 8;
 
   double base[kNP];
 #pragma unroll
@@ -73,7 +76,7 @@ CDM_KERNEL(CDM_NT) cdm_gridsearch_kernel(CDM_KARG(cdm_gs_args) a) {
 #pragma unroll
     for (int p = 0; p < kNP; p++)
       trial[p] = a.gpos[p] >= 0 ? __ldg(a.grid + (size_t)c * a.ngp + a.gpos[p]) : base[p];
-    if (!cdm_gs_in_bounds(lim, trial)) continue;
+    if (!a.cost_only && !cdm_gs_in_bounds(lim, trial)) continue;
     cdm_real P[kNPS];
 #pragma unroll
     for (int i = 0; i < kNPS; i++) P[i] = cdm_real(0.0f);
@@ -98,6 +101,8 @@ CDM_KERNEL(CDM_NT) cdm_gridsearch_kernel(CDM_KARG(cdm_gs_args) a) {
     }
   }
   if (lane != 0) return;
+  if (a.cost_out) a.cost_out[v] = bcost[0];
+  if (a.cost_only) return;
   a.best[v] = bcomb[0];
   if (bcomb[0] < 0) {
     a.flags[v] = 0;

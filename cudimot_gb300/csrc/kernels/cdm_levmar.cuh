@@ -176,6 +176,8 @@ CDM_KERNEL(CDM_NT) cdm_levmar_kernel(CDM_KARG(cdm_lm_args) a) {
   io.nmeas_pad = a.nmeas_pad;
   io.lane = lane;
   io.pairs = ptab + (size_t)lane * kNCOLSP * 2;
+  io.shells = nullptr;
+  io.stab = nullptr;
 
   cdm_real P[kNPS], FixP[kNFIX];
   float Pt[kNP];

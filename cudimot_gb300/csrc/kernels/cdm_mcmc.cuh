@@ -99,7 +99,8 @@ template <int Gw, bool RICIAN>
 CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
-  const float* ptab = cdm_build_pair_table<Gw>(sproto, a.nmeas_pad, a.nchunk);
+  const int* shdr;
+  const float* ptab = cdm_prepare_tables<Gw>(sproto, a.nmeas_pad, a.nchunk, a.shells_staged != 0, &shdr);
   const int v = blockIdx.x * (CDM_NT / Gw) + (int)threadIdx.x / Gw;
   if (v >= a.nvox) return;
   const unsigned gm = cdm_group_mask<Gw>();
@@ -114,6 +115,8 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
   io.nmeas_pad = a.nmeas_pad;
   io.lane = lane;
   io.pairs = ptab + (size_t)lane * kNCOLSP * 2;
+  io.shells = shdr;
+  io.stab = ptab + (size_t)lane * 8;
 
   cdm_real P[kNPS], FixP[kNFIX];
   cdm_load_params(a.params + (size_t)v * kNP, P);

@@ -99,30 +99,6 @@ CDM_KERNEL(CDM_NT) cdm_bic_aic_kernel(CDM_KARG(cdm_post_args) a) {
   a.bic[v] = -2.0 * b + np * log(n);
 }
 
-// Cost of given parameters, as the LM and grid search score them: sum of
-// squared residuals (FP32 model, FP64 warp sum); a warp per voxel.
-CDM_KERNEL(CDM_NT) cdm_cost_kernel(CDM_KARG(cdm_post_args) a,
-                                                          const double* __restrict__ params,
-                                                          double* __restrict__ cost) {
-  extern __shared__ __align__(16) float sproto[];
-  if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
-  const int v = blockIdx.x * (CDM_NT / 32) + (int)threadIdx.x / 32;
-  if (v >= a.nvox) return;
-  const int lane = threadIdx.x & 31;
-  cdm_real P[kNPS], FixP[kNFIX];
-  cdm_load_params(params + (size_t)v * kNP, P);
-  cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
-  cdm_update_derived(P, FixP);
-  float acc = 0.0f;
-  for (int m = lane; m < a.nmeas; m += 32) {
-    cdm_real cf[kNCOLS];
-    cdm_load_cfp(sproto, a.nmeas_pad, m, cf);
-    const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - (float)a.meas[(size_t)v * a.nmeas + m];
-    acc = fmaf(r, r, acc);
-  }
-  const double tot = cdm_group_sum<32>((double)acc, 0xFFFFFFFFu);
-  if (lane == 0) cost[v] = tot;
-}
 
 // Row helpers of the learned initialiser's fallback (voxels whose cost
 // exceeds a reference cost by more than a margin are refit).
@@ -245,3 +221,104 @@ CDM_KERNEL0 cdm_wait_selftest_kernel(uint64_t limit_ns, int* err) {
   __syncthreads();
   cdm_mbar_wait_phase0(sbar, limit_ns, threadIdx.x == 0 ? err : nullptr);
 }
+
+#if CDM_SHELLS
+// Shell table of the per-shell series (see cdm_prepare_tables): one CTA.
+// Thread 0 assigns every measurement its shell (equal values of protocol
+// column CDM_SHELL_KEY; in order of first appearance, at most kShellMax)
+// and its rank in the shell, and lays the shells out one after another,
+// each padded to whole pairs of Gw-lane chunks; the table is marked invalid
+// (the kernels then take the per-measurement path) when there are more
+// shells or the padding would add more than nmeas / 8 positions. All
+// threads then fill perm (padded position -> measurement, -1 for padding)
+// and the pair entries. shell_rank: int scratch [nmeas].
+template <int Gw>
+CDM_KERNEL0 cdm_prep_shells_kernel(const double* __restrict__ cfp, int nmeas, int nmeas_pad,
+                                   float* __restrict__ table, int* __restrict__ perm,
+                                   int* __restrict__ shell_rank) {
+  int* hdr = reinterpret_cast<int*>(table);
+  __shared__ int s_valid, s_nshell, s_npos, s_start[kShellMax + 1];
+  if (threadIdx.x == 0) {
+    double key[kShellMax];
+    int count[kShellMax], rep[kShellMax];
+    int nshell = 0;
+    bool ok = true;
+    for (int m = 0; m < nmeas && ok; m++) {
+      const double b = cfp[(size_t)m * CDM_CFP_TSIZE + CDM_SHELL_KEY];
+      int s = 0;
+      while (s < nshell && key[s] != b) s++;
+      if (s == nshell) {
+        if (nshell == kShellMax) {
+          ok = false;
+          break;
+        }
+        key[s] = b;
+        count[s] = 0;
+        rep[s] = m;
+        nshell++;
+      }
+      shell_rank[m] = (s << 24) | count[s]++;
+    }
+    int npos = 0;
+    for (int s = 0; ok && s < nshell; s++) {
+      s_start[s] = npos;
+      const int padded = (count[s] + 2 * Gw - 1) / (2 * Gw) * (2 * Gw);
+      hdr[4 + 3 * s] = rep[s];
+      hdr[5 + 3 * s] = padded / (2 * Gw);
+      hdr[6 + 3 * s] = npos / (2 * Gw);
+      npos += padded;
+    }
+    ok = ok && nmeas < (1 << 24) && npos <= nmeas + nmeas / 8 && npos <= cdm_shell_max_pos(nmeas, Gw);
+    s_valid = ok ? 1 : 0;
+    s_nshell = ok ? nshell : 0;
+    s_npos = ok ? npos : 0;
+    hdr[0] = s_valid;
+    hdr[1] = s_nshell;
+    hdr[2] = s_npos;
+  }
+  __syncthreads();
+  if (!s_valid) return;
+  const int npos = s_npos;
+  float* ent = table + kShellHeader;
+  for (int p = threadIdx.x; p < npos; p += blockDim.x) perm[p] = -1;
+  for (int p = threadIdx.x; p < npos; p += blockDim.x) {
+    const int c = p / Gw, l = p % Gw;
+    float* e = ent + ((size_t)(c / 2) * Gw + l) * 8 + (c & 1);
+    e[0] = e[2] = e[4] = e[6] = 0.0f;
+  }
+  __syncthreads();
+  for (int m = threadIdx.x; m < nmeas; m += blockDim.x) {
+    const int sr = shell_rank[m];
+    const int p = s_start[sr >> 24] + (sr & 0xFFFFFF);
+    perm[p] = m;
+    const int c = p / Gw, l = p % Gw;
+    float* e = ent + ((size_t)(c / 2) * Gw + l) * 8 + (c & 1);
+#pragma unroll
+    for (int k = 0; k < CDM_SHELL_MCOLS; k++) e[2 * k] = (float)cfp[(size_t)m * CDM_CFP_TSIZE + k];
+    e[6] = 1.0f;
+  }
+}
+
+// Signals in the shell order of the table ([npos / Gw][nvox][Gw], 0 on
+// padding), or in measurement order as cdm_pack_signals_kernel when the
+// table is invalid.
+template <int Gw>
+CDM_KERNEL0 cdm_pack_shell_signals_kernel(const double* __restrict__ meas, int nvox, int nmeas,
+                                          int nchunk, const float* __restrict__ table,
+                                          const int* __restrict__ perm, float* __restrict__ out) {
+  const int* hdr = reinterpret_cast<const int*>(table);
+  const bool shells = hdr[0] != 0;
+  const int nc = shells ? hdr[2] / Gw : nchunk;
+  const size_t total = (size_t)nc * nvox * Gw;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(i % Gw);
+    const size_t rest = i / Gw;
+    const int v = (int)(rest % nvox);
+    const int c = (int)(rest / nvox);
+    const int p = c * Gw + j;
+    const int m = shells ? perm[p] : (p < nmeas ? p : -1);
+    out[i] = m >= 0 ? (float)meas[(size_t)v * nmeas + m] : 0.0f;
+  }
+}
+#endif

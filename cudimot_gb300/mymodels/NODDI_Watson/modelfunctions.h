@@ -412,6 +412,105 @@ __device__ __forceinline__ float2 Predicted_Signal_Pair(const fp32* P, const flo
   return __ffma2_rn(watson_bc(k3), ab[4],
                     __ffma2_rn(watson_bc(k1), extra, __fmul2_rn(watson_bc(k2), intra)));
 }
+
+// Per-shell series (optional hook CDM_SHELL_SERIES). Within one b-shell the
+// dispersed-stick sum is a degree-6 polynomial in y = x^2 whose
+// coefficients depend on the parameters only: intra(y) = sum_j alpha_j
+// q_j(y), alpha_0 = a_0(b), alpha_j = a_j(b) P[9+j] (the Legendre-Gaussian
+// columns of the shell times the Watson coefficients). Written in the
+// Chebyshev basis of t = 2y - 1 (q_j(y) = sum_k WATSON_CHEB[j][k] T_k(t),
+// entries <= 1.41, so single precision keeps ~1e-7 of S0), with the
+// compartment weights and the isotropic term folded into its
+// coefficients, the pair evaluation is Clenshaw's recurrence at two
+// operations per degree. Shell_Coeffs forms the coefficients once per
+// shell and parameter set from the shell's protocol row (columns: gx, gy,
+// gz, b, exp(-b Diso), a_0..a_6):
+//   coef[0..1]  exponent of the extra-cellular term as c0 + c1 x^2, base 2
+//   coef[2..8]  Clenshaw inputs h6, h5, h4 - h6, h3, h2, h1, h0* of
+//               k2 intra + k3 exp(-b Diso) (h_k = half the Chebyshev
+//               coefficient, h0* the whole one)
+//   coef[9..10] intra < 0 (the truncated series) becomes 0.5e-3 as in
+//               Predicted_Signal: below coef[9] the sum is replaced by coef[10]
+//   coef[11]    k1, the extra-cellular weight
+// The protocol columns the pair needs per measurement are gx, gy, gz.
+#define CDM_SHELL_SERIES 1
+#define CDM_SHELL_KEY 3      // measurements with equal b form a shell
+#define CDM_SHELL_NCOEF 12
+#define CDM_SHELL_MCOLS 3
+
+__device__ constexpr float WATSON_CHEB[7][7] = {
+    {1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f},
+    {0.25f, 0.75f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f},
+    {0.36160714285714257f, 0.8035714285714288f, 1.4062499999999998f, 0.0f, 0.0f, 0.0f, 0.0f},
+    {0.15536221590909216f, 0.3262606534090914f, 0.39151278409090917f, 0.7177734374999999f, 0.0f,
+     0.0f, 0.0f},
+    {0.26318359375001155f, 0.5414062500000156f, 0.5955468750000072f, 0.7373437500000009f,
+     1.3825195312499998f, 0.0f, 0.0f},
+    {0.12224713010651644f, 0.24902193169846143f, 0.2642681724146847f, 0.29730169396652073f,
+     0.3743799109207968f, 0.7113218307495117f, 0.0f},
+    {0.2170320620332813f, 0.43970132048254484f, 0.4580222088360886f, 0.49437317779102763f,
+     0.5635854226817418f, 0.7172905379585632f, 1.3748068644205729f}};
+
+__device__ __forceinline__ void Shell_Coeffs(const fp32* P, const float* row, const fp32* FixP,
+                                             float* coef) {
+  const float k3 = FixP[0].v * P[0].v;
+  const float k0 = FixP[0].v * (1.0f - P[0].v);
+  const float k1 = k0 * (1.0f - P[1].v), k2 = k0 * P[1].v;
+  const float nb = -1.4426950408889634f * row[3];
+  coef[0] = nb * P[8].v;
+  coef[1] = nb * P[9].v;
+  float al[7];
+  al[0] = row[5];
+#pragma unroll
+  for (int j = 1; j < 7; j++) al[j] = row[5 + j] * P[9 + j].v;
+  float e[7];
+#pragma unroll
+  for (int k = 0; k < 7; k++) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = k; j < 7; j++) acc = fmaf(al[j], WATSON_CHEB[j][k], acc);
+    e[k] = acc;
+  }
+  const float kh = 0.5f * k2, iso = k3 * row[4];
+  const float h6 = kh * e[6];
+  coef[2] = h6;
+  coef[3] = kh * e[5];
+  coef[4] = fmaf(kh, e[4], -h6);
+  coef[5] = kh * e[3];
+  coef[6] = kh * e[2];
+  coef[7] = kh * e[1];
+  coef[8] = fmaf(k2, e[0], iso);
+  coef[9] = iso;
+  coef[10] = fmaf(k2, 0.5e-3f, iso);
+  coef[11] = k1;
+}
+
+// The signal of two measurements of one shell: g[c] = column c (gx, gy,
+// gz) of both.
+__device__ __forceinline__ float2 Predicted_Signal_Shell_Pair(const fp32* P, const float* coef,
+                                                              const float2* g) {
+  float2 xv = __fmul2_rn(g[0], watson_bc(P[5].v));
+  xv = __ffma2_rn(g[1], watson_bc(P[6].v), xv);
+  xv = __ffma2_rn(g[2], watson_bc(P[7].v), xv);
+  const float2 x2 = __fmul2_rn(xv, xv);
+  const float2 z = __ffma2_rn(watson_bc(coef[1]), x2, watson_bc(coef[0]));
+  const float2 extra = make_float2(watson_ex2(z.x), watson_ex2(z.y));
+  // u = 2t = 4y - 2 at the cosine clamped to [-1, 1]
+  float2 u = __ffma2_rn(watson_bc(4.0f), x2, watson_bc(-2.0f));
+  u.x = fminf(u.x, 2.0f);
+  u.y = fminf(u.y, 2.0f);
+  const float2 b6 = watson_bc(coef[2]);
+  const float2 b5 = __ffma2_rn(u, b6, watson_bc(coef[3]));
+  const float2 b4 = __ffma2_rn(u, b5, watson_bc(coef[4]));
+  const float2 b3 = __ffma2_rn(u, b4, __fadd2_rn(watson_bc(coef[5]), make_float2(-b5.x, -b5.y)));
+  const float2 b2 = __ffma2_rn(u, b3, __fadd2_rn(watson_bc(coef[6]), make_float2(-b4.x, -b4.y)));
+  const float2 b1 = __ffma2_rn(u, b2, __fadd2_rn(watson_bc(coef[7]), make_float2(-b3.x, -b3.y)));
+  const float2 b0 = __ffma2_rn(u, b1, __fadd2_rn(watson_bc(coef[8]), make_float2(-b2.x, -b2.y)));
+  float2 f = __fadd2_rn(b0, make_float2(-b2.x, -b2.y));
+  if (f.x < coef[9]) f.x = coef[10];
+  if (f.y < coef[9]) f.y = coef[10];
+  return __ffma2_rn(watson_bc(coef[11]), extra, f);
+}
 #endif
 
 MACRO bool ConstraintsMCMC(int npar, T* P) { return true; }

@@ -16,7 +16,8 @@ land in oracle/_ref/.
 The plugins and the precision each is evaluated in: CUDIMOT's NODDI-Watson
 closed forms cancel terms of ~1e10 and are usable in double only, so it is
 built with --eval double (and once in float, to report what single precision
-does to it); the SSFP model is built in double as well.
+does to it); NODDI-Bingham (its signal misses the single-precision bound by
+two orders of magnitude) and the SSFP model are built in double as well.
 """
 import argparse
 import concurrent.futures as cf
@@ -31,7 +32,7 @@ from cudimot_gb300 import build  # noqa: E402
 
 OUT = os.path.join(HERE, "_ref", "dropin")
 DROPIN = (("Ball_1_Stick", "float"), ("NODDI_Watson", "double"), ("NODDI_Watson", "float"),
-          ("DiffusionTensor", "float"), ("Ball_2_Sticks", "float"), ("NODDI_Bingham", "float"),
+          ("DiffusionTensor", "float"), ("Ball_2_Sticks", "float"), ("NODDI_Bingham", "double"),
           ("toymodel", "float"), ("Ball_2_Sticks_1Shell_SSFP", "double"))
 
 

@@ -49,7 +49,9 @@ def lm_voxelwise(c_got, c_ref, ang=None, rtol=1e-4, adeg=0.5):
     """LM parity voxel by voxel: the library's final cost within rtol
     (relative) of the reference's and, where the angle between the fitted
     orientations is given, within adeg degrees; or else the library's cost
-    lower than the reference's. Returns (mask of failing voxels, report)."""
+    lower than the reference's. Returns (mask of voxels that are neither,
+    report: their number and largest cost excess, and how many voxels ended
+    lower by more than rtol)."""
     rel = (c_got - c_ref) / c_ref
     agree = np.abs(rel) <= rtol
     if ang is not None:
@@ -60,3 +62,15 @@ def lm_voxelwise(c_got, c_ref, ang=None, rtol=1e-4, adeg=0.5):
            "lower_by_more_than_rtol": int(np.sum(rel < -rtol)),
            "max_rel": float(rel.max())}
     return bad, rep
+
+
+def assert_lm_voxelwise(c_got, c_ref, ang=None, max_frac=0.0, max_excess=0.0):
+    """lm_voxelwise, asserted. A single-precision LM and an FP64 one from
+    the same start can part ways at a saddle or on a flat valley floor and
+    end at different stationary points, either side: voxels that neither
+    agree nor end lower are allowed up to max_frac of the voxels, each at
+    most max_excess (relative cost) above the reference. The report says how
+    many ended lower instead."""
+    bad, rep = lm_voxelwise(c_got, c_ref, ang)
+    assert bad.mean() <= max_frac and rep["max_excess"] <= max_excess, rep
+    return rep

@@ -22,7 +22,7 @@ import pytest
 import torch
 
 from cudimot_gb300 import capi
-from tests.helpers import lm_voxelwise, angle_deg, b2s, dt, oracle
+from tests.helpers import assert_lm_voxelwise, angle_deg, b2s, dt, oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -76,8 +76,7 @@ def test_levmar_diffusion_tensor(built, cuda):
     wl = dt(4000, seed=5)
     got, ref, c_got, c_ref = _lm("DiffusionTensor", wl, cuda)
     ang = angle_deg(*principal_dir(got), *principal_dir(ref))
-    bad, rep = lm_voxelwise(c_got, c_ref, ang)
-    assert not bad.any(), rep
+    assert_lm_voxelwise(c_got, c_ref, ang)
 
 
 def test_levmar_ball_2_sticks(built, cuda):
