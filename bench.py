@@ -263,7 +263,8 @@ def profile_mlp_forward(a, dev):
     e1.record()
     torch.cuda.synchronize()
     li.net.check()
-    print(json.dumps({"stage": "mlp_forward", "nvox": a.nvox, "ms": e0.elapsed_time(e1)}))
+    print(json.dumps({"stage": "mlp_forward", "nvox": a.nvox, "ms": e0.elapsed_time(e1),
+                      "hidden_layer": hidden_layer_roofline(li.net, dev, n=a.nvox)}))
 
 
 def profile_stage(a):
@@ -479,6 +480,39 @@ def param_error(m, truth):
             "orientation_median_deg": float(np.median(ang))}
 
 
+def hidden_layer_roofline(net, dev, n=262_144, reps=20):
+    """The network's second hidden layer (262,144 x 256 x 256, bias + GELU,
+    bf16 out; the persistent tcgen05 kernel) timed alone with CUDA events on
+    the launching stream, against the measured bf16 peak; HBM bytes are the
+    bf16 input read once and the output written once."""
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(5)
+    x = (torch.rand(n, net.cfg.hidden, generator=g) * 1.2).to(torch.bfloat16).to(dev)
+    out = torch.empty_like(x)
+    for _ in range(3):
+        net.hidden_layer(1, x, out)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        net.hidden_layer(1, x, out)
+    e1.record(st)
+    torch.cuda.synchronize()
+    net.check()
+    ms = e0.elapsed_time(e1) / reps
+    flop = 2.0 * n * net.cfg.hidden * net.cfg.hidden
+    tf = flop / (ms / 1e3) / 1e12
+    peaks = measured_peaks()
+    peak = peaks.get("bf16_tflops")
+    hbm = 2.0 * x.numel() * 2 / (ms / 1e3) / 1e9
+    return {"kernel": "umma_gelu_persistent_kernel", "shape": [n, net.cfg.hidden, net.cfg.hidden],
+            "launch_ms": ms, "achieved": tf, "unit": "TFLOP/s", "bound": "tensor",
+            "peak": peak, "frac": tf / peak if peak else None,
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)",
+            "hbm_gbs": hbm, "hbm_frac": hbm / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None}
+
+
 def learned_comparison(dev, train_signals=20_000_000, lm_targets=1_000_000, epochs=2,
                        n=1_000_000):
     """Network-initialised vs grid-initialised NODDI-Watson fits of the same
@@ -584,6 +618,7 @@ def learned_comparison(dev, train_signals=20_000_000, lm_targets=1_000_000, epoc
                 "voxels_worse_by_1pct": int(np.sum(rel > 0.01)),
                 "voxels_better_by_1pct": int(np.sum(rel < -0.01)),
                 "median_rel": float(np.median(rel)), "max_rel": float(rel.max())},
+            "network_hidden_layer": hidden_layer_roofline(li.net, dev),
             "training": {"signals": int(n_train), "epochs": epochs, "steps": int(steps),
                          "seconds": li.train_seconds, "data_seconds": t_data,
                          "tflops": 3 * flop_sample * steps * 4096 / li.train_seconds / 1e12,
@@ -601,7 +636,7 @@ def bench_learned(a, dev):
                      {"l2": "inputs larger than L2 (no flush)"},
                      clk.summary(), **{k: v for k, v in res.items() if k in (
                          "surrogate_init", "grid_init", "speedup", "audit_lm_cost_vs_grid_init",
-                         "training")})
+                         "network_hidden_layer", "training")})
     line["steps"], line["warmup"] = 1, 1
     print(json.dumps(line))
 

@@ -394,7 +394,8 @@ cdm_status check_common(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_
     return cdm_fail(CDM_BAD_ARG, "FixP_size " + std::to_string(FixP_size) +
                                      " != model FixP_Tsize " + std::to_string(CDM_FIXP_TSIZE));
   const int pad = round_up(nmeas, 32);
-  if (std::max(fit_smem(pad), fit_smem_shells(pad, nmeas, 32)) > 200 * 1024)
+  const size_t cap = std::min<size_t>(200 * 1024, 227 * 1024 - kMcmcStaticSmem - 1024);
+  if (std::max(fit_smem(pad), fit_smem_shells(pad, nmeas, 32)) > cap)
     return cdm_fail(CDM_BAD_ARG, "protocol too large for shared memory staging");
   return CDM_OK;
 }
@@ -1313,7 +1314,7 @@ extern "C" cdm_status cdm_levmar_noalloc(const cdm_model_cfg* cfg, int nvox, int
   if (CFP_size != CDM_CFP_TSIZE || FixP_size != CDM_FIXP_TSIZE)
     return cdm_fail(CDM_BAD_ARG, "CFP_size/FixP_size do not match the model");
   // the shared-memory bound of every other entry point (check_common)
-  if (fit_smem(round_up(nmeas, 32)) > 200 * 1024)
+  if (fit_smem(round_up(nmeas, 32)) > std::min<size_t>(200 * 1024, 227 * 1024 - kMcmcStaticSmem - 1024))
     return cdm_fail(CDM_BAD_ARG, "protocol too large for shared memory staging");
   unsigned char* scratch = nullptr;
   CDM_TRY(noalloc_scratch(&scratch));

@@ -36,6 +36,10 @@ constexpr int kPairTables = 0;
 #endif
 
 constexpr int kGsTop = 4;
+// Static shared memory of the MCMC kernel at one lane per voxel (its sample
+// staging buffer, cdm_record_sample) plus its barrier: the dynamic shared
+// memory the host allows leaves room for it.
+constexpr int kMcmcStaticSmem = CDM_NT * (kNP + 1) * 4 * 8 + 64;
 
 // Per-shell series (plugins with the hook CDM_SHELL_SERIES, evaluated in
 // single precision): grid search and the Gaussian MCMC sum the signals of

@@ -90,6 +90,27 @@ __device__ __forceinline__ double cdm_likelihood(const cdm_voxel_io& io, const f
   return (double)(0.5f * (float)io.nmeas * logf(0.5f * (float)sse));
 }
 
+// Records sample s of a sample row (element index row0 + s of dst, a row
+// of nsamples doubles). Samples are recorded every sampleevery iterations,
+// one double per row each time; written straight to global memory, each
+// would leave its 32-byte DRAM sector partly written for a long time, and a
+// partly written sector costs a read of the sector when it is evicted (the
+// read excess of the sampler's DRAM traffic). So the value is kept in the
+// row's shared-memory slot until the sector is complete - element index
+// = 3 mod 4, assuming dst 32-byte aligned (cudaMalloc and torch
+// allocations are 256-byte aligned) - or the row ends, and the sector's
+// elements of this row are then written back to back.
+__device__ __forceinline__ void cdm_record_sample(double (&buf)[4], double* dst, size_t row0,
+                                                  int s, int nsamples, double x) {
+  const size_t e = row0 + (size_t)s;
+  const int slot = (int)(e & 3);
+  buf[slot] = x;
+  if (slot == 3 || s == nsamples - 1) {
+    const int first = slot < s ? 0 : slot - s;  // elements of this row in the sector
+    for (int k = first; k <= slot; k++) dst[e - slot + k] = buf[k];
+  }
+}
+
 // Minimum resident CTAs per SM requested from the register allocator.
 #ifndef CDM_MCMC_MIN_BLOCKS
 #define CDM_MCMC_MIN_BLOCKS 4
@@ -101,7 +122,10 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
   const int* shdr;
   const float* ptab = cdm_prepare_tables<Gw>(sproto, a.nmeas_pad, a.nchunk, a.shells_staged != 0, &shdr);
-  const int v = blockIdx.x * (CDM_NT / Gw) + (int)threadIdx.x / Gw;
+  // recorded samples wait here until their 32-byte DRAM sector is complete
+  __shared__ double sbuf[CDM_NT / Gw][kNP + 1][4];
+  const int vloc = (int)threadIdx.x / Gw;
+  const int v = blockIdx.x * (CDM_NT / Gw) + vloc;
   if (v >= a.nvox) return;
   const unsigned gm = cdm_group_mask<Gw>();
   const int lane = (int)threadIdx.x % Gw;
@@ -257,12 +281,14 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
       if (recording && (it % a.sampleevery) == 0) {
         const int s = it / a.sampleevery;
         if (s < a.nsamples && lane == 0) {
-          double* dst = a.samples + (size_t)v * kNP * a.nsamples + s;
 #pragma unroll
           for (int p = 0; p < kNP; p++)  // fixed parameters: their input value, in double
-            dst[(size_t)p * a.nsamples] =
-                lim.fixed[p] ? a.params[(size_t)v * kNP + p] : (double)(float)P[p];
-          if (RICIAN && a.tau_samples) a.tau_samples[(size_t)v * a.nsamples + s] = (double)tau;
+            cdm_record_sample(sbuf[vloc][p], a.samples, ((size_t)v * kNP + p) * a.nsamples, s,
+                              a.nsamples,
+                              lim.fixed[p] ? a.params[(size_t)v * kNP + p] : (double)(float)P[p]);
+          if (RICIAN && a.tau_samples)
+            cdm_record_sample(sbuf[vloc][kNP], a.tau_samples, (size_t)v * a.nsamples, s,
+                              a.nsamples, (double)tau);
         }
       }
       if ((!recording || a.update_proposal) && it > 0 && (it % a.sampleevery) == 0) {

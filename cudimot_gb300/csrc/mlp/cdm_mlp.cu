@@ -102,6 +102,27 @@ cdm_status launch_bn(const CUtensorMap& ta, const CUtensorMap& tb, const gemm_ar
   return CDM_OK;
 }
 
+// The persistent hidden-layer kernel (inference: bias + GELU, bf16 out,
+// N <= 256): one CTA per SM.
+cdm_status launch_persistent(const CUtensorMap& ta, const CUtensorMap& tb, const gemm_args& a,
+                             cudaStream_t st) {
+  static int sms = 0;
+  static bool attr = false;
+  if (!attr) {
+    int dev = 0;
+    MLP_CUDA(cudaGetDevice(&dev));
+    MLP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    MLP_CUDA(cudaFuncSetAttribute(umma_gelu_persistent_kernel,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, pers::kAlloc));
+    attr = true;
+  }
+  const int tiles = (a.M + kBM - 1) / kBM;
+  umma_gelu_persistent_kernel<<<std::max(1, std::min(tiles, sms)), pers::kThreads, pers::kAlloc,
+                                st>>>(ta, tb, a);
+  MLP_CUDA(cudaGetLastError());
+  return CDM_OK;
+}
+
 template <int EPI>
 cdm_status launch_epi(int bn, const CUtensorMap& ta, const CUtensorMap& tb, const gemm_args& a,
                       cudaStream_t st) {
@@ -155,6 +176,10 @@ cdm_status run_gemm(const gemm& g, cudaStream_t st) {
     if (g.bn < 256 && g.a.N > g.bn && (g.a.N % g.bn) % 8)
       return fail(CDM_BAD_ARG, "bf16 GEMM tile remainder must be a multiple of 8");
   }
+  // inference hidden layers (no pre-activation or transposed copy) on the
+  // persistent kernel
+  if (g.epi == EPI_BIAS_GELU && !g.a.aux_bf16 && !g.a.out_t && g.a.N <= 256 && g.bn == 256)
+    return launch_persistent(g.ta, g.tb, g.a, st);
   switch (g.epi) {
     case EPI_F32: return launch_epi<EPI_F32>(g.bn, g.ta, g.tb, g.a, st);
     case EPI_BIAS_F32: return launch_epi<EPI_BIAS_F32>(g.bn, g.ta, g.tb, g.a, st);
@@ -630,6 +655,20 @@ cdm_status cdm_mlp_forward(cdm_mlp* m, const void* x, int n, float* out, void* s
                     out + (size_t)r0 * m->pad_out, false, st));
   }
   return CDM_OK;
+}
+
+cdm_status cdm_mlp_hidden_layer(cdm_mlp* m, int layer, const void* x, int ld_x, int n, void* out,
+                                int ld_out, void* stream) {
+  if (!m || !x || !out || n < 0 || layer < 0 || layer > 2) return fail(CDM_BAD_ARG, "bad argument");
+  if (ld_x < m->dims[layer] || ld_out < m->cfg.hidden) return fail(CDM_BAD_ARG, "bad leading dimension");
+  if (n == 0) return CDM_OK;
+  gemm g;
+  MLP_TRY(make_gemm(&g, x, ld_x, m->wb[layer], m->dims[layer], n, m->cfg.hidden, m->dims[layer],
+                    EPI_BIAS_GELU, m->err));
+  g.a.bias = m->bias[layer];
+  g.a.ld_out = ld_out;
+  g.a.out_bf16 = (__nv_bfloat16*)out;
+  return run_gemm(g, (cudaStream_t)stream);
 }
 
 cdm_status cdm_mlp_prep_input(const double* meas, const double* s0, int s0_ld, int n, int nmeas,

@@ -160,14 +160,32 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// GELU in its tanh form, 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))),
+// with the hardware tanh approximation (tanh.approx.f32, relative error
+// ~2^-11, below the bf16 rounding the activations get): five FP32
+// operations and one MUFU instead of an erf. The network is defined with
+// this form (training and inference), and the CPU oracle restates it.
+constexpr float kGeluC0 = 0.7978845608028654f;               // sqrt(2/pi)
+constexpr float kGeluC1 = 0.7978845608028654f * 0.044715f;
+
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ float gelu(float z) {
-  return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f));
+  const float t = tanh_approx(z * fmaf(kGeluC1, z * z, kGeluC0));
+  const float hz = 0.5f * z;
+  return fmaf(hz, t, hz);
 }
 
 __device__ __forceinline__ float gelu_grad(float z) {
-  const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * __expf(-0.5f * z * z);
-  return cdf + z * pdf;
+  const float z2 = z * z;
+  const float t = tanh_approx(z * fmaf(kGeluC1, z2, kGeluC0));
+  // d/dz: 0.5 (1 + t) + 0.5 z (1 - t^2) (c0 + 3 c1 z^2)
+  const float du = fmaf(3.0f * kGeluC1, z2, kGeluC0);
+  return fmaf(0.5f * z * fmaf(-t, t, 1.0f), du, 0.5f * (1.0f + t));
 }
 
 // TMEM columns to allocate for BN accumulator columns (power of two >= 32).
@@ -378,6 +396,201 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(tmem_cols(BN)));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent hidden layer for inference: out_bf16 = bf16(gelu(bf16(A B^T +
+// bias))) with N <= 256 (one 256-wide tile column), any M. One CTA per SM
+// loops over the 128-row tiles (tile blockIdx.x, then every gridDim.x-th):
+//   * warp 0, lane 0 - TMA producer over a 4-stage ring (A 128x64 and B
+//     256x64 boxes), across tile boundaries;
+//   * warp 1, lane 0 - MMA issuer; it accumulates tile j in one of two TMEM
+//     accumulators (columns 256 (j & 1) .. +255 of a 512-column allocation),
+//     so the MMAs of tile j+1 run while the epilogue drains tile j;
+//   * warps 2..9 - epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (its
+//     32 rows) and columns 128 ((w - 2) / 4) .. +127 of the accumulator, 32
+//     at a time; bias (staged in shared memory), GELU, bf16; each 32 x 32
+//     block goes through a per-warp shared-memory buffer so that the global
+//     stores are whole 16-byte pieces, 64 contiguous bytes per row; then the
+//     warp releases the accumulator (acc_empty, 8 arrivals).
+// Every wait is bounded (2 s): on expiry the CTA stops its loops, records
+// kErrTimeout and still releases its tensor memory.
+namespace pers {
+constexpr int kBN = 256;
+constexpr int kStages = 4;
+constexpr int kEpiWarps = 8;
+constexpr int kThreads = 32 * (2 + kEpiWarps);
+constexpr int kABytes = kBM * kBK * 2;            // 16 KB
+constexpr int kBBytes = kBN * kBK * 2;            // 32 KB
+constexpr int kStageBytes = kABytes + kBBytes;    // 48 KB
+constexpr int kOutLd = 40;                        // bf16 per staged row (32 + 8: 80 B)
+constexpr int kOutBytes = 32 * kOutLd * 2;        // per epilogue warp
+constexpr int kOffOut = kStages * kStageBytes;
+constexpr int kOffBias = kOffOut + kEpiWarps * kOutBytes;
+constexpr int kOffBar = kOffBias + kBN * 4;
+constexpr int kBytes = kOffBar + (2 * kStages + 4) * 8 + 16;
+constexpr int kAlloc = kBytes + 1024;  // slack for the 1024-byte alignment of the stages
+static_assert(kAlloc <= 227 * 1024, "shared memory of the persistent GEMM");
+}  // namespace pers
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__global__ void __launch_bounds__(pers::kThreads, 1)
+    umma_gelu_persistent_kernel(const __grid_constant__ CUtensorMap tmA,
+                                const __grid_constant__ CUtensorMap tmB,
+                                const __grid_constant__ gemm_args a) {
+  using namespace pers;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + kOffBar);
+  uint64_t* empty = full + kStages;
+  uint64_t* acc_full = empty + kStages;
+  uint64_t* acc_empty = acc_full + 2;
+  uint32_t* tmem_slot = (uint32_t*)(acc_empty + 2);
+  float* sbias = (float*)(smem + kOffBias);
+  __shared__ int abort_flag;
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int ntiles = (a.M + kBM - 1) / kBM;
+  const int nk = (a.K + kBK - 1) / kBK;
+  const int ncols = min(kBN, a.N);
+
+  if (threadIdx.x == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < kStages; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], kEpiWarps);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+  }
+  for (int i = threadIdx.x; i < kBN; i += blockDim.x) sbias[i] = i < a.N ? a.bias[i] : 0.0f;
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      uint32_t g = 0;
+      for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        for (int kt = 0; kt < nk; kt++, g++) {
+          const uint32_t s = g % kStages;
+          if (g >= (uint32_t)kStages && !mbar_wait(&empty[s], ((g / kStages) - 1) & 1)) {
+            atomicExch(&abort_flag, 1);
+            t = ntiles;
+            break;
+          }
+          if (*(volatile int*)&abort_flag) {
+            t = ntiles;
+            break;
+          }
+          unsigned char* st = smem + s * kStageBytes;
+          mbar_expect_tx(&full[s], kStageBytes);
+          tma_load_2d(st, &tmA, &full[s], kt * kBK, t * kBM);
+          tma_load_2d(st + kABytes, &tmB, &full[s], kt * kBK, 0);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = instr_desc_bf16(kBM, kBN);
+      uint32_t g = 0;
+      int j = 0;
+      for (int t = blockIdx.x; t < ntiles; t += gridDim.x, j++) {
+        const int b = j & 1;
+        if (j >= 2 && !mbar_wait(&acc_empty[b], ((j >> 1) - 1) & 1)) {
+          atomicExch(&abort_flag, 1);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t acc = tmem + (uint32_t)(b * kBN);
+        bool ok = true;
+        for (int kt = 0; kt < nk; kt++, g++) {
+          const uint32_t s = g % kStages;
+          if (!mbar_wait(&full[s], (g / kStages) & 1)) {
+            atomicExch(&abort_flag, 1);
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t sa = smem_u32(smem + s * kStageBytes);
+          const uint32_t sb = sa + kABytes;
+#pragma unroll
+          for (int k = 0; k < kBK / 16; k++)
+            mma_bf16(acc, smem_desc(sa + k * 32), smem_desc(sb + k * 32), idesc,
+                     (kt > 0 || k > 0) ? 1u : 0u);
+          mma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        mma_commit(&acc_full[b]);
+      }
+    }
+  } else {
+    const int q = warp % 4;             // TMEM lane quarter this warp may read
+    const int h = (warp - 2) / 4;       // column half of the accumulator
+    __nv_bfloat16* stage = reinterpret_cast<__nv_bfloat16*>(smem + kOffOut + (warp - 2) * kOutBytes);
+    int j = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, j++) {
+      const int b = j & 1;
+      if (!mbar_wait(&acc_full[b], (j >> 1) & 1)) {
+        atomicExch(&abort_flag, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int r0 = t * kBM + 32 * q;  // first global row of this warp
+      const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * kBN);
+#pragma unroll 1
+      for (int c = 0; c < 4; c++) {
+        const int c0 = h * 128 + 32 * c;
+        float v[32];
+        tmem_ld32(base + (uint32_t)c0, v);
+        uint32_t o[16];  // bf16 pairs
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+          const float z0 = __bfloat162float(__float2bfloat16(v[2 * i] + sbias[c0 + 2 * i]));
+          const float z1 = __bfloat162float(__float2bfloat16(v[2 * i + 1] + sbias[c0 + 2 * i + 1]));
+          const __nv_bfloat162 g2 = __floats2bfloat162_rn(gelu(z0), gelu(z1));
+          o[i] = *reinterpret_cast<const uint32_t*>(&g2);
+        }
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+          *reinterpret_cast<uint4*>(stage + lane * kOutLd + 8 * p) =
+              make_uint4(o[4 * p], o[4 * p + 1], o[4 * p + 2], o[4 * p + 3]);
+        __syncwarp();
+#pragma unroll
+        for (int p = lane; p < 128; p += 32) {
+          const int r = p >> 2, col = c0 + 8 * (p & 3);
+          if (r0 + r < a.M && col < ncols)
+            *reinterpret_cast<uint4*>(a.out_bf16 + (size_t)(r0 + r) * a.ld_out + col) =
+                *reinterpret_cast<const uint4*>(stage + r * kOutLd + 8 * (p & 3));
+        }
+        __syncwarp();
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[b]);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (abort_flag && threadIdx.x == 0 && a.err) atomicExch(a.err, kErrTimeout);
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
   }
 }
 

@@ -38,6 +38,7 @@ def lib():
             "cdm_mlp_forward": [vp, vp, i, vp, vp],
             "cdm_mlp_prep_input": [vp, vp, i, i, i, i, vp, vp],
             "cdm_mlp_gemm_bf16": [vp, i, vp, i, i, i, i, vp, i, vp],
+            "cdm_mlp_hidden_layer": [vp, i, vp, i, i, vp, i, vp],
             "cdm_mlp_check": [vp],
         }
         for n, a in sig.items():
@@ -162,6 +163,12 @@ class Mlp:
             out = torch.zeros(n, 16, dtype=torch.float32, device=x.device)
         _check(lib().cdm_mlp_forward(self.h, _p(x), n, _p(out), _stream()), "forward")
         return out
+
+    def hidden_layer(self, layer, x, out):
+        """One hidden layer of inference alone: out = bf16(gelu(x W^T + b))
+        (bf16 CUDA tensors [n][width])."""
+        _check(lib().cdm_mlp_hidden_layer(self.h, layer, _p(x), x.stride(0), x.shape[0], _p(out),
+                                          out.stride(0), _stream()), "hidden_layer")
 
     def check(self):
         _check(lib().cdm_mlp_check(self.h), "device check")

@@ -6,8 +6,8 @@
  * deviations; the means seed LM (replacing the grid search) and the
  * standard deviations seed the MCMC proposal widths.
  *
- * Network: n_in -> hidden -> hidden -> hidden -> n_mu + n_sig, GELU, BF16
- * weights and activations, FP32 accumulation on the tensor cores
+ * Network: n_in -> hidden -> hidden -> hidden -> n_mu + n_sig, GELU (tanh
+ * form), BF16 weights and activations, FP32 accumulation on the tensor cores
  * (tcgen05.mma, TMA-fed), FP32 master weights, Adam. Loss: Gaussian
  * negative log-likelihood, mean j against log-std group[j].
  *
@@ -57,6 +57,11 @@ cdm_status cdm_mlp_gradients(cdm_mlp* m, const void* x, const float* targets, in
 /* Inference on n rows. */
 cdm_status cdm_mlp_forward(cdm_mlp* m, const void* x, int n, float* out, void* stream);
 
+/* One hidden layer (0..2) of inference alone, for tests and timing:
+ * out bf16 [n][ld_out] = bf16(gelu(bf16(x W_l^T + b_l))), x bf16 [n][ld_x]
+ * with the layer's input width; the kernel cdm_mlp_forward runs for it. */
+cdm_status cdm_mlp_hidden_layer(cdm_mlp* m, int layer, const void* x, int ld_x, int n, void* out,
+                                int ld_out, void* stream);
 /* x[r][c] = meas[r][c] / s0[r * s0_ld] (s0 null: 1) as bf16 [n][ld],
  * columns nmeas..ld-1 zero. */
 cdm_status cdm_mlp_prep_input(const double* meas, const double* s0, int s0_ld, int n, int nmeas,

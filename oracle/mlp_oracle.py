@@ -1,7 +1,7 @@
 """CPU oracle of the learned initialiser's network (test infrastructure).
 
 Restates, in numpy, what libcdm_mlp computes on the tensor cores:
-forward n_in -> H -> H -> H -> n_out with GELU (erf form), the Gaussian
+forward n_in -> H -> H -> H -> n_out with GELU (tanh form), the Gaussian
 negative log-likelihood head and the backward pass, with the library's
 rounding points when `bf16=True`:
   * GEMM operands (inputs, weights, activations, output gradients) are
@@ -11,14 +11,7 @@ rounding points when `bf16=True`:
 With `bf16=False` and float64 arrays it is the exact network, which the
 tests check against finite differences (pinning the oracle itself).
 """
-import math
-
 import numpy as np
-
-try:
-    from scipy.special import erf as _erf
-except ImportError:  # pragma: no cover
-    _erf = np.vectorize(math.erf)
 
 
 def bf16(x):
@@ -29,14 +22,18 @@ def bf16(x):
     return r.astype(np.uint32).view(np.float32).reshape(x.shape)
 
 
+_C0 = np.sqrt(2.0 / np.pi)
+_C1 = _C0 * 0.044715
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / np.sqrt(2.0)))
+    """GELU in its tanh form, as the library defines the network."""
+    return 0.5 * z * (1.0 + np.tanh(z * (_C0 + _C1 * z * z)))
 
 
 def gelu_grad(z):
-    cdf = 0.5 * (1.0 + _erf(z / np.sqrt(2.0)))
-    pdf = np.exp(-0.5 * z * z) / np.sqrt(2.0 * np.pi)
-    return cdf + z * pdf
+    t = np.tanh(z * (_C0 + _C1 * z * z))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * (_C0 + 3.0 * _C1 * z * z)
 
 
 class MlpOracle:

@@ -100,3 +100,32 @@ def test_adam_training_lowers_loss(built, cuda):
     net.check()
     assert np.isfinite(hist).all()
     assert hist[-1] < hist[0] - 2.0, hist
+
+
+@pytest.mark.parametrize("layer,n", [(0, 300), (1, 262144 + 77)])
+def test_hidden_layer_matches_reference(built, cuda, layer, n):
+    """One inference hidden layer (the persistent tcgen05 kernel: one CTA
+    per SM looping over 128-row tiles, two TMEM accumulators) against an
+    FP32 matmul of the same bf16 operands with the library's rounding
+    points: z = bf16(x W^T + b), out = bf16(gelu(z)). 262,221 rows give
+    2,049 tiles, so every CTA runs many tiles and the last one is ragged.
+    A z that lands on the other side of a bf16 rounding (different
+    accumulation order) moves its output by one bf16 step: the bound is two
+    steps plus a small absolute term near zero."""
+    from oracle.mlp_oracle import gelu
+    cfg, net, _ = _net(seed=2)
+    W, b, _, _ = net.get_params(grads=True)
+    g = torch.Generator(device="cpu").manual_seed(n + layer)
+    width = cfg.n_in if layer == 0 else cfg.hidden
+    x = (torch.rand(n, width, generator=g) * 1.2).to(torch.bfloat16).to(cuda)
+    out = torch.full((n, cfg.hidden), float("nan"), dtype=torch.bfloat16, device=cuda)
+    net.hidden_layer(layer, x, out)
+    torch.cuda.synchronize()
+    net.check()
+    w = torch.as_tensor(bf16(W[layer])).to(cuda)
+    z = (x.float() @ w.T + torch.as_tensor(b[layer]).to(cuda)).to(torch.bfloat16).float()
+    ref = torch.as_tensor(gelu(z.cpu().numpy().astype(np.float64))).to(torch.bfloat16).float()
+    got = out.float().cpu()
+    assert torch.isfinite(got).all()
+    err = (got - ref).abs()
+    assert bool((err <= 2.0 ** -6 * ref.abs() + 2e-3).all()), float(err.max())
