@@ -599,6 +599,15 @@ cdm_status launch_mcmc(cdm_ctx* c, int Gw, bool rician, int nvox, int nmeas, dou
     a.proto_bytes = (uint32_t)(proto_bytes(c->nmeas_pad) + shell_bytes(nmeas, Gw));
     sm = fit_smem_shells(c->nmeas_pad, nmeas, Gw);
   }
+  // custom priors: a [nmeas][CFP_Tsize] copy of the protocol after the tables
+  a.cfp_all_off = -1;
+  for (int p = 0; p < kNP; p++)
+    if (c->lim.ptype[p] == kCustomPrior) a.cfp_all_off = (int)((sm + 7) / 8 * 2);
+  if (a.cfp_all_off >= 0) {
+    sm = (size_t)a.cfp_all_off * 4 + (size_t)nmeas * CDM_CFP_TSIZE * kRealBytes;
+    if (sm > 227 * 1024 - (size_t)kMcmcStaticSmem - 1024)
+      return cdm_fail(CDM_BAD_ARG, "protocol too large for the custom priors' copy of it");
+  }
   CDM_TRY(set_smem(fam, Gw, sm));
   return launch(fam, Gw, blocks_for(nvox, Gw), CDM_NT, sm, st, a);
 }

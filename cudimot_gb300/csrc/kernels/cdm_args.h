@@ -36,6 +36,12 @@ constexpr int kPairTables = 0;
 #endif
 
 constexpr int kGsTop = 4;
+constexpr int kCustomPrior = 5;  // prior type CUSTOM (cudimot.h)
+#ifdef CDM_EVAL_DOUBLE
+constexpr int kRealBytes = 8;    // bytes of the plugin's evaluation type
+#else
+constexpr int kRealBytes = 4;
+#endif
 // Static shared memory of the MCMC kernel at one lane per voxel (its sample
 // staging buffer, cdm_record_sample) plus its barrier: the dynamic shared
 // memory the host allows leaves room for it.
@@ -150,6 +156,8 @@ struct cdm_mcmc_args {
   uint32_t voxel_offset;
   const double* prop_sd;  // [nvox][NPARAMS] initial proposal widths; null or <= 0: P/10 as CUDIMOT
   int shells_staged;      // a shell table follows the protocol in the staged bytes (Gaussian only)
+  int cfp_all_off;        // float offset in shared memory of the [nmeas][CFP_Tsize] copy of
+                          // the protocol that custom priors receive, or -1 (no custom prior)
   int* err;
   cdm_limits lim;
 };

@@ -64,6 +64,9 @@ typedef fp32 cdm_real;
 #define CDM_KARG(T) const __grid_constant__ T
 #endif
 
+static_assert(CUSTOM == kCustomPrior, "prior type CUSTOM");
+static_assert(sizeof(cdm_real) == kRealBytes, "evaluation type size");
+
 // Error codes written to the device error word.
 #define CDM_DEVERR_STAGE_TIMEOUT 1
 

@@ -86,8 +86,13 @@ __device__ __forceinline__ double cdm_likelihood(const cdm_voxel_io& io, const f
     const double s = cdm_group_rician<Gw>(io, sproto, P, FixP, tau, gmask);
     return -(double)io.nmeas * (double)logf(tau) - s;
   }
+  // (n/2) log(SSE/2) with SSE kept in FP64: log(m 2^e) = log m + e log 2,
+  // the mantissa's log in FP32 (absolute error ~6e-8 for m in [0.5, 1))
+  // and the rest exact, instead of the FP32 log of a value of ~1e6 (1e-6)
   const double sse = cdm_group_sse<Gw>(io, sproto, P, FixP, gmask);
-  return (double)(0.5f * (float)io.nmeas * logf(0.5f * (float)sse));
+  int ex;
+  const double m = frexp(0.5 * sse, &ex);
+  return 0.5 * (double)io.nmeas * ((double)logf((float)m) + (double)ex * 0.69314718055994531);
 }
 
 // Records sample s of a sample row (element index row0 + s of dst, a row
@@ -122,6 +127,12 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
   const int* shdr;
   const float* ptab = cdm_prepare_tables<Gw>(sproto, a.nmeas_pad, a.nchunk, a.shells_staged != 0, &shdr);
+  if (a.cfp_all_off >= 0) {  // the protocol as custom priors see it
+    cdm_real* dst = reinterpret_cast<cdm_real*>(sproto + a.cfp_all_off);
+    for (int i = (int)threadIdx.x; i < a.nmeas * CDM_CFP_TSIZE; i += CDM_NT)
+      dst[i] = cdm_real(sproto[(size_t)(i / CDM_CFP_TSIZE) * kNCOLS4 + i % CDM_CFP_TSIZE]);
+    __syncthreads();
+  }
   // recorded samples wait here until their 32-byte DRAM sector is complete
   __shared__ double sbuf[CDM_NT / Gw][kNP + 1][4];
   const int vloc = (int)threadIdx.x / Gw;
@@ -156,11 +167,9 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
   int tacc = 0, trej = 0;
   const uint32_t vid = a.voxel_offset + (uint32_t)v;
   const int nburn = a.nburn < 1 ? 1 : a.nburn;
-  // Custom priors receive the whole CFP array in CUDIMOT; with the staged
-  // SoA table there is no AoS copy, so they see the voxel's first
-  // measurement only (no shipped plugin defines one).
-  cdm_real cf0[kNCOLS];
-  cdm_load_cfp(sproto, a.nmeas_pad, 0, cf0);
+  // custom priors receive the whole CFP array, [nmeas][CFP_Tsize], as in
+  // CUDIMOT (MCMC.cu custom_priors); the copy is built by the CTA below
+  cdm_real* cf0 = a.cfp_all_off >= 0 ? reinterpret_cast<cdm_real*>(sproto + a.cfp_all_off) : nullptr;
 
   double energy = 0.0;
   bool stale = false;  // derived values of P out of date (after a rejection)

@@ -5,7 +5,8 @@
     steps run eagerly, bit for bit, and twice in a row;
   * the steps do what the scripts do: the grid search leaves theta/phi at
     the tensor fit's V1, FitFractions leaves kappa at the grid value, and
-    the final fit's cost is no worse than the grid search's;
+    the final fit's cost is no worse than the grid search's; and each stage
+    matches the FP64 oracle's run of the same stage from the same input;
   * Ball_1_Stick's and Ball_2_Sticks' one-step pipelines from the tensor
     fit match LM from the same initial values;
   * NODDI-Bingham's pipeline (grid search + LM with the orientation fixed,
@@ -17,7 +18,7 @@ import torch
 
 from cudimot_gb300 import capi
 from cudimot_gb300.pipeline import Pipeline
-from tests.helpers import b1s, oracle, watson
+from tests.helpers import angle_deg, assert_lm_voxelwise, b1s, oracle, watson
 
 pytestmark = pytest.mark.gpu
 
@@ -49,9 +50,16 @@ def test_watson_pipeline_graph_equals_eager(built, cuda):
 
 
 def test_watson_pipeline_steps(built, cuda):
+    """Pipeline_NODDI_Watson.sh's staged --fixed sequence, stage by stage,
+    against the FP64 oracle run from the same input as each GPU stage: the
+    b=0 mean (S0, FixP), the grid search with the orientation fixed (winners
+    bit for bit), FitFractions (LM with kappa and orientation fixed) and
+    the full fit (LM), both held to the LM parity bounds of the library's
+    own NODDI-Watson test."""
     wl = watson(1024, seed=32)
     m = T(wl.meas, cuda)
     pl = Pipeline("NODDI_Watson", m, wl.cfp[:, :3], wl.cfp[:, 3])
+    o = oracle("NODDI_Watson")
     # step by step, inspecting the shared parameter array
     from cudimot_gb300 import utils
     utils.mean_columns(m, pl.b0, pl.fixp)
@@ -61,24 +69,37 @@ def test_watson_pipeline_steps(built, cuda):
             utils.copy_columns(None, 0, pl.params, p, 1, scale)
         else:
             utils.copy_columns(pl.dti, utils.DTI_COLS.index(col), pl.params, p, 1, scale)
+    torch.cuda.synchronize()
+    f = pl.fixp.cpu().numpy()
+    b0 = wl.cfp[:, 3] <= 50.0
+    np.testing.assert_allclose(f[:, 0], wl.meas[:, b0].mean(1), rtol=1e-13)
+    start = pl.params.cpu().numpy().copy()
     st, lib, samples = pl.ctx[0]
     lib.fit_enqueue(m, pl.params, pl.cfp, pl.fixp, samples)
     torch.cuda.synchronize()
     after_gs = pl.params.cpu().numpy().copy()
     np.testing.assert_array_equal(after_gs[:, 3:5], pl.dti.cpu().numpy()[:, 12:14])
+    ref_gs, _, _ = o.gridsearch(lib.cfg, wl.meas, start, wl.cfp, f)
+    np.testing.assert_array_equal(after_gs, ref_gs)
     st, lib, samples = pl.ctx[1]
     lib.fit_enqueue(m, pl.params, pl.cfp, pl.fixp, samples)
     torch.cuda.synchronize()
     after_ff = pl.params.cpu().numpy().copy()
     np.testing.assert_array_equal(after_ff[:, 2:5], after_gs[:, 2:5])
+    ref_ff = o.levmar(lib.cfg, wl.meas, after_gs, wl.cfp, f)[0]
+    np.testing.assert_array_equal(ref_ff[:, 2:5], after_gs[:, 2:5])
+    assert_lm_voxelwise(o.cost(wl.meas, after_ff, wl.cfp, f), o.cost(wl.meas, ref_ff, wl.cfp, f),
+                        max_frac=0.0075, max_excess=0.01)
     st, lib, samples = pl.ctx[2]
     lib.fit_enqueue(m, pl.params, pl.cfp, pl.fixp, samples)
     torch.cuda.synchronize()
     final = pl.params.cpu().numpy()
-    o = oracle("NODDI_Watson")
-    f = pl.fixp.cpu().numpy()
-    c_gs = o.cost(wl.meas, after_gs, wl.cfp, f)
+    ref_fin = o.levmar(lib.cfg, wl.meas, after_ff, wl.cfp, f)[0]
+    ang = angle_deg(final[:, 3], final[:, 4], ref_fin[:, 3], ref_fin[:, 4])
     c_fin = o.cost(wl.meas, final, wl.cfp, f)
+    assert_lm_voxelwise(c_fin, o.cost(wl.meas, ref_fin, wl.cfp, f), ang, max_frac=0.0075,
+                        max_excess=0.01)
+    c_gs = o.cost(wl.meas, after_gs, wl.cfp, f)
     assert np.mean(c_fin <= c_gs * (1 + 1e-6)) >= 0.99
 
 

@@ -5,8 +5,9 @@ split_parts rule) with the voxel index offset by the range start, the ranks
 gather the results and reduce their step times with MAX (as bench.py
 does). Because the fit of a voxel depends only on the voxel and its global
 index (MCMC draws are keyed by it), the gathered result must equal the
-single-process fit exactly. The per-rank fit here is the CPU oracle; the
-GPU library is exercised by the gpu tests."""
+single-process fit exactly. The per-rank fit is the CPU oracle, and, where
+a GPU is present, the library itself (both ranks on the one GPU, each
+fitting its own voxels: no kernel of one rank waits on the other's)."""
 import os
 import socket
 
@@ -36,12 +37,26 @@ def _fit(meas, init, cfp, fixp, offset):
     return p, s
 
 
-def _worker(rank, world, port, data, out):
+def _fit_library(meas, init, cfp, fixp, offset):
+    # explicit lane counts: the automatic choice widens groups for small calls
+    cfg = capi.model_cfg("Ball_1_Stick", run_mcmc=1, nburn=50, njumps=100, sampleevery=10,
+                         lanes_levmar=4, lanes_mcmc=2, first_voxel=offset)
+    dev = torch.device("cuda:0")
+    lib = capi.Cudimot("Ball_1_Stick", cfg)
+    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
+    p = t(init)
+    s = torch.zeros(meas.shape[0], 5, 10, dtype=torch.float64, device=dev)
+    lib.fit(t(meas), p, t(cfp), t(fixp), s)
+    torch.cuda.synchronize()
+    return p.cpu().numpy(), s.cpu().numpy()
+
+
+def _worker(rank, world, port, data, out, fit="oracle"):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     meas, init, cfp, fixp = data
     a, b = parts.shard_range(meas.shape[0], world, rank)
-    p, s = _fit(meas[a:b], init[a:b], cfp, fixp[a:b], a)
+    p, s = (_fit if fit == "oracle" else _fit_library)(meas[a:b], init[a:b], cfp, fixp[a:b], a)
     t = torch.tensor([float(rank + 1)])
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     gathered = [None] * world
@@ -52,14 +67,12 @@ def _worker(rank, world, port, data, out):
     dist.destroy_process_group()
 
 
-def test_two_rank_shards_equal_single_process(built):
-    from cudimot_gb300 import synth
-    wl = synth.ball_1_stick(37, seed=5)  # odd size: the last shard takes the remainder
+def _run_ranks(wl, fit):
     data = (wl.meas, wl.init, wl.cfp, wl.fixp)
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_worker, args=(r, 2, port, data, q)) for r in range(2)]
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, data, q, fit)) for r in range(2)]
     for p in procs:
         p.start()
     tmax, gathered = q.get(timeout=300)
@@ -67,10 +80,30 @@ def test_two_rank_shards_equal_single_process(built):
         p.join(timeout=60)
         assert p.exitcode == 0
     assert tmax == 2.0
+    return gathered
+
+
+def test_two_rank_shards_equal_single_process(built):
+    from cudimot_gb300 import synth
+    wl = synth.ball_1_stick(37, seed=5)  # odd size: the last shard takes the remainder
+    gathered = _run_ranks(wl, "oracle")
     assert [(a, b) for a, b, _, _ in gathered] == [(0, 18), (18, 37)]
     p_all = np.concatenate([g[2] for g in gathered])
     s_all = np.concatenate([g[3] for g in gathered])
     p_ref, s_ref = _fit(wl.meas, wl.init, wl.cfp, wl.fixp, 0)
+    assert np.array_equal(p_all, p_ref)
+    assert np.array_equal(s_all, s_ref)
+
+
+@pytest.mark.gpu
+def test_two_rank_shards_through_library(built, cuda):
+    from cudimot_gb300 import synth
+    wl = synth.ball_1_stick(1001, seed=6)
+    gathered = _run_ranks(wl, "library")
+    assert [(a, b) for a, b, _, _ in gathered] == [(0, 500), (500, 1001)]
+    p_all = np.concatenate([g[2] for g in gathered])
+    s_all = np.concatenate([g[3] for g in gathered])
+    p_ref, s_ref = _fit_library(wl.meas, wl.init, wl.cfp, wl.fixp, 0)
     assert np.array_equal(p_all, p_ref)
     assert np.array_equal(s_all, s_ref)
 
