@@ -53,6 +53,10 @@ def parse():
                     default=None,
                     help="run the preceding stages, then one launch of this stage (for ncu); "
                          "mlp_forward: two inference passes of the network on --nvox voxels")
+    ap.add_argument("--lanes", type=int, default=None,
+                    help="with --profile-stage: lanes per voxel (default: those the 200,000-voxel "
+                         "headline runs with, 2 for grid search and MCMC, 4 for LM; the automatic "
+                         "rule would widen the groups of a small case)")
     ap.add_argument("--rician", action="store_true",
                     help="with --profile-stage mcmc: the Rician likelihood (tau sampled)")
     ap.add_argument("--nburn", type=int, default=NBURN)
@@ -277,8 +281,11 @@ def profile_stage(a):
         return
     a.nvox = a.nvox or 20000
     cfp, meas, fixp, init, _ = make_workload(a.nvox, 8219, dev)
+    lanes = a.lanes or {"levmar": 4}.get(a.profile_stage, 2)
+    lk = dict(lanes_gridsearch=2, lanes_levmar=4, lanes_mcmc=2)
+    lk[f"lanes_{a.profile_stage}"] = lanes
     cfg = capi.model_cfg(MODEL, grid=synth.WATSON_GRID, run_mcmc=1, nburn=a.nburn,
-                         njumps=a.njumps, sampleevery=SE, rician=int(a.rician))
+                         njumps=a.njumps, sampleevery=SE, rician=int(a.rician), **lk)
     lib = capi.Cudimot(MODEL, cfg)
     t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
     m, c, f, p = t(meas), t(cfp), t(fixp), t(init)
@@ -301,7 +308,7 @@ def profile_stage(a):
     e1.record()
     torch.cuda.synchronize()
     print(json.dumps({"stage": a.profile_stage, "rician": a.rician, "nvox": a.nvox,
-                      "ms": e0.elapsed_time(e1)}))
+                      "lanes": lanes, "ms": e0.elapsed_time(e1)}))
 
 
 def measured_traffic(kernel, config):
@@ -448,12 +455,34 @@ def bench_heterogeneous(a, dev):
         for v in vols:
             v["lib"].fit(v["meas"], v["params"], v["cfp"], v["fixp"], v["samples"])
 
+    # the persistent multi-model kernel: LM per volume, then every volume's
+    # MCMC tiles in one launch (lane counts of the MCMC limited to the ones
+    # the multi-model library is built with)
+    from cudimot_gb300 import build, hetero
+    hx = hetero.Hetero()
+    for v in vols:
+        lk = autotune.lanes_kwargs(tuned[v["model"]])
+        if lk.get("lanes_mcmc") not in build.HETERO_LANES:
+            lk["lanes_mcmc"] = 2
+        v["hx_lanes"] = lk["lanes_mcmc"]
+        v["hx_lib"] = capi.Cudimot(v["model"], capi.model_cfg(
+            v["model"], run_mcmc=1, nburn=NBURN, njumps=NJUMPS, sampleevery=SE, **lk))
+
+    def run_persistent():
+        for v in vols:
+            v["hx_lib"].levmar(v["meas"], v["params"], v["cfp"], v["fixp"])
+        hx.mcmc([hx.prepare(v["hx_lib"], v["meas"], v["params"], v["cfp"], v["fixp"], v["samples"])
+                 for v in vols])
+
     timed_events(run_batch, a.warmup, reset)
     timed_events(run_seq, 1, reset)
+    timed_events(run_persistent, 1, reset)
     with ClockSampler(dev.index or 0) as clk:
         ms = timed_events(run_batch, a.steps, reset)
     ms_seq = timed_events(run_seq, a.steps, reset)
+    ms_per = timed_events(run_persistent, a.steps, reset)
     ms_b, ms_s = statistics.median(ms), statistics.median(ms_seq)
+    ms_p = statistics.median(ms_per)
     line = base_line("voxels/s fitted (LM+MCMC), heterogeneous batch", total / (ms_b / 1e3),
                      "voxels/s", a, ms_b,
                      {"workload": "heterogeneous_lm_mcmc",
@@ -464,6 +493,11 @@ def bench_heterogeneous(a, dev):
                       "launch": "one CUDA graph, one branch per volume",
                       "lanes_from_autotuner": tuned},
                      clk.summary(), sequential={"value": total / (ms_s / 1e3), "ms_per_step": ms_s},
+                     persistent={"value": total / (ms_p / 1e3), "ms_per_step": ms_p,
+                                 "launch": "LM per volume, then one persistent MCMC launch over "
+                                           "every volume's tiles (libcdm_hetero)",
+                                 "grid": hx.last_grid,
+                                 "mcmc_lanes": {v["model"]: v["hx_lanes"] for v in vols}},
                      gpu_launches=sum(9 for _ in vols) * a.steps)
     print(json.dumps(line))
 

@@ -378,6 +378,129 @@ def build_utils(force=False):
     return out, None
 
 
+# The models of the multi-model library built by default: the mix of the
+# heterogeneous workload (tensor, ball & two sticks, NODDI-Watson).
+HETERO_MODELS = ("DiffusionTensor", "Ball_2_Sticks", "NODDI_Watson")
+HETERO_LANES = (1, 2, 4)
+
+
+def hetero_lib_path(tag="default"):
+    return os.path.join(LIBDIR, f"libcdm_hetero_{tag}.so")
+
+
+def build_hetero(models=HETERO_MODELS, lanes=HETERO_LANES, tag="default", model_dirs=None,
+                 eval_types=None, force=False, verbose=False, jobs=None):
+    """libcdm_hetero_<tag>.so: one persistent MCMC kernel over several models
+    (cdm_hetero.h). Each model's part (cdm_hetero_part.cu) is compiled with
+    relocatable device code in a translation unit of its own, against that
+    model's plugin; the parts and the persistent kernel are device-linked
+    into one cubin, which the host half embeds."""
+    model_dirs = list(model_dirs or [os.path.join(MODELS, m) for m in models])
+    eval_types = list(eval_types or [None] * len(model_dirs))
+    names = [os.path.basename(d.rstrip("/")) for d in model_dirs]
+    out = hetero_lib_path(tag)
+    hdir = os.path.join(GENDIR, f"hetero_{tag}")
+    os.makedirs(hdir, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    hsrc = os.path.join(CSRC, "hetero")
+    h = hashlib.sha256()
+    for f in sources() + sorted(os.path.join(hsrc, x) for x in os.listdir(hsrc)) + \
+            [os.path.join(ROOT, "include", "cdm_hetero.h")]:
+        h.update(open(f, "rb").read())
+    for d, e in zip(model_dirs, eval_types):
+        h.update(f"{d}|{e}".encode())
+        for x in sorted(os.listdir(d)):
+            if x.endswith((".h", ".cc", ".cu", ".hpp")):
+                h.update(open(os.path.join(d, x), "rb").read())
+    h.update(repr(tuple(lanes)).encode())
+    dig = h.hexdigest()
+    stamp = out + ".sha256"
+    if not force and os.path.exists(out) and os.path.exists(stamp) and open(stamp).read() == dig:
+        return out, None
+    lane_list = " ".join(f"X({g})" for g in lanes)
+    with open(os.path.join(hdir, "cdm_hx_dispatch.h"), "w") as f:
+        f.write("// generated by cudimot_gb300/build.py: entries of the linked models\n#pragma once\n")
+        entries = []
+        for i in range(len(names)):
+            for g in lanes:
+                for r in (0, 1):
+                    nm = f"cdm_hx_{i}_mcmc_{g}_{r}"
+                    f.write(f'extern "C" __device__ void {nm}(int, unsigned char*, const void*);\n')
+                    entries.append(nm)
+        f.write("__device__ __forceinline__ void cdm_hx_dispatch(int fn, int tile, unsigned char* "
+                "scratch, const void* args) {\n  switch (fn) {\n")
+        for k, nm in enumerate(entries):
+            f.write(f"    case {k}: {nm}(tile, scratch, args); break;\n")
+        f.write("    default: break;\n  }\n}\n")
+    with open(os.path.join(hdir, "cdm_hx_set.h"), "w") as f:
+        f.write("// generated by cudimot_gb300/build.py: the linked models\n#pragma once\n")
+        f.write(f"constexpr int kHxNumModels = {len(names)};\n")
+        f.write("static const char* const kHxModels[] = {" + ", ".join(f'"{n}"' for n in names) + "};\n")
+        f.write("static const int kHxEvalDouble[] = {" +
+                ", ".join("1" if e == "double" else "0" for e in eval_types) + "};\n")
+        f.write(f"constexpr int kHxNumLanes = {len(lanes)};\n")
+        f.write("static const int kHxLanes[] = {" + ", ".join(str(g) for g in lanes) + "};\n")
+        f.write("constexpr int kHxThreads = 128;\n")
+    # link-time optimisation: the parts reach the device link as IR, so the
+    # entries are inlined into the persistent kernel and registers are
+    # allocated for the whole kernel (a call through the ABI spills)
+    lto = "-gencode=arch=compute_103a,code=lto_103a"
+    base = [nvcc_path(), "-O3", "-std=c++17", lto, "-lineinfo", "-rdc=true",
+            "-Xcompiler", "-ffp-contract=off"]
+    if verbose:
+        base += ["-Xptxas", "-v"]
+
+    def part(i):
+        d, e, n = model_dirs[i], eval_types[i], names[i]
+        gen = os.path.join(hdir, f"gen_{i}")
+        os.makedirs(gen, exist_ok=True)
+        _write_sizes(gen, block_sizes(d))
+        macro = f"-DCDM_HX_LANES(X)={lane_list}"
+        o = os.path.join(hdir, f"part_{i}.o")
+        cmd = base + eval_flags(e) + [f"-DCDM_HX_ID={i}", macro] + _includes(gen, d) + \
+            ["-c", os.path.join(hsrc, "cdm_hetero_part.cu"), "-o", o]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose:
+            sys.stderr.write(r.stdout + r.stderr)
+        return o, None if r.returncode == 0 else f"{n}: " + (r.stdout + r.stderr)[-6000:]
+
+    kobj = os.path.join(hdir, "kernel.o")
+    kcmd = base + ["-I", hdir, "-I", hsrc, "-c", os.path.join(hsrc, "cdm_hetero_kernel.cu"), "-o", kobj]
+    with cf.ThreadPoolExecutor(jobs or min(len(names) + 1, os.cpu_count() or 1)) as ex:
+        parts = list(ex.map(part, range(len(names))))
+        kr = subprocess.run(kcmd, capture_output=True, text=True)
+    for _, err in parts:
+        if err:
+            return out, err
+    if kr.returncode != 0:
+        return out, (kr.stdout + kr.stderr)[-6000:]
+    cubin = os.path.join(hdir, "cdm_hetero.cubin")
+    lcmd = [nvcc_path(), "-arch=sm_103a", "-dlto", "-dlink", "--cubin"] + [o for o, _ in parts] + \
+        [kobj, "-o", cubin]
+    if verbose:
+        lcmd[1:1] = ["-Xnvlink", "-v"]
+    r = subprocess.run(lcmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return out, (r.stdout + r.stderr)[-6000:]
+    if verbose:
+        sys.stderr.write(r.stdout + r.stderr)
+    image = os.path.join(hdir, "cdm_hetero_image.cpp")
+    with open(image, "w") as f:
+        f.write("// generated by cudimot_gb300/build.py: the multi-model module, embedded\n")
+        f.write('__asm__(".section .rodata\\n.balign 64\\n.globl cdm_hetero_image\\n'
+                'cdm_hetero_image:\\n.incbin \\"' + cubin + '\\"\\n.byte 0\\n.previous\\n");\n')
+    cmd = [nvcc_path(), "-O3", "-std=c++17", ARCH, "-Xcompiler", "-fPIC", "-shared",
+           "-I", hdir, "-I", hsrc, "-I", os.path.join(ROOT, "include"),
+           os.path.join(hsrc, "cdm_hetero_host.cu"), image, "-o", out + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return out, (r.stdout + r.stderr)[-6000:]
+    os.replace(out + ".tmp", out)
+    with open(stamp, "w") as f:
+        f.write(dig)
+    return out, None
+
+
 def build_all(models=None, model_dirs=(), jobs=None, verbose=False, force=False):
     todo = [(os.path.join(MODELS, m), m) for m in (models or shipped_models())]
     todo += [(d, None) for d in model_dirs]
@@ -389,6 +512,7 @@ def build_all(models=None, model_dirs=(), jobs=None, verbose=False, force=False)
         futs[ex.submit(build_batch, force)] = ("batch", None)
         futs[ex.submit(build_mlp, force)] = ("mlp", None)
         futs[ex.submit(build_utils, force)] = ("utils", None)
+        futs[ex.submit(build_hetero, force=force)] = ("hetero", None)
         for f in cf.as_completed(futs):
             out, err = f.result()
             if err:

@@ -226,6 +226,7 @@ def _declare(lib):
         "cdm_selftest_wait_timeout": [_vp, i, _vp],
         "cdm_fit_reserve": [_vp, i, i],
         "cdm_mcmc_seeded": [_vp, i, i, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+        "cdm_mcmc_prepare": [_vp, i, i, i, i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "cdm_synth_signals": [_vp, i, i, _vp, _vp, _vp, C.c_double, C.c_double, C.c_uint64, i,
                               _vp, _vp, _vp, i, _vp],
         "cdm_mlp_head_info": [C.POINTER(i), C.POINTER(i), _vp],

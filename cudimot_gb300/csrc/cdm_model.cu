@@ -26,6 +26,7 @@
 
 #include "cdm_host.h"
 #include "cudimot_gb300.h"
+#include "cdm_hetero.h"
 
 #include "cdm_kernels.h"
 #include "cdm_noalloc_scratch.h"
@@ -213,10 +214,31 @@ cdm_status launch(int fam, int lanes, dim3 grid, dim3 block, size_t smem, cudaSt
   return launch_argv(fam, lanes, grid, block, smem, st, argv);
 }
 
+// The dynamic shared memory a launch may use without opting in is 48 KB
+// less the kernel's static shared memory (the MCMC kernel's sample staging
+// is 4-37 KB, by lane count and parameter count), so the opt-in depends on
+// both; the static size is read once per kernel.
 cdm_status set_smem(int fam, int lanes, size_t bytes) {
-  if (bytes <= 48 * 1024) return CDM_OK;
+  if (bytes == 0) return CDM_OK;
   const void* fn = kfn(fam, lanes);
   if (!fn) return cdm_fail(CDM_CUDA_ERROR, std::string("kernel ") + cdm_kfam_name(fam) + " is not available");
+  static std::mutex mu;
+  static long static_bytes[CDM_K_COUNT][6];
+  static bool known[CDM_K_COUNT][6];
+  const int li = fam < CDM_K_NLANE_FAMILIES ? cdm_lane_index(lanes) : 0;
+  if (fam < 0 || fam >= CDM_K_COUNT || li < 0) return cdm_fail(CDM_BAD_ARG, "kernel family or lanes");
+  long st = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!known[fam][li]) {
+      cudaFuncAttributes fa;
+      CDM_CUDA(cudaFuncGetAttributes(&fa, fn));
+      static_bytes[fam][li] = (long)fa.sharedSizeBytes;
+      known[fam][li] = true;
+    }
+    st = static_bytes[fam][li];
+  }
+  if ((long)bytes + st <= 48 * 1024) return CDM_OK;
   CDM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   return CDM_OK;
 }
@@ -351,6 +373,8 @@ struct cdm_ctx {
   std::vector<uintptr_t> graph_key;
   // current protocol / packed signal state
   int nmeas_pad = 0;
+  // cdm_mcmc_prepare: the MCMC launch is described here instead of made
+  cdm_tile_work* export_to = nullptr;
 };
 
 namespace {
@@ -609,6 +633,22 @@ cdm_status launch_mcmc(cdm_ctx* c, int Gw, bool rician, int nvox, int nmeas, dou
       return cdm_fail(CDM_BAD_ARG, "protocol too large for the custom priors' copy of it");
   }
   CDM_TRY(set_smem(fam, Gw, sm));
+  if (c->export_to) {
+    static_assert(sizeof(cdm_mcmc_args) <= CDM_TILE_ARGS_MAX, "MCMC argument block");
+    cdm_tile_work* w = c->export_to;
+    std::snprintf(w->model, sizeof(w->model), "%s", CDM_MODEL_NAME);
+    w->eval_double = kRealBytes == 8 ? 1 : 0;
+    w->threads = CDM_NT;
+    w->lanes = Gw;
+    w->rician = rician ? 1 : 0;
+    w->ntiles = blocks_for(nvox, Gw);
+    w->smem_bytes = (uint32_t)sm;
+    w->scratch_bytes = (uint32_t)((CDM_NT / Gw) * (kNP + 1) * 4 * sizeof(double));
+    w->args_bytes = (uint32_t)sizeof(cdm_mcmc_args);
+    w->err = c->err;
+    std::memcpy(w->args, &a, sizeof(cdm_mcmc_args));
+    return CDM_OK;
+  }
   return launch(fam, Gw, blocks_for(nvox, Gw), CDM_NT, sm, st, a);
 }
 
@@ -856,6 +896,26 @@ cdm_status cdm_mcmc(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_size
   CDM_TRY(check_common(c, nvox, nmeas, CFP_size, FixP_size));
   return run_mcmc(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau_samples, first_voxel(c),
                   (cudaStream_t)stream);
+}
+
+cdm_status cdm_mcmc_prepare(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_size,
+                            const double* meas, double* params, const double* CFP,
+                            const double* FixP, double* samples, double* tau_samples,
+                            void* stream, cdm_tile_work* out) {
+  if (!out) return cdm_fail(CDM_BAD_ARG, "null cdm_tile_work");
+  std::memset(out, 0, sizeof(*out));
+  CDM_TRY(check_common(c, nvox, nmeas, CFP_size, FixP_size));
+  c->export_to = out;
+  const cdm_status s = run_mcmc(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau_samples,
+                                first_voxel(c), (cudaStream_t)stream);
+  c->export_to = nullptr;
+  if (s == CDM_OK && nvox == 0) {  // run_mcmc returns before the launch
+    std::snprintf(out->model, sizeof(out->model), "%s", CDM_MODEL_NAME);
+    out->eval_double = kRealBytes == 8 ? 1 : 0;
+    out->threads = CDM_NT;
+    out->err = c->err;
+  }
+  return s;
 }
 
 cdm_status cdm_mcmc_seeded(cdm_ctx* c, int nvox, int nmeas, int CFP_size, int FixP_size,

@@ -54,14 +54,27 @@ typedef fp32 cdm_real;
 // device functions taking their argument block by reference; the module
 // defines extern "C" kernels with fixed names that call them, so that a
 // host library compiled without the plugin can look them up by name.
-#ifdef CDM_DEVICE_MODULE
+//
+// A part of the persistent multi-model kernel (CDM_HETERO) also makes them
+// device functions, with two more leading arguments: the tile the CTA
+// works on in place of blockIdx.x, and shared-memory scratch for what the
+// kernel would otherwise keep in static shared memory (the static shared
+// memory of every model linked into the one kernel would add up).
+#if defined(CDM_HETERO)
+#define CDM_KERNEL(...) __device__ __forceinline__ void
+#define CDM_KERNEL0 __device__ __forceinline__ void
+#define CDM_KARG(T) int cdm_tile, unsigned char* cdm_scratch, const T&
+#define CDM_BLOCK_IDX cdm_tile
+#elif defined(CDM_DEVICE_MODULE)
 #define CDM_KERNEL(...) __device__ __forceinline__ void
 #define CDM_KERNEL0 __device__ __forceinline__ void
 #define CDM_KARG(T) const T&
+#define CDM_BLOCK_IDX blockIdx.x
 #else
 #define CDM_KERNEL(...) __global__ void __launch_bounds__(__VA_ARGS__)
 #define CDM_KERNEL0 __global__ void
 #define CDM_KARG(T) const __grid_constant__ T
+#define CDM_BLOCK_IDX blockIdx.x
 #endif
 
 static_assert(CUSTOM == kCustomPrior, "prior type CUSTOM");
@@ -124,6 +137,11 @@ __device__ __forceinline__ bool cdm_stage_protocol(const float* __restrict__ gsr
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+#ifdef CDM_HETERO
+  // the previous tile wrote this shared memory with ordinary stores; order
+  // them before the bulk copy (async proxy) that overwrites it
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+#endif
   __syncthreads();
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sbar), "r"(bytes)
@@ -135,8 +153,16 @@ __device__ __forceinline__ bool cdm_stage_protocol(const float* __restrict__ gsr
         : "memory");
   }
   const bool done = cdm_mbar_wait_phase0(sbar, 2000000000ull, err);
+#ifdef CDM_HETERO
+  // the whole CTA leaves together (the persistent kernel's barriers follow),
+  // and the next tile initialises the barrier again
+  const bool all = __syncthreads_and(done) != 0;
+  if (threadIdx.x == 0 && all) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(sbar) : "memory");
+  return all;
+#else
   __syncthreads();
   return done;
+#endif
 }
 
 // Load one measurement's protocol values (raw CFP then derived) from the

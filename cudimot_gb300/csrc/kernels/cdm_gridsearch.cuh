@@ -41,7 +41,7 @@ CDM_KERNEL(CDM_NT) cdm_gridsearch_kernel(CDM_KARG(cdm_gs_args) a) {
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
   const int* shdr;
   const float* ptab = cdm_prepare_tables<Gw>(sproto, a.nmeas_pad, a.nchunk, a.shells_staged != 0, &shdr);
-  const int v = blockIdx.x * (CDM_NT / Gw) + (int)threadIdx.x / Gw;
+  const int v = (int)CDM_BLOCK_IDX * (CDM_NT / Gw) + (int)threadIdx.x / Gw;
   if (v >= a.nvox) return;
   const unsigned gm = cdm_group_mask<Gw>();
   const int lane = (int)threadIdx.x % Gw;

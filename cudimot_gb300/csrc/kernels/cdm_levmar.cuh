@@ -162,7 +162,7 @@ CDM_KERNEL(CDM_NT) cdm_levmar_kernel(CDM_KARG(cdm_lm_args) a) {
   extern __shared__ __align__(16) float sproto[];
   if (!cdm_stage_protocol(a.proto, sproto, a.proto_bytes, a.err)) return;
   const float* ptab = cdm_build_pair_table<Gw>(sproto, a.nmeas_pad, a.nchunk);
-  const int v = blockIdx.x * (CDM_NT / Gw) + (int)threadIdx.x / Gw;
+  const int v = (int)CDM_BLOCK_IDX * (CDM_NT / Gw) + (int)threadIdx.x / Gw;
   if (v >= a.nvox) return;
   const unsigned gm = cdm_group_mask<Gw>();
   const int lane = (int)threadIdx.x % Gw;

@@ -134,9 +134,13 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
     __syncthreads();
   }
   // recorded samples wait here until their 32-byte DRAM sector is complete
+#ifdef CDM_HETERO
+  double(*sbuf)[kNP + 1][4] = reinterpret_cast<double(*)[kNP + 1][4]>(cdm_scratch);
+#else
   __shared__ double sbuf[CDM_NT / Gw][kNP + 1][4];
+#endif
   const int vloc = (int)threadIdx.x / Gw;
-  const int v = blockIdx.x * (CDM_NT / Gw) + vloc;
+  const int v = (int)CDM_BLOCK_IDX * (CDM_NT / Gw) + vloc;
   if (v >= a.nvox) return;
   const unsigned gm = cdm_group_mask<Gw>();
   const int lane = (int)threadIdx.x % Gw;

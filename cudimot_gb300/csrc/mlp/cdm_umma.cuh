@@ -418,20 +418,27 @@ __global__ void __launch_bounds__(kThreads, 1)
 // kErrTimeout and still releases its tensor memory.
 namespace pers {
 constexpr int kBN = 256;
-constexpr int kStages = 4;
-constexpr int kEpiWarps = 8;
+constexpr int kStages = 3;
+// 16 epilogue warps: four per SM sub-partition, so that one warp's TMEM
+// load, shared-memory round trip and stores overlap three others' GELU
+constexpr int kEpiWarps = 16;
 constexpr int kThreads = 32 * (2 + kEpiWarps);
+constexpr int kColsPerWarp = kBN / (kEpiWarps / 4);  // 64: each TMEM lane quarter has 4 warps
 constexpr int kABytes = kBM * kBK * 2;            // 16 KB
 constexpr int kBBytes = kBN * kBK * 2;            // 32 KB
 constexpr int kStageBytes = kABytes + kBBytes;    // 48 KB
-constexpr int kOutLd = 40;                        // bf16 per staged row (32 + 8: 80 B)
-constexpr int kOutBytes = 32 * kOutLd * 2;        // per epilogue warp
+// per epilogue warp: 32 rows x 32 bf16 (64 B per row, no padding); the
+// 16-byte piece j of row r sits at slot j ^ ((r >> 1) & 3), so that both the
+// row-per-lane writes and the four-pieces-per-row reads of a quarter warp
+// touch eight different 16-byte bank groups
+constexpr int kOutBytes = 32 * 64;
 constexpr int kOffOut = kStages * kStageBytes;
 constexpr int kOffBias = kOffOut + kEpiWarps * kOutBytes;
 constexpr int kOffBar = kOffBias + kBN * 4;
 constexpr int kBytes = kOffBar + (2 * kStages + 4) * 8 + 16;
 constexpr int kAlloc = kBytes + 1024;  // slack for the 1024-byte alignment of the stages
-static_assert(kAlloc <= 227 * 1024, "shared memory of the persistent GEMM");
+// (the kernel's static shared memory, up to 1 KB with its alignment, comes on top)
+static_assert(kAlloc + 1024 <= 227 * 1024, "shared memory of the persistent GEMM");
 }  // namespace pers
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
@@ -542,8 +549,8 @@ __global__ void __launch_bounds__(pers::kThreads, 1)
     }
   } else {
     const int q = warp % 4;             // TMEM lane quarter this warp may read
-    const int h = (warp - 2) / 4;       // column half of the accumulator
-    __nv_bfloat16* stage = reinterpret_cast<__nv_bfloat16*>(smem + kOffOut + (warp - 2) * kOutBytes);
+    const int h = (warp - 2) / 4;       // column quarter of the accumulator
+    unsigned char* stage = smem + kOffOut + (warp - 2) * kOutBytes;
     int j = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, j++) {
       const int b = j & 1;
@@ -555,29 +562,36 @@ __global__ void __launch_bounds__(pers::kThreads, 1)
       const int r0 = t * kBM + 32 * q;  // first global row of this warp
       const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * kBN);
 #pragma unroll 1
-      for (int c = 0; c < 4; c++) {
-        const int c0 = h * 128 + 32 * c;
+      for (int c = 0; c < kColsPerWarp / 32; c++) {
+        const int c0 = h * kColsPerWarp + 32 * c;
         float v[32];
         tmem_ld32(base + (uint32_t)c0, v);
         uint32_t o[16];  // bf16 pairs
+        const float4* b4 = reinterpret_cast<const float4*>(sbias + c0);  // broadcast loads
 #pragma unroll
-        for (int i = 0; i < 16; i++) {
-          const float z0 = __bfloat162float(__float2bfloat16(v[2 * i] + sbias[c0 + 2 * i]));
-          const float z1 = __bfloat162float(__float2bfloat16(v[2 * i + 1] + sbias[c0 + 2 * i + 1]));
-          const __nv_bfloat162 g2 = __floats2bfloat162_rn(gelu(z0), gelu(z1));
-          o[i] = *reinterpret_cast<const uint32_t*>(&g2);
+        for (int i = 0; i < 8; i++) {
+          const float4 b = b4[i];
+          const float z0 = __bfloat162float(__float2bfloat16(v[4 * i] + b.x));
+          const float z1 = __bfloat162float(__float2bfloat16(v[4 * i + 1] + b.y));
+          const float z2 = __bfloat162float(__float2bfloat16(v[4 * i + 2] + b.z));
+          const float z3 = __bfloat162float(__float2bfloat16(v[4 * i + 3] + b.w));
+          const __nv_bfloat162 g01 = __floats2bfloat162_rn(gelu(z0), gelu(z1));
+          const __nv_bfloat162 g23 = __floats2bfloat162_rn(gelu(z2), gelu(z3));
+          o[2 * i] = *reinterpret_cast<const uint32_t*>(&g01);
+          o[2 * i + 1] = *reinterpret_cast<const uint32_t*>(&g23);
         }
+        const int sw = (lane >> 1) & 3;
 #pragma unroll
         for (int p = 0; p < 4; p++)
-          *reinterpret_cast<uint4*>(stage + lane * kOutLd + 8 * p) =
+          *reinterpret_cast<uint4*>(stage + lane * 64 + ((p ^ sw) << 4)) =
               make_uint4(o[4 * p], o[4 * p + 1], o[4 * p + 2], o[4 * p + 3]);
         __syncwarp();
 #pragma unroll
         for (int p = lane; p < 128; p += 32) {
-          const int r = p >> 2, col = c0 + 8 * (p & 3);
+          const int r = p >> 2, j = p & 3, col = c0 + 8 * j;
           if (r0 + r < a.M && col < ncols)
             *reinterpret_cast<uint4*>(a.out_bf16 + (size_t)(r0 + r) * a.ld_out + col) =
-                *reinterpret_cast<const uint4*>(stage + r * kOutLd + 8 * (p & 3));
+                *reinterpret_cast<const uint4*>(stage + r * 64 + ((j ^ ((r >> 1) & 3)) << 4));
         }
         __syncwarp();
       }

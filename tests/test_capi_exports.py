@@ -60,3 +60,28 @@ def test_status_strings(built):
     lib = capi.load_library("Ball_1_Stick")
     assert [lib.cdm_status_string(i).decode() for i in range(6)] == \
         ["OK", "BAD_ARG", "CUDA_ERROR", "TIMEOUT", "NOT_SUPPORTED", "IO_ERROR"]
+
+
+def test_hetero_exports(built):
+    """cdm_hetero.h: cdm_mcmc_prepare in every model library, the rest in
+    the multi-model library (which loads without a GPU)."""
+    from cudimot_gb300 import build, hetero
+    text = open(os.path.join(os.path.dirname(HEADER), "cdm_hetero.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = sorted(set(re.findall(r"\b(cdm_[a-z_0-9]+)\s*\(", text)))
+    assert "cdm_mcmc_prepare" in names
+    for model in MODELS:
+        assert hasattr(C.CDLL(capi.lib_path(model)), "cdm_mcmc_prepare"), model
+    lib = hetero.load()
+    for n in names:
+        if n != "cdm_mcmc_prepare":
+            assert hasattr(lib, n), n
+    assert set(hetero.EXPORTED) == set(names) - {"cdm_mcmc_prepare"}
+    # the linked set, without a device
+    s = lib.cdm_hetero_models(None, 0)
+    buf = C.create_string_buffer(s + 1)
+    lib.cdm_hetero_models(buf, s + 1)
+    models = buf.value.decode().split(",")
+    assert [m.split("/")[0] for m in models] == list(build.HETERO_MODELS)
+    assert all(m.endswith("/f32/1:2:4") for m in models)
+    assert hetero.TileWork.args.offset == 104 and C.sizeof(hetero.TileWork) == 1128

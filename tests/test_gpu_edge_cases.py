@@ -194,3 +194,28 @@ def test_largest_protocol(built, cuda):
         with pytest.raises(capi.CdmError, match="BAD_ARG"):
             call()
     lib.synchronize(timeout_ms=10000)
+
+
+@pytest.mark.parametrize("model", ["Ball_1_Stick", "DiffusionTensor", "Ball_2_Sticks",
+                                   "NODDI_Watson", "NODDI_Bingham"])
+def test_mcmc_every_lane_count(built, cuda, model):
+    """MCMC runs at every lane count, Gaussian and Rician: the kernel's
+    static shared memory (sample staging, up to 37 KB at one lane for the
+    8-parameter model) plus the staged protocol may pass 48 KB, which needs
+    the opt-in even when the protocol alone does not."""
+    from tests import helpers
+    wl = {"Ball_1_Stick": helpers.b1s, "DiffusionTensor": helpers.dt, "Ball_2_Sticks": helpers.b2s,
+          "NODDI_Watson": helpers.watson, "NODDI_Bingham": helpers.bingham}[model](70, seed=44)
+    npar = wl.init.shape[1]
+    for rician in (0, 1):
+        for lanes in (1, 2, 4, 8, 16, 32):
+            cfg = capi.model_cfg(model, run_mcmc=1, nburn=10, njumps=20, sampleevery=10,
+                                 lanes_mcmc=lanes, rician=rician)
+            lib = capi.Cudimot(model, cfg)
+            s = torch.zeros(70, npar, 2, dtype=torch.float64, device=cuda)
+            tau = torch.zeros(70, 2, dtype=torch.float64, device=cuda) if rician else None
+            lib.mcmc(T(wl.meas, cuda), T(wl.init, cuda), T(wl.cfp, cuda), T(wl.fixp, cuda), s,
+                     tau=tau)
+            lib.synchronize(timeout_ms=60000)
+            got = s.cpu().numpy()
+            assert np.all(np.isfinite(got)) and np.any(got != 0.0), (model, lanes, rician)

@@ -87,7 +87,9 @@ def test_watson_pipeline_steps(built, cuda):
     after_ff = pl.params.cpu().numpy().copy()
     np.testing.assert_array_equal(after_ff[:, 2:5], after_gs[:, 2:5])
     ref_ff = o.levmar(lib.cfg, wl.meas, after_gs, wl.cfp, f)[0]
-    np.testing.assert_array_equal(ref_ff[:, 2:5], after_gs[:, 2:5])
+    # the oracle, like CUDIMOT, carries fixed parameters through the bounds
+    # transform and back (a few ulp); the library leaves them untouched
+    np.testing.assert_allclose(ref_ff[:, 2:5], after_gs[:, 2:5], rtol=1e-13, atol=1e-13)
     assert_lm_voxelwise(o.cost(wl.meas, after_ff, wl.cfp, f), o.cost(wl.meas, ref_ff, wl.cfp, f),
                         max_frac=0.0075, max_excess=0.01)
     st, lib, samples = pl.ctx[2]
