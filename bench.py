@@ -280,13 +280,19 @@ def profile_stage(a):
         profile_mlp_forward(a, dev)
         return
     a.nvox = a.nvox or 20000
-    cfp, meas, fixp, init, _ = make_workload(a.nvox, 8219, dev)
+    model, grid = MODEL, synth.WATSON_GRID
+    if a.workload == "noddi_bingham":  # the Bingham workload and grid
+        model, grid = "NODDI_Bingham", synth.BINGHAM_GRID
+        wl = bingham_workload(a.nvox, dev)
+        cfp, meas, fixp, init = wl.cfp, wl.meas, wl.fixp, wl.init
+    else:
+        cfp, meas, fixp, init, _ = make_workload(a.nvox, 8219, dev)
     lanes = a.lanes or {"levmar": 4}.get(a.profile_stage, 2)
     lk = dict(lanes_gridsearch=2, lanes_levmar=4, lanes_mcmc=2)
     lk[f"lanes_{a.profile_stage}"] = lanes
-    cfg = capi.model_cfg(MODEL, grid=synth.WATSON_GRID, run_mcmc=1, nburn=a.nburn,
+    cfg = capi.model_cfg(model, grid=grid, run_mcmc=1, nburn=a.nburn,
                          njumps=a.njumps, sampleevery=SE, rician=int(a.rician), **lk)
-    lib = capi.Cudimot(MODEL, cfg)
+    lib = capi.Cudimot(model, cfg)
     t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
     m, c, f, p = t(meas), t(cfp), t(fixp), t(init)
     if a.profile_stage in ("levmar", "mcmc"):
@@ -302,12 +308,12 @@ def profile_stage(a):
         lib.levmar(m, p, c, f)
     else:
         ns = max(a.njumps // SE, 1)
-        s = torch.zeros(a.nvox, 5, ns, dtype=torch.float64, device=dev)
+        s = torch.zeros(a.nvox, init.shape[1], ns, dtype=torch.float64, device=dev)
         tau = torch.zeros(a.nvox, ns, dtype=torch.float64, device=dev) if a.rician else None
         lib.mcmc(m, p, c, f, s, tau=tau)
     e1.record()
     torch.cuda.synchronize()
-    print(json.dumps({"stage": a.profile_stage, "rician": a.rician, "nvox": a.nvox,
+    print(json.dumps({"stage": a.profile_stage, "model": model, "rician": a.rician, "nvox": a.nvox,
                       "lanes": lanes, "ms": e0.elapsed_time(e1)}))
 
 
@@ -397,11 +403,25 @@ def bench_b1s_lm(a, dev):
         t0 = time.perf_counter()
         lib.fit_host(hm, hp, hc, hf, hs)
         e2e.append(time.perf_counter() - t0)
+    # roofline of the step: the LM kernel's work (passes from the device
+    # counter) over the step's time, against the FP32 peak
+    from cudimot_gb300 import flops
+    ops = flops.count_ops("Ball_1_Stick", wl.truth, wl.cfp, wl.fixp)
+    fl_pass = flops.levmar_pass_flops(ops, 134, 5)
+    pk = fp32_peak_tflops(dev)
+    achieved = fl_pass * st.lm_iterations / (ms_step / 1e3) / 1e12
+    roof = {"bound": "latency", "kernel": "cdm_levmar_kernel", "achieved": achieved,
+            "unit": "TFLOP/s", "peak": pk["tflops"] if pk else None,
+            "frac": achieved / pk["tflops"] if pk else None,
+            "peak_source": pk["source"] if pk else None, "flop_per_pass": fl_pass,
+            "note": "10,000 voxels x 4 lanes are 40,000 threads, half of the 77,824 the GPU "
+                    "holds at once: one partial wave of ~7 dependent LM passes, so the fit "
+                    "is bound by pass latency, not by a pipe"}
     line = base_line("voxels/s fitted (plain LM)", n / (ms_step / 1e3), "voxels/s", a, ms_step,
                      {"workload": "ball_1_stick_lm", "model": "Ball_1_Stick", "nvox": n, "nmeas": 134,
                       "iter_levmar": 200, "l2": "256 MB written before each step (inputs fit in L2)"},
                      clk.summary(), lm_iterations_per_voxel=st.lm_iterations / n,
-                     gpu_launches=3 * max(a.steps, 10),
+                     roofline=roof, gpu_launches=3 * max(a.steps, 10),
                      e2e={"value": n / statistics.median(e2e), "unit": "voxels/s",
                           "h2d_bytes_per_step": int(hm.nbytes + hc.nbytes + wl.init.nbytes),
                           "d2h_bytes_per_step": int(wl.init.nbytes + hs.nbytes)})
@@ -456,14 +476,15 @@ def bench_heterogeneous(a, dev):
             v["lib"].fit(v["meas"], v["params"], v["cfp"], v["fixp"], v["samples"])
 
     # the persistent multi-model kernel: LM per volume, then every volume's
-    # MCMC tiles in one launch (lane counts of the MCMC limited to the ones
-    # the multi-model library is built with)
-    from cudimot_gb300 import build, hetero
+    # MCMC tiles in one launch. MCMC at 2 lanes for every model: one CTA
+    # holds the largest fit's tables and the largest sample staging of all
+    # of them, and at 1 lane (128 voxels per CTA) the staging alone is 32 KB
+    # for the tensor model, which leaves room for 3 CTAs per SM instead of 4
+    from cudimot_gb300 import hetero
     hx = hetero.Hetero()
     for v in vols:
         lk = autotune.lanes_kwargs(tuned[v["model"]])
-        if lk.get("lanes_mcmc") not in build.HETERO_LANES:
-            lk["lanes_mcmc"] = 2
+        lk["lanes_mcmc"] = 2
         v["hx_lanes"] = lk["lanes_mcmc"]
         v["hx_lib"] = capi.Cudimot(v["model"], capi.model_cfg(
             v["model"], run_mcmc=1, nburn=NBURN, njumps=NJUMPS, sampleevery=SE, **lk))
@@ -496,7 +517,7 @@ def bench_heterogeneous(a, dev):
                      persistent={"value": total / (ms_p / 1e3), "ms_per_step": ms_p,
                                  "launch": "LM per volume, then one persistent MCMC launch over "
                                            "every volume's tiles (libcdm_hetero)",
-                                 "grid": hx.last_grid,
+                                 "grid": hx.last_grid, "launches": hx.last_launches,
                                  "mcmc_lanes": {v["model"]: v["hx_lanes"] for v in vols}},
                      gpu_launches=sum(9 for _ in vols) * a.steps)
     print(json.dumps(line))
@@ -748,6 +769,25 @@ def bench_rician(a, dev):
     print(json.dumps(line))
 
 
+def bingham_workload(n, dev):
+    """The NODDI-Bingham workload; clean signals from the library's plugin."""
+    import torch
+    from cudimot_gb300 import capi, synth
+    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
+    lib0 = capi.Cudimot("NODDI_Bingham", capi.model_cfg("NODDI_Bingham"))
+
+    def signal(truth, cfp, S0):
+        out = np.empty((truth.shape[0], cfp.shape[0]))
+        for r0 in range(0, truth.shape[0], 1 << 18):
+            tr = truth[r0:r0 + (1 << 18)]
+            clean = torch.zeros(tr.shape[0], cfp.shape[0], dtype=torch.float64, device=dev)
+            lib0.predicted_signal(t(tr[:, :, None]), t(cfp), t(S0[r0:r0 + tr.shape[0], None]), clean)
+            out[r0:r0 + tr.shape[0]] = clean.cpu().numpy()
+        return out
+
+    return synth.noddi_bingham(n, signal_fn=signal)
+
+
 def bench_bingham(a, dev):
     """NODDI-Bingham precision study: --nvox voxels (default 1,000,000) of
     the NODDI-Watson protocol and parameters plus beta = U(0,0.9) kappa and
@@ -761,18 +801,7 @@ def bench_bingham(a, dev):
     model = "NODDI_Bingham"
     n = a.nvox or 1_000_000
     t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
-    lib0 = capi.Cudimot(model, capi.model_cfg(model))
-
-    def signal(truth, cfp, S0):
-        out = np.empty((truth.shape[0], cfp.shape[0]))
-        for r0 in range(0, truth.shape[0], 1 << 18):
-            tr = truth[r0:r0 + (1 << 18)]
-            clean = torch.zeros(tr.shape[0], cfp.shape[0], dtype=torch.float64, device=dev)
-            lib0.predicted_signal(t(tr[:, :, None]), t(cfp), t(S0[r0:r0 + tr.shape[0], None]), clean)
-            out[r0:r0 + tr.shape[0]] = clean.cpu().numpy()
-        return out
-
-    wl = synth.noddi_bingham(n, signal_fn=signal)
+    wl = bingham_workload(n, dev)
     cfg = capi.model_cfg(model, grid=synth.BINGHAM_GRID, run_mcmc=1, nburn=NBURN, njumps=NJUMPS,
                          sampleevery=SE)
     lib = capi.Cudimot(model, cfg)
@@ -795,6 +824,25 @@ def bench_bingham(a, dev):
     ms = {"gridsearch": ev[0].elapsed_time(ev[1]), "levmar": ev[1].elapsed_time(ev[2]),
           "mcmc": ev[2].elapsed_time(ev[3])}
     total = sum(ms.values())
+    lm_passes = lib.stats().lm_iterations
+    # per-stage FP32 rates from the plugin's operation counts (FLOPs of
+    # the library's Bingham plugin, averaged over the workload's voxels)
+    from cudimot_gb300 import flops
+    ops = flops.count_ops(model, wl.truth[:512], wl.cfp, wl.fixp[:512])
+    like = flops.likelihood_flops(ops, 288)
+    like_prop = ops["derived_p_one_param"] + 288 * (ops["signal"] + 3.0)
+    work = {"gridsearch": 11050 * like * n, "levmar": flops.levmar_pass_flops(ops, 288, 7) * lm_passes,
+            "mcmc": (NBURN + NJUMPS) * 7 * like_prop * n}
+    pk = fp32_peak_tflops(dev)
+    stage_rate = {st_: work[st_] / (ms[st_] / 1e3) / 1e12 for st_ in ms}
+    roof = {"bound": "fp32", "kernel": "cdm_mcmc_kernel", "achieved": stage_rate["mcmc"],
+            "unit": "TFLOP/s", "peak": pk["tflops"] if pk else None,
+            "frac": stage_rate["mcmc"] / pk["tflops"] if pk else None,
+            "peak_source": pk["source"] if pk else None,
+            "flop_per_signal": ops["signal"], "stages_tflops": stage_rate,
+            "note": "FP32 work of the plugin as the library evaluates it (the saddlepoint 1F1 "
+                    "restated for single precision); the LM solve and the energies are FP64 "
+                    "and not counted"}
     # precision study on a subset: LM in FP32 (GPU) vs FP64 (oracle) from the same start
     from oracle.oracle import Oracle
     o = Oracle(model)
@@ -855,8 +903,8 @@ def bench_bingham(a, dev):
                      {"workload": "noddi_bingham_gs_lm_mcmc", "model": model, "nvox": n, "nmeas": 288,
                       "grid_combs": 11050, "nburn": NBURN, "njumps": NJUMPS, "sampleevery": SE,
                       "l2": "inputs larger than L2 (no flush)"},
-                     clk.summary(), stages_ms=ms,
-                     lm_iterations_per_voxel=lib.stats().lm_iterations / (n + k),
+                     clk.summary(), stages_ms=ms, roofline=roof,
+                     lm_iterations_per_voxel=lm_passes / n,
                      fp32_vs_fp64_oracle_lm=vs_oracle, posterior_mean_vs_truth=vs_truth,
                      reference_kernels=refk, gpu_launches=9)
     # one pass of the 1M-voxel fit (a few minutes) is the measurement

@@ -382,6 +382,9 @@ def build_utils(force=False):
 # heterogeneous workload (tensor, ball & two sticks, NODDI-Watson).
 HETERO_MODELS = ("DiffusionTensor", "Ball_2_Sticks", "NODDI_Watson")
 HETERO_LANES = (1, 2, 4)
+# bytes of a model's MCMC argument block in the persistent kernel's
+# parameters (one slot per entry; models with up to 17 parameters)
+HETERO_ARGS_BLOCK = 640
 
 
 def hetero_lib_path(tag="default"):
@@ -389,7 +392,7 @@ def hetero_lib_path(tag="default"):
 
 
 def build_hetero(models=HETERO_MODELS, lanes=HETERO_LANES, tag="default", model_dirs=None,
-                 eval_types=None, force=False, verbose=False, jobs=None):
+                 eval_types=None, force=False, verbose=False, jobs=None, lto=False):
     """libcdm_hetero_<tag>.so: one persistent MCMC kernel over several models
     (cdm_hetero.h). Each model's part (cdm_hetero_part.cu) is compiled with
     relocatable device code in a translation unit of its own, against that
@@ -412,12 +415,12 @@ def build_hetero(models=HETERO_MODELS, lanes=HETERO_LANES, tag="default", model_
         for x in sorted(os.listdir(d)):
             if x.endswith((".h", ".cc", ".cu", ".hpp")):
                 h.update(open(os.path.join(d, x), "rb").read())
-    h.update(repr(tuple(lanes)).encode())
+    h.update(repr((tuple(lanes), lto)).encode())
     dig = h.hexdigest()
     stamp = out + ".sha256"
     if not force and os.path.exists(out) and os.path.exists(stamp) and open(stamp).read() == dig:
         return out, None
-    lane_list = " ".join(f"X({g})" for g in lanes)
+    lane_list = " ".join(f"X({g}, {li})" for li, g in enumerate(lanes))
     with open(os.path.join(hdir, "cdm_hx_dispatch.h"), "w") as f:
         f.write("// generated by cudimot_gb300/build.py: entries of the linked models\n#pragma once\n")
         entries = []
@@ -425,13 +428,19 @@ def build_hetero(models=HETERO_MODELS, lanes=HETERO_LANES, tag="default", model_
             for g in lanes:
                 for r in (0, 1):
                     nm = f"cdm_hx_{i}_mcmc_{g}_{r}"
-                    f.write(f'extern "C" __device__ void {nm}(int, unsigned char*, const void*);\n')
+                    f.write(f'extern "C" __device__ void {nm}(int, unsigned char*);\n')
                     entries.append(nm)
-        f.write("__device__ __forceinline__ void cdm_hx_dispatch(int fn, int tile, unsigned char* "
-                "scratch, const void* args) {\n  switch (fn) {\n")
+        # entry k reads its argument block from slot k of the constant
+        # table cdm_hx_args
+        f.write("__device__ __forceinline__ void cdm_hx_dispatch(int fn, int tile, "
+                "unsigned char* scratch) {\n  switch (fn) {\n")
         for k, nm in enumerate(entries):
-            f.write(f"    case {k}: {nm}(tile, scratch, args); break;\n")
+            f.write(f"    case {k}: {nm}(tile, scratch); break;\n")
         f.write("    default: break;\n  }\n}\n")
+    with open(os.path.join(hdir, "cdm_hx_entries.h"), "w") as f:
+        f.write("// generated by cudimot_gb300/build.py\n#pragma once\n")
+        f.write(f"#define CDM_HX_ENTRIES {len(entries)}\n#define CDM_HX_ARGS_BLOCK {HETERO_ARGS_BLOCK}\n")
+        f.write(f"#define CDM_HX_NLANES {len(lanes)}\n#define CDM_HX_LANES(X) {lane_list}\n")
     with open(os.path.join(hdir, "cdm_hx_set.h"), "w") as f:
         f.write("// generated by cudimot_gb300/build.py: the linked models\n#pragma once\n")
         f.write(f"constexpr int kHxNumModels = {len(names)};\n")
@@ -441,12 +450,13 @@ def build_hetero(models=HETERO_MODELS, lanes=HETERO_LANES, tag="default", model_
         f.write(f"constexpr int kHxNumLanes = {len(lanes)};\n")
         f.write("static const int kHxLanes[] = {" + ", ".join(str(g) for g in lanes) + "};\n")
         f.write("constexpr int kHxThreads = 128;\n")
-    # link-time optimisation: the parts reach the device link as IR, so the
-    # entries are inlined into the persistent kernel and registers are
-    # allocated for the whole kernel (a call through the ABI spills)
-    lto = "-gencode=arch=compute_103a,code=lto_103a"
-    base = [nvcc_path(), "-O3", "-std=c++17", lto, "-lineinfo", "-rdc=true",
-            "-Xcompiler", "-ffp-contract=off"]
+    # lto: the parts reach the device link as IR and the entries are
+    # inlined into the persistent kernel; otherwise each entry is compiled
+    # on its own, as a kernel of the model library is, and called through
+    # the ABI once per tile (saving and restoring the registers it uses)
+    gen_flag = "-gencode=arch=compute_103a,code=lto_103a" if lto else ARCH
+    base = [nvcc_path(), "-O3", "-std=c++17", gen_flag, "-lineinfo", "-rdc=true",
+            "-maxrregcount=128", "-Xcompiler", "-ffp-contract=off"]
     if verbose:
         base += ["-Xptxas", "-v"]
 
@@ -455,9 +465,8 @@ def build_hetero(models=HETERO_MODELS, lanes=HETERO_LANES, tag="default", model_
         gen = os.path.join(hdir, f"gen_{i}")
         os.makedirs(gen, exist_ok=True)
         _write_sizes(gen, block_sizes(d))
-        macro = f"-DCDM_HX_LANES(X)={lane_list}"
         o = os.path.join(hdir, f"part_{i}.o")
-        cmd = base + eval_flags(e) + [f"-DCDM_HX_ID={i}", macro] + _includes(gen, d) + \
+        cmd = base + eval_flags(e) + [f"-DCDM_HX_ID={i}", "-I", hdir] + _includes(gen, d) + \
             ["-c", os.path.join(hsrc, "cdm_hetero_part.cu"), "-o", o]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if verbose:
@@ -475,8 +484,8 @@ def build_hetero(models=HETERO_MODELS, lanes=HETERO_LANES, tag="default", model_
     if kr.returncode != 0:
         return out, (kr.stdout + kr.stderr)[-6000:]
     cubin = os.path.join(hdir, "cdm_hetero.cubin")
-    lcmd = [nvcc_path(), "-arch=sm_103a", "-dlto", "-dlink", "--cubin"] + [o for o, _ in parts] + \
-        [kobj, "-o", cubin]
+    lcmd = [nvcc_path(), "-arch=sm_103a"] + (["-dlto"] if lto else []) + ["-dlink", "--cubin"] + \
+        [o for o, _ in parts] + [kobj, "-o", cubin]
     if verbose:
         lcmd[1:1] = ["-Xnvlink", "-v"]
     r = subprocess.run(lcmd, capture_output=True, text=True)

@@ -46,31 +46,34 @@ struct cdm_hetero {
   size_t static_smem = 0;
   unsigned args_bytes[kHxNumModels] = {};
   cdm_hx_item* d_items = nullptr;
-  unsigned char* d_args = nullptr;
-  int* d_counter = nullptr;
+  int* d_counter = nullptr;  // one per launch of a call
   int cap = 0;
+  int counters = 0;
   int last_grid = 0;
+  int last_launches = 0;
+  unsigned char* d_args = nullptr;  // the constant slot table cdm_hx_args
   std::vector<cdm_hx_item> items;
-  std::vector<unsigned char> args;
+  std::vector<unsigned char> slots;  // host image of the slot table, per launch
 };
 
 namespace {
 
-cdm_status grow(cdm_hetero* h, int n) {
-  if (n <= h->cap) return CDM_OK;
-  const int cap = std::max(n, 2 * h->cap);
-  cdm_hx_item* it = nullptr;
-  unsigned char* ar = nullptr;
-  HX_CUDA(cudaMalloc(&it, sizeof(cdm_hx_item) * cap));
-  if (cudaMalloc(&ar, (size_t)CDM_TILE_ARGS_MAX * cap) != cudaSuccess) {
-    cudaFree(it);
-    return fail(CDM_CUDA_ERROR, "cudaMalloc of the argument blocks failed");
+cdm_status grow(cdm_hetero* h, int n, int launches) {
+  if (n > h->cap) {
+    const int cap = std::max(n, 2 * h->cap);
+    cdm_hx_item* it = nullptr;
+    HX_CUDA(cudaMalloc(&it, sizeof(cdm_hx_item) * cap));
+    cudaFree(h->d_items);
+    h->d_items = it;
+    h->cap = cap;
   }
-  cudaFree(h->d_items);
-  cudaFree(h->d_args);
-  h->d_items = it;
-  h->d_args = ar;
-  h->cap = cap;
+  if (launches > h->counters) {
+    int* c = nullptr;
+    HX_CUDA(cudaMalloc(&c, sizeof(int) * launches));
+    cudaFree(h->d_counter);
+    h->d_counter = c;
+    h->counters = launches;
+  }
   return CDM_OK;
 }
 
@@ -141,9 +144,15 @@ cdm_status cdm_hetero_create(cdm_hetero** out) {
     if (e != cudaSuccess)
       return bail(fail(CDM_CUDA_ERROR, std::string(name) + ": " + cudaGetErrorString(e)));
   }
-  if (cudaMalloc(&h->d_counter, sizeof(int)) != cudaSuccess)
-    return bail(fail(CDM_CUDA_ERROR, "cudaMalloc of the tile counter failed"));
-  const cdm_status s = grow(h, 16);
+  {
+    void* p = nullptr;
+    size_t bytes = 0;
+    e = cudaLibraryGetGlobal(&p, &bytes, h->lib, "cdm_hx_args");
+    if (e != cudaSuccess || bytes != sizeof(unsigned char) * CDM_HX_ENTRIES * CDM_HX_ARGS_BLOCK)
+      return bail(fail(CDM_CUDA_ERROR, std::string("cdm_hx_args: ") + cudaGetErrorString(e)));
+    h->d_args = static_cast<unsigned char*>(p);
+  }
+  const cdm_status s = grow(h, 16, 4);
   if (s != CDM_OK) return bail(s);
   *out = h;
   return CDM_OK;
@@ -152,7 +161,6 @@ cdm_status cdm_hetero_create(cdm_hetero** out) {
 cdm_status cdm_hetero_destroy(cdm_hetero* h) {
   if (!h) return CDM_OK;
   if (h->d_items) cudaFree(h->d_items);
-  if (h->d_args) cudaFree(h->d_args);
   if (h->d_counter) cudaFree(h->d_counter);
   if (h->lib) cudaLibraryUnload(h->lib);
   delete h;
@@ -164,10 +172,8 @@ int cdm_hetero_last_grid(const cdm_hetero* h) { return h ? h->last_grid : 0; }
 cdm_status cdm_hetero_mcmc(cdm_hetero* h, int n, const cdm_tile_work* items, void* stream) {
   if (!h) return fail(CDM_BAD_ARG, "null cdm_hetero");
   if (n < 0 || (n > 0 && !items)) return fail(CDM_BAD_ARG, "bad item list");
-  h->items.clear();
-  h->args.assign((size_t)std::max(n, 1) * CDM_TILE_ARGS_MAX, 0);
-  size_t max_sm = 0, max_args = 0, max_scratch = 0;
-  long tiles = 0;
+  // check every item first: nothing is launched for a bad list
+  std::vector<int> fn(n, -1);
   for (int k = 0; k < n; k++) {
     const cdm_tile_work& w = items[k];
     const int m = model_index(w);
@@ -184,59 +190,85 @@ cdm_status cdm_hetero_mcmc(cdm_hetero* h, int n, const cdm_tile_work* items, voi
       return fail(CDM_BAD_ARG, "item " + std::to_string(k) + ": built for " +
                                    std::to_string(w.threads) + " threads per CTA, this library for " +
                                    std::to_string(kHxThreads));
-    if (w.args_bytes != h->args_bytes[m] || w.args_bytes % 4 || w.args_bytes > CDM_TILE_ARGS_MAX)
+    if (w.args_bytes != h->args_bytes[m] || w.args_bytes > CDM_HX_ARGS_BLOCK)
       return fail(CDM_BAD_ARG, "item " + std::to_string(k) + ": argument block of " +
                                    std::to_string(w.args_bytes) + " bytes, the linked model's is " +
                                    std::to_string(h->args_bytes[m]));
     if (w.ntiles < 0 || !w.err) return fail(CDM_BAD_ARG, "item " + std::to_string(k) + ": not prepared");
-    if (w.ntiles == 0) continue;
-    cdm_hx_item it;
-    it.args = nullptr;  // set after the upload buffer is known
-    it.err = static_cast<int*>(w.err);
-    it.fn = (m * kHxNumLanes + l) * 2 + (w.rician ? 1 : 0);
-    it.tile0 = (int)tiles;
-    it.ntiles = w.ntiles;
-    it.args_words = w.args_bytes / 4;
-    std::memcpy(h->args.data() + h->items.size() * CDM_TILE_ARGS_MAX, w.args, w.args_bytes);
-    h->items.push_back(it);
-    tiles += w.ntiles;
-    max_sm = std::max(max_sm, (size_t)w.smem_bytes);
-    max_args = std::max(max_args, (size_t)w.args_bytes);
-    max_scratch = std::max(max_scratch, (size_t)w.scratch_bytes);
+    if (w.ntiles > 0) fn[k] = (m * kHxNumLanes + l) * 2 + (w.rician ? 1 : 0);
+  }
+  // launches: each fit's argument block has the slot of its entry, so fits
+  // that share an entry (same model, lanes and likelihood) go to successive
+  // launches, in order
+  std::vector<std::vector<int>> groups;
+  for (int k = 0; k < n; k++) {
+    if (fn[k] < 0) continue;
+    size_t g = 0;
+    while (g < groups.size() &&
+           std::any_of(groups[g].begin(), groups[g].end(), [&](int j) { return fn[j] == fn[k]; }))
+      g++;
+    if (g == groups.size()) groups.emplace_back();
+    groups[g].push_back(k);
   }
   h->last_grid = 0;
-  if (h->items.empty()) return CDM_OK;
-  if (tiles > 0x7fffffffL) return fail(CDM_BAD_ARG, "too many tiles");
-  const int ni = (int)h->items.size();
-  const cdm_status gs = grow(h, ni);
+  if (groups.empty()) return CDM_OK;
+  const cdm_status gs = grow(h, n, (int)groups.size());
   if (gs != CDM_OK) return gs;
-  for (int k = 0; k < ni; k++) h->items[k].args = h->d_args + (size_t)k * CDM_TILE_ARGS_MAX;
-  cdm_hx_launch L;
-  L.items = h->d_items;
-  L.nitems = ni;
-  L.ntiles = (int)tiles;
-  L.counter = h->d_counter;
-  L.args_off = (uint32_t)round16(max_sm);
-  L.scratch_off = (uint32_t)round16(L.args_off + max_args);
-  const size_t smem = L.scratch_off + max_scratch;
-  if (smem + h->static_smem > 227 * 1024)
-    return fail(CDM_BAD_ARG, "the fits need " + std::to_string(smem + h->static_smem) +
-                                 " bytes of shared memory per CTA, more than 227 KB");
   cudaStream_t st = (cudaStream_t)stream;
-  HX_CUDA(cudaMemcpyAsync(h->d_items, h->items.data(), sizeof(cdm_hx_item) * ni,
-                          cudaMemcpyHostToDevice, st));
-  HX_CUDA(cudaMemcpyAsync(h->d_args, h->args.data(), (size_t)CDM_TILE_ARGS_MAX * ni,
-                          cudaMemcpyHostToDevice, st));
-  HX_CUDA(cudaMemsetAsync(h->d_counter, 0, sizeof(int), st));
-  HX_CUDA(cudaFuncSetAttribute(h->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, h->kernel, kHxThreads, smem));
-  if (per_sm < 1) return fail(CDM_BAD_ARG, "the persistent kernel does not fit on an SM");
-  const int grid = (int)std::min<long>(tiles, (long)h->num_sms * per_sm);
-  void* argv[] = {&L};
-  HX_CUDA(cudaLaunchKernel(h->kernel, dim3(grid), dim3(kHxThreads), argv, smem, st));
-  h->last_grid = grid;
+  HX_CUDA(cudaMemsetAsync(h->d_counter, 0, sizeof(int) * groups.size(), st));
+  h->items.clear();
+  const size_t table = (size_t)CDM_HX_ENTRIES * CDM_HX_ARGS_BLOCK;
+  h->slots.assign(table * groups.size(), 0);
+  for (size_t g = 0; g < groups.size(); g++) {
+    cdm_hx_launch L;
+    std::memset(&L, 0, sizeof(L));
+    unsigned char* slots = h->slots.data() + g * table;
+    size_t max_sm = 0, max_scratch = 0;
+    long tiles = 0;
+    const size_t first = h->items.size();
+    for (int k : groups[g]) {
+      const cdm_tile_work& w = items[k];
+      cdm_hx_item it;
+      it.err = static_cast<int*>(w.err);
+      it.fn = fn[k];
+      it.tile0 = (int)tiles;
+      it.ntiles = w.ntiles;
+      it.pad = 0;
+      h->items.push_back(it);
+      std::memcpy(slots + (size_t)fn[k] * CDM_HX_ARGS_BLOCK, w.args, w.args_bytes);
+      tiles += w.ntiles;
+      max_sm = std::max(max_sm, (size_t)w.smem_bytes);
+      max_scratch = std::max(max_scratch, (size_t)w.scratch_bytes);
+    }
+    if (tiles > 0x7fffffffL) return fail(CDM_BAD_ARG, "too many tiles");
+    L.items = h->d_items + first;
+    L.nitems = (int)(h->items.size() - first);
+    L.ntiles = (int)tiles;
+    L.counter = h->d_counter + g;
+    L.scratch_off = (uint32_t)round16(max_sm);
+    const size_t smem = L.scratch_off + max_scratch;
+    if (smem + h->static_smem > 227 * 1024)
+      return fail(CDM_BAD_ARG, "the fits need " + std::to_string(smem + h->static_smem) +
+                                   " bytes of shared memory per CTA, more than 227 KB");
+    // descriptors and argument slots of this launch, in stream order: a
+    // later launch of the same call rewrites the slots only after this
+    // launch has run
+    HX_CUDA(cudaMemcpyAsync(h->d_items + first, h->items.data() + first,
+                            sizeof(cdm_hx_item) * L.nitems, cudaMemcpyHostToDevice, st));
+    HX_CUDA(cudaMemcpyAsync(h->d_args, slots, table, cudaMemcpyHostToDevice, st));
+    HX_CUDA(cudaFuncSetAttribute(h->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, h->kernel, kHxThreads, smem));
+    if (per_sm < 1) return fail(CDM_BAD_ARG, "the persistent kernel does not fit on an SM");
+    const int grid = (int)std::min<long>(tiles, (long)h->num_sms * per_sm);
+    void* argv[] = {&L};
+    HX_CUDA(cudaLaunchKernel(h->kernel, dim3(grid), dim3(kHxThreads), argv, smem, st));
+    h->last_grid = std::max(h->last_grid, grid);
+  }
+  h->last_launches = (int)groups.size();
   return CDM_OK;
 }
+
+int cdm_hetero_last_launches(const cdm_hetero* h) { return h ? h->last_launches : 0; }
 
 }  // extern "C"

@@ -2,13 +2,16 @@
 //
 // One launch of SMs x resident CTAs. Each CTA repeatedly takes the next
 // tile from a device counter (tiles of all fits numbered consecutively,
-// fit after fit), finds its fit, copies the fit's argument block into
-// shared memory and calls that model's MCMC code for the tile
-// (cdm_hetero_part.cu: the same code as the model library's own MCMC
-// kernel, with the tile in place of blockIdx.x). Dynamic shared memory is
-// laid out as [the largest fit's protocol tables | argument block |
-// scratch]. A fit whose error word is set (a bounded wait ran out) makes
-// the CTA that ran it stop taking tiles; there is no other wait.
+// fit after fit), finds its fit and calls that model's MCMC code for the
+// tile (cdm_hetero_part.cu: the same code as the model library's own MCMC
+// kernel, with the tile in place of blockIdx.x). The fits' argument blocks
+// are in cdm_hx_args, one constant-memory slot per entry of the dispatch
+// table, written by the host before the launch in stream order; each entry
+// reads its own slot, so the chain code takes its arguments from the
+// constant bank as the model library's kernel does. Dynamic shared memory
+// is laid out as [the largest fit's protocol tables | scratch]. A fit whose
+// error word is set (a bounded wait ran out) makes the CTA that ran it stop
+// taking tiles; there is no other wait.
 #include <stdint.h>
 
 #include "cdm_hetero_desc.h"
@@ -20,6 +23,10 @@
 #ifndef CDM_MCMC_MIN_BLOCKS
 #define CDM_MCMC_MIN_BLOCKS 4
 #endif
+
+extern "C" {
+__constant__ __align__(16) unsigned char cdm_hx_args[CDM_HX_ENTRIES][CDM_HX_ARGS_BLOCK];
+}
 
 extern "C" __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS)
     cdm_hx_mcmc(const __grid_constant__ cdm_hx_launch L) {
@@ -40,11 +47,7 @@ extern "C" __global__ void __launch_bounds__(CDM_NT, CDM_MCMC_MIN_BLOCKS)
     const int t = s_tile, i = s_item;
     if (t >= L.ntiles) break;
     const cdm_hx_item it = L.items[i];
-    uint32_t* dst = reinterpret_cast<uint32_t*>(dsm + L.args_off);
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(it.args);
-    for (uint32_t k = threadIdx.x; k < it.args_words; k += CDM_NT) dst[k] = src[k];
-    __syncthreads();
-    cdm_hx_dispatch(it.fn, t - it.tile0, dsm + L.scratch_off, dsm + L.args_off);
+    cdm_hx_dispatch(it.fn, t - it.tile0, dsm + L.scratch_off);
     __syncthreads();
     prev = i;
   }

@@ -37,7 +37,7 @@ __device__ __forceinline__ float cdm_prior(const cdm_limits& lim, int p, cdm_rea
       return d * d / (2.0f * lim.pb[p] * lim.pb[p]);
     }
     case GAMMAPRIOR:
-      return (1.0f - lim.pa[p]) * logf(x) + lim.pb[p] * x;
+      return __fmaf_rn(lim.pb[p], x, __fmul_rn(1.0f - lim.pa[p], logf(x)));
     case ARDPRIOR:
       return lim.pa[p] * logf(x);
     case SINPRIOR:
@@ -82,9 +82,14 @@ __device__ __forceinline__ void cdm_set(Tv* a, int i, Tv x) {
 template <int Gw, bool RICIAN>
 __device__ __forceinline__ double cdm_likelihood(const cdm_voxel_io& io, const float* sproto,
                                                  cdm_real* P, cdm_real* FixP, float tau, unsigned gmask) {
+  // The energies are written with explicitly rounded operations: whether a
+  // multiply and an add are fused is then fixed by the source, not by the
+  // compiler's view of the surrounding code, so the chain is the same in
+  // every kernel this code is compiled into (model library, multi-model
+  // kernel).
   if (RICIAN) {
     const double s = cdm_group_rician<Gw>(io, sproto, P, FixP, tau, gmask);
-    return -(double)io.nmeas * (double)logf(tau) - s;
+    return __fma_rn(-(double)io.nmeas, (double)logf(tau), -s);
   }
   // (n/2) log(SSE/2) with SSE kept in FP64: log(m 2^e) = log m + e log 2,
   // the mantissa's log in FP32 (absolute error ~6e-8 for m in [0.5, 1))
@@ -92,7 +97,8 @@ __device__ __forceinline__ double cdm_likelihood(const cdm_voxel_io& io, const f
   const double sse = cdm_group_sse<Gw>(io, sproto, P, FixP, gmask);
   int ex;
   const double m = frexp(0.5 * sse, &ex);
-  return 0.5 * (double)io.nmeas * ((double)logf((float)m) + (double)ex * 0.69314718055994531);
+  const double l = __fma_rn((double)ex, 0.69314718055994531, (double)logf((float)m));
+  return __dmul_rn(0.5 * (double)io.nmeas, l);
 }
 
 // Records sample s of a sample row (element index row0 + s of dst, a row
@@ -226,22 +232,22 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
       tau = (float)((double)io.nmeas / cdm_group_sum<Gw>((double)s2, gm));
       tauSD = tau * 0.5f;
     }
-    energy = (double)total_prior + cdm_likelihood<Gw, RICIAN>(io, sproto, P, FixP, tau, gm);
+    energy = __dadd_rn((double)total_prior, cdm_likelihood<Gw, RICIAN>(io, sproto, P, FixP, tau, gm));
 
     for (int it = 0; it < niters; it++) {
       const uint32_t git = (uint32_t)(recording ? nburn + it : it);
       if (RICIAN) {
         const cdm_draw d = cdm_mcmc_draw(a.seed, vid, git, CDM_RNG_SLOT_TAU, a.stream);
         const float old = tau;
-        tau = tau + d.normal * tauSD;
+        tau = __fmaf_rn(d.normal, tauSD, tau);
         if (tau > 0.0f) {
           if (stale) cdm_update_derived(P, FixP);
           stale = false;
           float tp = 0.0f;
 #pragma unroll
           for (int p = 0; p < kNP; p++) tp += prior[p];
-          const double ne = (double)tp + cdm_likelihood<Gw, RICIAN>(io, sproto, P, FixP, tau, gm);
-          if (expf((float)(energy - ne)) > d.uniform) {
+          const double ne = __dadd_rn((double)tp, cdm_likelihood<Gw, RICIAN>(io, sproto, P, FixP, tau, gm));
+          if (expf((float)__dsub_rn(energy, ne)) > d.uniform) {
             tacc++;
             energy = ne;
           } else {
@@ -261,7 +267,7 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
         }
         const cdm_draw d = cdm_mcmc_draw(a.seed, vid, git, (uint32_t)p, a.stream);
         const cdm_real old = cdm_get(P, p);
-        cdm_set(P, p, cdm_real((float)old + d.normal * cdm_get(propSD, p)));
+        cdm_set(P, p, cdm_real(__fmaf_rn(d.normal, cdm_get(propSD, p), (float)old)));
         bool accepted = false;
         bool derived = false;
         if (cdm_in_bounds(lim, p, P)) {
@@ -272,8 +278,8 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
           float tp = 0.0f;
 #pragma unroll
           for (int q = 0; q < kNP; q++) tp += (q == p) ? np_ : prior[q];
-          const double ne = (double)tp + cdm_likelihood<Gw, RICIAN>(io, sproto, P, FixP, tau, gm);
-          if (expf((float)(energy - ne)) > d.uniform) {
+          const double ne = __dadd_rn((double)tp, cdm_likelihood<Gw, RICIAN>(io, sproto, P, FixP, tau, gm));
+          if (expf((float)__dsub_rn(energy, ne)) > d.uniform) {
             accepted = true;
             energy = ne;
             cdm_set(prior, p, np_);

@@ -36,6 +36,15 @@ def likelihood_flops(ops, nmeas):
     return ops["derived_p"] + nmeas * (ops["signal"] + 3.0)
 
 
+def levmar_pass_flops(ops, nmeas, nparams):
+    """One LM pass of the fused kernel per voxel: for every measurement the
+    signal, the Jacobian row, the residual, J^T r (2 per parameter) and the
+    upper triangle of J^T J (2 per entry); plus Derived_P. The FP64 solve is
+    not counted (it runs on the FP64 pipe, n^3/6 multiply-adds)."""
+    per_meas = ops["signal"] + ops["jacobian"] + 1.0 + 2.0 * nparams + nparams * (nparams + 1)
+    return ops["derived_p"] + nmeas * per_meas
+
+
 def watson_c1_flops_per_voxel(nburn=1250, njumps=1250, combs=968, nmeas=288, n=512, seed=1):
     """NODDI-Watson FLOPs per voxel of the C1 workload, averaged over
     parameters drawn from its prior and its 288-measurement protocol."""

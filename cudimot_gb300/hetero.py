@@ -27,7 +27,7 @@ class TileWork(C.Structure):
 
 
 EXPORTED = ("cdm_hetero_create", "cdm_hetero_destroy", "cdm_hetero_models", "cdm_hetero_mcmc",
-            "cdm_hetero_last_grid", "cdm_hetero_last_error")
+            "cdm_hetero_last_grid", "cdm_hetero_last_launches", "cdm_hetero_last_error")
 
 
 def load(tag: str = "default", path: str = None):
@@ -42,8 +42,10 @@ def load(tag: str = "default", path: str = None):
     lib.cdm_hetero_models.restype = C.c_size_t
     lib.cdm_hetero_mcmc.argtypes = [vp, C.c_int, C.POINTER(TileWork), vp]
     lib.cdm_hetero_last_grid.argtypes = [vp]
+    lib.cdm_hetero_last_launches.argtypes = [vp]
     lib.cdm_hetero_last_error.restype = C.c_char_p
-    for n in ("cdm_hetero_create", "cdm_hetero_destroy", "cdm_hetero_mcmc", "cdm_hetero_last_grid"):
+    for n in ("cdm_hetero_create", "cdm_hetero_destroy", "cdm_hetero_mcmc", "cdm_hetero_last_grid",
+              "cdm_hetero_last_launches"):
         getattr(lib, n).restype = C.c_int
     return lib
 
@@ -100,3 +102,7 @@ class Hetero:
     @property
     def last_grid(self) -> int:
         return self.lib.cdm_hetero_last_grid(self.h)
+
+    @property
+    def last_launches(self) -> int:
+        return self.lib.cdm_hetero_last_launches(self.h)

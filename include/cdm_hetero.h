@@ -70,16 +70,22 @@ size_t cdm_hetero_models(char* buf, size_t cap);
 /* Run the MCMC of n prepared fits in one persistent launch on `stream`
  * (the stream the fits were prepared on, or one ordered after it). Every
  * item's model, evaluation type, lane count and CTA size must be one this
- * library was built with (CDM_BAD_ARG otherwise, before any launch). A
- * bounded wait that runs out inside a tile sets that context's error word
- * (read by cdm_synchronize / cdm_get_stats of its library) and stops the
- * CTA. Not capturable into a CUDA graph (the descriptors are uploaded from
- * host memory on each call). */
+ * library was built with (CDM_BAD_ARG otherwise, before any launch). The
+ * fits' argument blocks travel as the kernel's parameters, one slot per
+ * (model, lanes, likelihood): fits that share all three run in successive
+ * launches of the same kernel. A bounded wait that runs out inside a tile
+ * sets that context's error word (read by cdm_synchronize / cdm_get_stats
+ * of its library) and stops the CTA. Calls on one cdm_hetero must be
+ * ordered on the GPU (one stream, or streams ordered by the caller): they
+ * share its descriptor buffers. Not capturable into a CUDA graph (the
+ * descriptors are uploaded from host memory on each call). */
 cdm_status cdm_hetero_mcmc(cdm_hetero* h, int n, const cdm_tile_work* items, void* stream);
 
-/* CTAs of the last cdm_hetero_mcmc launch (SMs x resident CTAs, or fewer
- * when there are fewer tiles). */
+/* CTAs of the largest launch of the last cdm_hetero_mcmc call (SMs x
+ * resident CTAs, or fewer when there are fewer tiles), and the number of
+ * launches it made (1 unless two fits shared model, lanes and likelihood). */
 int cdm_hetero_last_grid(const cdm_hetero* h);
+int cdm_hetero_last_launches(const cdm_hetero* h);
 
 /* Message of the last failure on this thread. */
 const char* cdm_hetero_last_error(void);
