@@ -392,7 +392,8 @@ def hetero_lib_path(tag="default"):
 
 
 def build_hetero(models=HETERO_MODELS, lanes=HETERO_LANES, tag="default", model_dirs=None,
-                 eval_types=None, force=False, verbose=False, jobs=None, lto=False):
+                 eval_types=None, force=False, verbose=False, jobs=None, lto=False, maxrreg=128,
+                 whole=False):
     """libcdm_hetero_<tag>.so: one persistent MCMC kernel over several models
     (cdm_hetero.h). Each model's part (cdm_hetero_part.cu) is compiled with
     relocatable device code in a translation unit of its own, against that
@@ -415,7 +416,7 @@ def build_hetero(models=HETERO_MODELS, lanes=HETERO_LANES, tag="default", model_
         for x in sorted(os.listdir(d)):
             if x.endswith((".h", ".cc", ".cu", ".hpp")):
                 h.update(open(os.path.join(d, x), "rb").read())
-    h.update(repr((tuple(lanes), lto)).encode())
+    h.update(repr((tuple(lanes), lto, maxrreg, whole)).encode())
     dig = h.hexdigest()
     stamp = out + ".sha256"
     if not force and os.path.exists(out) and os.path.exists(stamp) and open(stamp).read() == dig:
@@ -455,8 +456,11 @@ def build_hetero(models=HETERO_MODELS, lanes=HETERO_LANES, tag="default", model_
     # on its own, as a kernel of the model library is, and called through
     # the ABI once per tile (saving and restoring the registers it uses)
     gen_flag = "-gencode=arch=compute_103a,code=lto_103a" if lto else ARCH
+    # registers per thread: 128 gives 4 resident CTAs of 128 threads per
+    # SM, as the model libraries' MCMC kernels have
     base = [nvcc_path(), "-O3", "-std=c++17", gen_flag, "-lineinfo", "-rdc=true",
-            "-maxrregcount=128", "-Xcompiler", "-ffp-contract=off"]
+            f"-maxrregcount={maxrreg}", f"-DCDM_MCMC_MIN_BLOCKS={65536 // (128 * maxrreg)}",
+            "-Xcompiler", "-ffp-contract=off"]
     if verbose:
         base += ["-Xptxas", "-v"]
 
@@ -473,26 +477,52 @@ def build_hetero(models=HETERO_MODELS, lanes=HETERO_LANES, tag="default", model_
             sys.stderr.write(r.stdout + r.stderr)
         return o, None if r.returncode == 0 else f"{n}: " + (r.stdout + r.stderr)[-6000:]
 
-    kobj = os.path.join(hdir, "kernel.o")
-    kcmd = base + ["-I", hdir, "-I", hsrc, "-c", os.path.join(hsrc, "cdm_hetero_kernel.cu"), "-o", kobj]
-    with cf.ThreadPoolExecutor(jobs or min(len(names) + 1, os.cpu_count() or 1)) as ex:
-        parts = list(ex.map(part, range(len(names))))
-        kr = subprocess.run(kcmd, capture_output=True, text=True)
-    for _, err in parts:
-        if err:
-            return out, err
-    if kr.returncode != 0:
-        return out, (kr.stdout + kr.stderr)[-6000:]
     cubin = os.path.join(hdir, "cdm_hetero.cubin")
-    lcmd = [nvcc_path(), "-arch=sm_103a"] + (["-dlto"] if lto else []) + ["-dlink", "--cubin"] + \
-        [o for o, _ in parts] + [kobj, "-o", cubin]
-    if verbose:
-        lcmd[1:1] = ["-Xnvlink", "-v"]
-    r = subprocess.run(lcmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        return out, (r.stdout + r.stderr)[-6000:]
-    if verbose:
-        sys.stderr.write(r.stdout + r.stderr)
+    if whole:
+        # one model: the part and the persistent kernel in one translation
+        # unit, compiled as a whole program (no device link)
+        if len(names) != 1:
+            return out, "whole-program build of the multi-model kernel takes one model"
+        gen = os.path.join(hdir, "gen_0")
+        os.makedirs(gen, exist_ok=True)
+        _write_sizes(gen, block_sizes(model_dirs[0]))
+        tu = os.path.join(hdir, "cdm_hetero_whole.cu")
+        with open(tu, "w") as f:
+            f.write("// generated by cudimot_gb300/build.py\n#define CDM_HX_ID 0\n")
+            f.write(f'#include "{os.path.join(hsrc, "cdm_hetero_part.cu")}"\n')
+            f.write(f'#include "{os.path.join(hsrc, "cdm_hetero_kernel.cu")}"\n')
+        cmd = [nvcc_path(), "-O3", "-std=c++17", ARCH, "-lineinfo", "-cubin",
+               "-Xcompiler", "-ffp-contract=off", "-I", hdir, "-I", hsrc] + eval_flags(eval_types[0]) + \
+            _includes(gen, model_dirs[0]) + [tu, "-o", cubin]
+        if verbose:
+            cmd[1:1] = ["-Xptxas", "-v"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if verbose:
+            sys.stderr.write(r.stdout + r.stderr)
+        if r.returncode != 0:
+            return out, (r.stdout + r.stderr)[-6000:]
+        parts = None
+    kobj = os.path.join(hdir, "kernel.o")
+    if not whole:
+        kcmd = base + ["-I", hdir, "-I", hsrc, "-c", os.path.join(hsrc, "cdm_hetero_kernel.cu"),
+                       "-o", kobj]
+        with cf.ThreadPoolExecutor(jobs or min(len(names) + 1, os.cpu_count() or 1)) as ex:
+            parts = list(ex.map(part, range(len(names))))
+            kr = subprocess.run(kcmd, capture_output=True, text=True)
+        for _, err in parts:
+            if err:
+                return out, err
+        if kr.returncode != 0:
+            return out, (kr.stdout + kr.stderr)[-6000:]
+        lcmd = [nvcc_path(), "-arch=sm_103a"] + (["-dlto"] if lto else []) + ["-dlink", "--cubin"] + \
+            [o for o, _ in parts] + [kobj, "-o", cubin]
+        if verbose:
+            lcmd[1:1] = ["-Xnvlink", "-v"]
+        r = subprocess.run(lcmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            return out, (r.stdout + r.stderr)[-6000:]
+        if verbose:
+            sys.stderr.write(r.stdout + r.stderr)
     image = os.path.join(hdir, "cdm_hetero_image.cpp")
     with open(image, "w") as f:
         f.write("// generated by cudimot_gb300/build.py: the multi-model module, embedded\n")

@@ -217,29 +217,29 @@ cdm_status launch(int fam, int lanes, dim3 grid, dim3 block, size_t smem, cudaSt
 // The dynamic shared memory a launch may use without opting in is 48 KB
 // less the kernel's static shared memory (the MCMC kernel's sample staging
 // is 4-37 KB, by lane count and parameter count), so the opt-in depends on
-// both; the static size is read once per kernel.
+// both; the static size is read once per kernel. The opt-in only ever
+// grows: lowering it while an earlier launch of the same kernel with more
+// shared memory is still queued is not safe.
 cdm_status set_smem(int fam, int lanes, size_t bytes) {
   if (bytes == 0) return CDM_OK;
   const void* fn = kfn(fam, lanes);
   if (!fn) return cdm_fail(CDM_CUDA_ERROR, std::string("kernel ") + cdm_kfam_name(fam) + " is not available");
   static std::mutex mu;
   static long static_bytes[CDM_K_COUNT][6];
+  static long opted[CDM_K_COUNT][6];
   static bool known[CDM_K_COUNT][6];
   const int li = fam < CDM_K_NLANE_FAMILIES ? cdm_lane_index(lanes) : 0;
   if (fam < 0 || fam >= CDM_K_COUNT || li < 0) return cdm_fail(CDM_BAD_ARG, "kernel family or lanes");
-  long st = 0;
-  {
-    std::lock_guard<std::mutex> lock(mu);
-    if (!known[fam][li]) {
-      cudaFuncAttributes fa;
-      CDM_CUDA(cudaFuncGetAttributes(&fa, fn));
-      static_bytes[fam][li] = (long)fa.sharedSizeBytes;
-      known[fam][li] = true;
-    }
-    st = static_bytes[fam][li];
+  std::lock_guard<std::mutex> lock(mu);
+  if (!known[fam][li]) {
+    cudaFuncAttributes fa;
+    CDM_CUDA(cudaFuncGetAttributes(&fa, fn));
+    static_bytes[fam][li] = (long)fa.sharedSizeBytes;
+    known[fam][li] = true;
   }
-  if ((long)bytes + st <= 48 * 1024) return CDM_OK;
+  if ((long)bytes + static_bytes[fam][li] <= 48 * 1024 || (long)bytes <= opted[fam][li]) return CDM_OK;
   CDM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  opted[fam][li] = (long)bytes;
   return CDM_OK;
 }
 

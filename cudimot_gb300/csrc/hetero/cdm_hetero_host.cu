@@ -44,6 +44,7 @@ struct cdm_hetero {
   cudaLibrary_t lib = nullptr;
   const void* kernel = nullptr;
   size_t static_smem = 0;
+  long opted_smem = 0;  // dynamic shared memory the kernel is opted in for
   unsigned args_bytes[kHxNumModels] = {};
   cdm_hx_item* d_items = nullptr;
   int* d_counter = nullptr;  // one per launch of a call
@@ -256,7 +257,12 @@ cdm_status cdm_hetero_mcmc(cdm_hetero* h, int n, const cdm_tile_work* items, voi
     HX_CUDA(cudaMemcpyAsync(h->d_items + first, h->items.data() + first,
                             sizeof(cdm_hx_item) * L.nitems, cudaMemcpyHostToDevice, st));
     HX_CUDA(cudaMemcpyAsync(h->d_args, slots, table, cudaMemcpyHostToDevice, st));
-    HX_CUDA(cudaFuncSetAttribute(h->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // the opt-in only grows: an earlier launch of this call (or of an
+    // earlier call) with more shared memory may still be queued
+    if ((long)smem > h->opted_smem) {
+      HX_CUDA(cudaFuncSetAttribute(h->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      h->opted_smem = (long)smem;
+    }
     int per_sm = 0;
     HX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, h->kernel, kHxThreads, smem));
     if (per_sm < 1) return fail(CDM_BAD_ARG, "the persistent kernel does not fit on an SM");

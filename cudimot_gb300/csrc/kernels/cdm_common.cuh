@@ -63,7 +63,10 @@ typedef fp32 cdm_real;
 #if defined(CDM_HETERO)
 #define CDM_KERNEL(...) __device__ __forceinline__ void
 #define CDM_KERNEL0 __device__ __forceinline__ void
-#define CDM_KARG(T) int cdm_tile, unsigned char* cdm_scratch, const T&
+// The argument block is in memory the kernel never writes: __restrict__
+// lets the compiler keep what it has loaded from it across the kernel's
+// own stores (a kernel parameter is known read-only; a reference is not).
+#define CDM_KARG(T) int cdm_tile, unsigned char* __restrict__ cdm_scratch, const T& __restrict__
 #define CDM_BLOCK_IDX cdm_tile
 #elif defined(CDM_DEVICE_MODULE)
 #define CDM_KERNEL(...) __device__ __forceinline__ void
