@@ -49,10 +49,13 @@ def parse():
                     help="voxels (default: the workload's own size)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="voxels for the CPU baseline")
-    ap.add_argument("--profile-stage", choices=["gridsearch", "levmar", "mcmc", "mlp_forward"],
+    ap.add_argument("--profile-stage",
+                    choices=["gridsearch", "levmar", "mcmc", "mlp_forward", "hetero_mcmc"],
                     default=None,
                     help="run the preceding stages, then one launch of this stage (for ncu); "
-                         "mlp_forward: two inference passes of the network on --nvox voxels")
+                         "mlp_forward: two inference passes of the network on --nvox voxels; "
+                         "hetero_mcmc: the MCMC of one NODDI-Watson fit through the model "
+                         "library, then through the persistent multi-model kernel")
     ap.add_argument("--lanes", type=int, default=None,
                     help="with --profile-stage: lanes per voxel (default: those the 200,000-voxel "
                          "headline runs with, 2 for grid search and MCMC, 4 for LM; the automatic "
@@ -271,6 +274,42 @@ def profile_mlp_forward(a, dev):
                       "hidden_layer": hidden_layer_roofline(li.net, dev, n=a.nvox)}))
 
 
+def profile_hetero(a, dev):
+    """One NODDI-Watson MCMC (--nvox voxels, --nburn + --njumps, 2 lanes)
+    through the model library's kernel, then the same fit through the
+    persistent multi-model kernel (libcdm_hetero): two launches to compare."""
+    import torch
+    from cudimot_gb300 import capi, hetero
+    a.nvox = a.nvox or 200_000
+    cfp, meas, fixp, init, _ = make_workload(a.nvox, 8219, dev)
+    t = lambda x: torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device=dev)  # noqa
+    m, c, f, i = t(meas), t(cfp), t(fixp), t(init)
+    cfg = capi.model_cfg(MODEL, run_mcmc=1, nburn=a.nburn, njumps=a.njumps, sampleevery=SE,
+                         lanes_mcmc=a.lanes or 2)
+    ns = max(a.njumps // SE, 1)
+    res = {}
+    h = hetero.Hetero()
+    keep = []
+    for path in ("library", "persistent"):
+        ctx = capi.Cudimot(MODEL, cfg)
+        p = i.clone()
+        s = torch.zeros(a.nvox, 5, ns, dtype=torch.float64, device=dev)
+        keep.append((ctx, p, s))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if path == "library":
+            e0.record()
+            ctx.mcmc(m, p, c, f, s)
+        else:
+            w = h.prepare(ctx, m, p, c, f, s)
+            e0.record()
+            h.mcmc([w])
+        e1.record()
+        torch.cuda.synchronize()
+        res[path] = e0.elapsed_time(e1)
+    res["samples_equal"] = bool(torch.equal(keep[0][2], keep[1][2]))
+    print(json.dumps({"stage": "hetero_mcmc", "nvox": a.nvox, "ms": res}))
+
+
 def profile_stage(a):
     """One launch of one stage on a small case, for ncu captures."""
     import torch
@@ -278,6 +317,9 @@ def profile_stage(a):
     dev = torch.device("cuda:0")
     if a.profile_stage == "mlp_forward":
         profile_mlp_forward(a, dev)
+        return
+    if a.profile_stage == "hetero_mcmc":
+        profile_hetero(a, dev)
         return
     a.nvox = a.nvox or 20000
     model, grid = MODEL, synth.WATSON_GRID

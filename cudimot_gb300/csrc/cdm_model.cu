@@ -375,6 +375,11 @@ struct cdm_ctx {
   int nmeas_pad = 0;
   // cdm_mcmc_prepare: the MCMC launch is described here instead of made
   cdm_tile_work* export_to = nullptr;
+  // cdm_fit_host on large calls: the pieces' contexts (own streams, own
+  // buffers) and the configuration they were made for
+  static constexpr int kMaxPieces = 4;
+  cdm_ctx* piece[kMaxPieces] = {};
+  cdm_model_cfg piece_cfg[kMaxPieces];
 };
 
 namespace {
@@ -864,6 +869,7 @@ cdm_status cdm_create(const cdm_model_cfg* cfg, cdm_ctx** out) {
 
 cdm_status cdm_destroy(cdm_ctx* c) {
   if (!c) return CDM_OK;
+  for (cdm_ctx* p : c->piece) cdm_destroy(p);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   void* bufs[] = {c->grid_dev, c->proto32, c->proto64, c->sig, c->gs_flags, c->gs_cand,
                   c->gs_best, c->shell_perm, c->shell_rank, c->err, c->counters, c->h_meas, c->h_params, c->h_cfp, c->h_fixp,
@@ -1208,13 +1214,15 @@ cdm_status cdm_clean_signals(int nvox, int nmeas, double* meas, void* stream) {
   return k_clean_signals((int)((threads + 255) / 256), (cudaStream_t)stream, nvox, nmeas, meas);
 }
 
-cdm_status cdm_fit_host(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
-                        const double* CFP, const double* FixP, double* samples, double* tau,
-                        double* pred, double* BIC, double* AIC, int part_size, int64_t timeout_ms) {
-  CDM_TRY(check_common(c, nvox, nmeas, CDM_CFP_TSIZE, CDM_FIXP_TSIZE));
-  if (!meas || !params || !CFP || !samples || (CDM_FIXP_TSIZE > 0 && !FixP))
-    return cdm_fail(CDM_BAD_ARG, "null array");
-  (void)part_size;  // CUDIMOT's SIZE_PART parts (dMRI_Data.cu:66-79): one part here
+}  // extern "C"
+
+namespace {
+
+// cdm_fit_host's stream work for one context: host->device copies, the fit
+// (cdm_fit, one captured graph), device->host copies; no synchronisation.
+cdm_status fit_host_enqueue(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
+                            const double* CFP, const double* FixP, double* samples, double* tau,
+                            double* pred, double* BIC, double* AIC, cudaStream_t st) {
   const cdm_model_cfg& o = c->cfg;
   const int ns = o.run_mcmc ? o.njumps / std::max(o.sampleevery, 1) : 1;
   const size_t nv = (size_t)nvox;
@@ -1232,8 +1240,6 @@ cdm_status cdm_fit_host(cdm_ctx* c, int nvox, int nmeas, const double* meas, dou
     CDM_TRY(dev_alloc(&c->h_bic, &c->h_bic_cap, nv));
     CDM_TRY(dev_alloc(&c->h_aic, &c->h_aic_cap, nv));
   }
-  if (!c->own_stream) CDM_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
-  cudaStream_t st = c->own_stream;
   CDM_CUDA(cudaMemcpyAsync(c->h_meas, meas, nv * nmeas * sizeof(double), cudaMemcpyHostToDevice, st));
   CDM_CUDA(cudaMemcpyAsync(c->h_params, params, nv * kNP * sizeof(double), cudaMemcpyHostToDevice, st));
   CDM_CUDA(cudaMemcpyAsync(c->h_cfp, CFP, (size_t)nmeas * CDM_CFP_TSIZE * sizeof(double),
@@ -1256,7 +1262,101 @@ cdm_status cdm_fit_host(cdm_ctx* c, int nvox, int nmeas, const double* meas, dou
     CDM_CUDA(cudaMemcpyAsync(BIC, c->h_bic, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
     CDM_CUDA(cudaMemcpyAsync(AIC, c->h_aic, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
   }
-  return cdm_synchronize(c, st, timeout_ms);
+  return CDM_OK;
+}
+
+// Pieces of a large cdm_fit_host call: 50,000 voxels or more per piece, at
+// most kMaxPieces.
+int fit_host_npieces(int nvox) {
+  return std::max(1, std::min(cdm_ctx::kMaxPieces, nvox / 50000));
+}
+
+// A large cdm_fit_host call as consecutive voxel ranges, each fitted by a
+// context of its own on its own stream (copies in, fit, copies out), all
+// in flight at once: the copies of one range overlap the fits of the
+// others, and the ranges' kernels share the GPU. Each range's context has
+// first_voxel = its start and the lane counts the whole call would have, so
+// every voxel gets the result of one call over all of them (the MCMC draws
+// are keyed by the global voxel index). On the GB300 a single 460 MB copy
+// issued right after the GPU had been busy took 26-45 ms instead of 2.2 ms;
+// in pieces, behind other pieces' fits, that time is hidden.
+cdm_status fit_host_pieces(cdm_ctx* c, int npieces, int nvox, int nmeas, const double* meas,
+                           double* params, const double* CFP, const double* FixP, double* samples,
+                           double* tau, double* pred, double* BIC, double* AIC, int64_t timeout_ms) {
+  const cdm_model_cfg& o = c->cfg;
+  const int ns = o.run_mcmc ? o.njumps / std::max(o.sampleevery, 1) : 1;
+  const int lanes_gs = pick_lanes(c, o.lanes_gridsearch, 2, nvox);
+  const int lanes_lm = pick_lanes(c, o.lanes_levmar, 4, nvox);
+  const int lanes_mc = pick_lanes(c, o.lanes_mcmc, 2, nvox);
+  for (int k = 0; k < npieces; k++) {
+    const int v0 = (int)((int64_t)nvox * k / npieces), v1 = (int)((int64_t)nvox * (k + 1) / npieces);
+    cdm_model_cfg pc;
+    std::memcpy(&pc, &o, sizeof(pc));  // byte for byte, padding included (compared below)
+    pc.first_voxel = o.first_voxel + v0;
+    pc.lanes_gridsearch = lanes_gs;
+    pc.lanes_levmar = lanes_lm;
+    pc.lanes_mcmc = lanes_mc;
+    pc.grid = c->grid_host.empty() ? nullptr : c->grid_host.data();
+    if (c->grid_host.empty()) pc.run_gridsearch = 0;
+    if (c->piece[k] && std::memcmp(&c->piece_cfg[k], &pc, sizeof(pc)) != 0) {
+      cdm_destroy(c->piece[k]);
+      c->piece[k] = nullptr;
+    }
+    if (!c->piece[k]) {
+      CDM_TRY(cdm_create(&pc, &c->piece[k]));
+      c->piece_cfg[k] = pc;
+    }
+    cdm_ctx* p = c->piece[k];
+    if (!p->own_stream) CDM_CUDA(cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking));
+    const size_t a = (size_t)v0;
+    CDM_TRY(fit_host_enqueue(p, v1 - v0, nmeas, meas + a * nmeas, params + a * kNP, CFP,
+                             FixP ? FixP + a * CDM_FIXP_TSIZE : nullptr, samples + a * kNP * ns,
+                             tau ? tau + a * ns : nullptr, pred ? pred + a * nmeas : nullptr,
+                             BIC ? BIC + a : nullptr, AIC ? AIC + a : nullptr, p->own_stream));
+  }
+  // wait for every piece; this context's counters become the pieces' sums
+  // (the statistics of this fit, as cdm_fit leaves them)
+  cdm_status first = CDM_OK;
+  std::string msg;
+  unsigned long long sum[4] = {0, 0, 0, 0};
+  for (int k = 0; k < npieces; k++) {
+    cdm_ctx* p = c->piece[k];
+    const cdm_status st = cdm_synchronize(p, p->own_stream, timeout_ms);
+    if (st != CDM_OK && first == CDM_OK) {
+      first = st;
+      msg = cdm_last_error();
+    }
+    unsigned long long h[4];
+    CDM_CUDA(cudaMemcpy(h, p->counters, sizeof(h), cudaMemcpyDeviceToHost));
+    CDM_CUDA(cudaMemset(p->counters, 0, sizeof(h)));
+    for (int i = 0; i < 4; i++) sum[i] += h[i];
+  }
+  CDM_TRY(ensure_base(c));
+  CDM_CUDA(cudaMemcpy(c->counters, sum, sizeof(sum), cudaMemcpyHostToDevice));
+  if (first != CDM_OK) return cdm_fail(first, msg);
+  return CDM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+cdm_status cdm_fit_host(cdm_ctx* c, int nvox, int nmeas, const double* meas, double* params,
+                        const double* CFP, const double* FixP, double* samples, double* tau,
+                        double* pred, double* BIC, double* AIC, int part_size, int64_t timeout_ms) {
+  CDM_TRY(check_common(c, nvox, nmeas, CDM_CFP_TSIZE, CDM_FIXP_TSIZE));
+  if (!meas || !params || !CFP || !samples || (CDM_FIXP_TSIZE > 0 && !FixP))
+    return cdm_fail(CDM_BAD_ARG, "null array");
+  (void)part_size;  // CUDIMOT's SIZE_PART parts (dMRI_Data.cu:66-79): see fit_host_pieces
+  const int npieces = fit_host_npieces(nvox);
+  if (npieces <= 1) {
+    if (!c->own_stream) CDM_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+    CDM_TRY(fit_host_enqueue(c, nvox, nmeas, meas, params, CFP, FixP, samples, tau, pred, BIC, AIC,
+                             c->own_stream));
+    return cdm_synchronize(c, c->own_stream, timeout_ms);
+  }
+  return fit_host_pieces(c, npieces, nvox, nmeas, meas, params, CFP, FixP, samples, tau, pred, BIC,
+                         AIC, timeout_ms);
 }
 
 }  // extern "C"

@@ -197,8 +197,13 @@ cdm_status cdm_fit(cdm_ctx* ctx, int nvox, int nmeas, const double* meas, double
 /* As cdm_fit, with HOST arrays: copies in, fits, copies out, and waits for
  * completion (at most timeout_ms, < 0 = no limit). The signals go through
  * cdm_clean_signals first when the cfg has rician, as CUDIMOT's data loader
- * does. part_size stands for CUDIMOT's SIZE_PART and is ignored: all voxels
- * are fitted as one part (they fit in HBM). */
+ * does. part_size stands for CUDIMOT's SIZE_PART and is ignored: the
+ * voxels are fitted as one part when fewer than 100,000, else as 2-4
+ * consecutive ranges in flight at once, each on a context and stream of its
+ * own (created on first use and kept by ctx), so that the copies of one
+ * range overlap the fits of the others; with first_voxel set per range and
+ * the lane counts of the whole call, every result equals one cdm_fit over
+ * all the voxels, and cdm_get_stats reports the call's sums. */
 cdm_status cdm_fit_host(cdm_ctx* ctx, int nvox, int nmeas, const double* meas,
                         double* params, const double* CFP, const double* FixP,
                         double* samples, double* tau, double* pred, double* BIC, double* AIC,

@@ -59,3 +59,33 @@ def test_first_voxel_changes_the_draws(built, cuda):
         torch.cuda.synchronize()
         out.append(s.cpu().numpy())
     assert not np.array_equal(out[0], out[1])
+
+
+def test_fit_host_pieces_equal_one_fit(built, cuda):
+    """cdm_fit_host on 150,001 voxels runs as 3 voxel ranges in flight at
+    once (each on a context and stream of its own, copies overlapping the
+    other ranges' fits); parameters, samples, BIC/AIC and the LM counters
+    equal those of cdm_fit over the whole volume on the device."""
+    from cudimot_gb300 import synth
+    wl = synth.ball_1_stick(150_001, seed=23)
+    cfg = capi.model_cfg("Ball_1_Stick", run_mcmc=1, nburn=20, njumps=40, sampleevery=10,
+                         bic_aic=1)
+    dev_lib = capi.Cudimot("Ball_1_Stick", cfg)
+    p = T(wl.init, cuda)
+    s = torch.zeros(wl.nvox, 5, 4, dtype=torch.float64, device=cuda)
+    bic = torch.zeros(wl.nvox, dtype=torch.float64, device=cuda)
+    aic = torch.zeros_like(bic)
+    dev_lib.fit(T(wl.meas, cuda), p, T(wl.cfp, cuda), T(wl.fixp, cuda), s, bic=bic, aic=aic)
+    torch.cuda.synchronize()
+    ref_stats = dev_lib.stats()
+    host_lib = capi.Cudimot("Ball_1_Stick", cfg)
+    hp = np.ascontiguousarray(wl.init.copy())
+    hs = np.zeros((wl.nvox, 5, 4))
+    hb, ha = np.zeros(wl.nvox), np.zeros(wl.nvox)
+    host_lib.fit_host(np.ascontiguousarray(wl.meas), hp, np.ascontiguousarray(wl.cfp),
+                      np.ascontiguousarray(wl.fixp), hs, None, None, hb, ha)
+    assert np.array_equal(hp, p.cpu().numpy())
+    assert np.array_equal(hs, s.cpu().numpy())
+    assert np.array_equal(hb, bic.cpu().numpy()) and np.array_equal(ha, aic.cpu().numpy())
+    st = host_lib.stats()
+    assert st.lm_iterations == ref_stats.lm_iterations and st.lm_successes == ref_stats.lm_successes
