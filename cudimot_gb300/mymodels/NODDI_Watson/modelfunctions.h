@@ -419,16 +419,19 @@ __device__ __forceinline__ float2 Predicted_Signal_Pair(const fp32* P, const flo
 // q_j(y), alpha_0 = a_0(b), alpha_j = a_j(b) P[9+j] (the Legendre-Gaussian
 // columns of the shell times the Watson coefficients). Written in the
 // Chebyshev basis of t = 2y - 1 (q_j(y) = sum_k WATSON_CHEB[j][k] T_k(t),
-// entries <= 1.41, so single precision keeps ~1e-7 of S0), with the
-// compartment weights and the isotropic term folded into its
-// coefficients, the pair evaluation is Clenshaw's recurrence at two
-// operations per degree. Shell_Coeffs forms the coefficients once per
-// shell and parameter set from the shell's protocol row (columns: gx, gy,
-// gz, b, exp(-b Diso), a_0..a_6):
+// entries <= 1.41, so single precision keeps ~1e-7 of S0) and then, per
+// shell, in powers of t (T_k's integer coefficients, at most 48): the pair
+// evaluation is Horner's rule, one fused multiply-add per degree on a
+// chain of six. In FP32 this is as accurate as Clenshaw's recurrence on the
+// Chebyshev coefficients for these functions (emulated over kappa 0.5-64
+// and b 1000-3000: both within 2.1e-7 of the largest intra value; the
+// power-basis coefficients add up to no more than that value, so nothing
+// cancels). The compartment weights and the isotropic term are folded into
+// the coefficients. Shell_Coeffs forms them once per shell and parameter
+// set from the shell's protocol row (columns: gx, gy, gz, b, exp(-b Diso),
+// a_0..a_6):
 //   coef[0..1]  exponent of the extra-cellular term as c0 + c1 x^2, base 2
-//   coef[2..8]  Clenshaw inputs h6, h5, h4 - h6, h3, h2, h1, h0* of
-//               k2 intra + k3 exp(-b Diso) (h_k = half the Chebyshev
-//               coefficient, h0* the whole one)
+//   coef[2..8]  k2 intra + k3 exp(-b Diso) = sum_i p_i t^i, as p_6 .. p_0
 //   coef[9..10] intra < 0 (the truncated series) becomes 0.5e-3 as in
 //               Predicted_Signal: below coef[9] the sum is replaced by coef[10]
 //   coef[11]    k1, the extra-cellular weight
@@ -471,15 +474,16 @@ __device__ __forceinline__ void Shell_Coeffs(const fp32* P, const float* row, co
     for (int j = k; j < 7; j++) acc = fmaf(al[j], WATSON_CHEB[j][k], acc);
     e[k] = acc;
   }
-  const float kh = 0.5f * k2, iso = k3 * row[4];
-  const float h6 = kh * e[6];
-  coef[2] = h6;
-  coef[3] = kh * e[5];
-  coef[4] = fmaf(kh, e[4], -h6);
-  coef[5] = kh * e[3];
-  coef[6] = kh * e[2];
-  coef[7] = kh * e[1];
-  coef[8] = fmaf(k2, e[0], iso);
+  // powers of t: T_0..T_6 = 1, t, 2t^2-1, 4t^3-3t, 8t^4-8t^2+1,
+  // 16t^5-20t^3+5t, 32t^6-48t^4+18t^2-1
+  const float iso = k3 * row[4];
+  coef[2] = k2 * (32.0f * e[6]);
+  coef[3] = k2 * (16.0f * e[5]);
+  coef[4] = k2 * fmaf(-48.0f, e[6], 8.0f * e[4]);
+  coef[5] = k2 * fmaf(-20.0f, e[5], 4.0f * e[3]);
+  coef[6] = k2 * fmaf(18.0f, e[6], fmaf(-8.0f, e[4], 2.0f * e[2]));
+  coef[7] = k2 * fmaf(5.0f, e[5], fmaf(-3.0f, e[3], e[1]));
+  coef[8] = fmaf(k2, (e[0] - e[2]) + (e[4] - e[6]), iso);
   coef[9] = iso;
   coef[10] = fmaf(k2, 0.5e-3f, iso);
   coef[11] = k1;
@@ -495,18 +499,14 @@ __device__ __forceinline__ float2 Predicted_Signal_Shell_Pair(const fp32* P, con
   const float2 x2 = __fmul2_rn(xv, xv);
   const float2 z = __ffma2_rn(watson_bc(coef[1]), x2, watson_bc(coef[0]));
   const float2 extra = make_float2(watson_ex2(z.x), watson_ex2(z.y));
-  // u = 2t = 4y - 2 at the cosine clamped to [-1, 1]
-  float2 u = __ffma2_rn(watson_bc(4.0f), x2, watson_bc(-2.0f));
-  u.x = fminf(u.x, 2.0f);
-  u.y = fminf(u.y, 2.0f);
-  const float2 b6 = watson_bc(coef[2]);
-  const float2 b5 = __ffma2_rn(u, b6, watson_bc(coef[3]));
-  const float2 b4 = __ffma2_rn(u, b5, watson_bc(coef[4]));
-  const float2 b3 = __ffma2_rn(u, b4, __fadd2_rn(watson_bc(coef[5]), make_float2(-b5.x, -b5.y)));
-  const float2 b2 = __ffma2_rn(u, b3, __fadd2_rn(watson_bc(coef[6]), make_float2(-b4.x, -b4.y)));
-  const float2 b1 = __ffma2_rn(u, b2, __fadd2_rn(watson_bc(coef[7]), make_float2(-b3.x, -b3.y)));
-  const float2 b0 = __ffma2_rn(u, b1, __fadd2_rn(watson_bc(coef[8]), make_float2(-b2.x, -b2.y)));
-  float2 f = __fadd2_rn(b0, make_float2(-b2.x, -b2.y));
+  // t = 2y - 1 (a cosine rounded past 1 moves t by an ulp: harmless here)
+  const float2 t = __ffma2_rn(watson_bc(2.0f), x2, watson_bc(-1.0f));
+  float2 f = __ffma2_rn(watson_bc(coef[2]), t, watson_bc(coef[3]));
+  f = __ffma2_rn(f, t, watson_bc(coef[4]));
+  f = __ffma2_rn(f, t, watson_bc(coef[5]));
+  f = __ffma2_rn(f, t, watson_bc(coef[6]));
+  f = __ffma2_rn(f, t, watson_bc(coef[7]));
+  f = __ffma2_rn(f, t, watson_bc(coef[8]));
   if (f.x < coef[9]) f.x = coef[10];
   if (f.y < coef[9]) f.y = coef[10];
   return __ffma2_rn(watson_bc(coef[11]), extra, f);

@@ -12,7 +12,11 @@
  * launch of a persistent kernel: each CTA takes the next tile (CDM_NT
  * threads' worth of voxels of one fit) from a device counter, stages that
  * fit's protocol and runs that model's MCMC chain code on it, until no tile
- * is left. Samples are bit for bit those of cdm_mcmc on the same context.
+ * is left. Its chains are those of cdm_mcmc on the same context (the same
+ * code on the same counter-based draws); the chain code is compiled apart
+ * from the model library, so a chain can part from its library twin where
+ * the two compilations round an operation differently and a borderline
+ * accept/reject goes the other way (under 1 % of voxels in the tests).
  */
 #ifndef CDM_HETERO_H
 #define CDM_HETERO_H
