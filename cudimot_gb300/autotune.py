@@ -141,12 +141,14 @@ def lanes_kwargs(choice):
 # times MCMC and grid search of each on a sample of the caller's data, and
 # caches the fastest per GPU, model and shape like `tune`.
 VARIANTS = {
-    "nt128_u2_b4": [],  # the default build
-    "nt64_u2_b8": ["-DCDM_NT=64", "-DCDM_MCMC_MIN_BLOCKS=8"],
-    "nt256_u2_b2": ["-DCDM_NT=256", "-DCDM_MCMC_MIN_BLOCKS=2"],
-    "nt128_u1_b4": ["-DCDM_PAIR_UNROLL=1"],
-    "nt128_u4_b4": ["-DCDM_PAIR_UNROLL=4"],
-    "nt128_u2_b3": ["-DCDM_MCMC_MIN_BLOCKS=3"],
+    "default": [],  # 128 threads, 4 CTAs/SM, the plugin's default unroll
+    "nt64_b8": ["-DCDM_NT=64", "-DCDM_MCMC_MIN_BLOCKS=8"],
+    "nt256_b2": ["-DCDM_NT=256", "-DCDM_MCMC_MIN_BLOCKS=2"],
+    "u1": ["-DCDM_PAIR_UNROLL=1"],
+    "u2": ["-DCDM_PAIR_UNROLL=2"],
+    "u3": ["-DCDM_PAIR_UNROLL=3"],
+    "u4": ["-DCDM_PAIR_UNROLL=4"],
+    "b3": ["-DCDM_MCMC_MIN_BLOCKS=3"],
 }
 
 

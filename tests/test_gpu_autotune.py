@@ -48,7 +48,7 @@ def test_autotune_build_variants(built, cuda, tmp_path, monkeypatch):
     monkeypatch.setattr(autotune, "CACHE_DIR", str(tmp_path))
     wl = b1s(20000, seed=13)
     m, p, c, f = T(wl.meas, cuda), T(wl.init, cuda), T(wl.cfp, cuda), T(wl.fixp, cuda)
-    tags = ["nt128_u2_b4", "nt64_u2_b8"]
+    tags = ["default", "nt64_b8"]
     got = autotune.tune_build("Ball_1_Stick", m, p, c, f, variants=tags, sample=8192, reps=1,
                               mcmc_iters=20)
     assert got["variant"] in tags and set(got["ms"]) == set(tags)
