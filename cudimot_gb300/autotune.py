@@ -144,10 +144,10 @@ VARIANTS = {
     "default": [],  # 128 threads, 4 CTAs/SM, the plugin's default unroll
     "nt64_b8": ["-DCDM_NT=64", "-DCDM_MCMC_MIN_BLOCKS=8"],
     "nt256_b2": ["-DCDM_NT=256", "-DCDM_MCMC_MIN_BLOCKS=2"],
-    "u1": ["-DCDM_PAIR_UNROLL=1"],
-    "u2": ["-DCDM_PAIR_UNROLL=2"],
-    "u3": ["-DCDM_PAIR_UNROLL=3"],
-    "u4": ["-DCDM_PAIR_UNROLL=4"],
+    "u1": ["-DCDM_PAIR_UNROLL=1", "-DCDM_SHELL_UNROLL=1"],
+    "u2": ["-DCDM_PAIR_UNROLL=2", "-DCDM_SHELL_UNROLL=2"],
+    "u3": ["-DCDM_PAIR_UNROLL=3", "-DCDM_SHELL_UNROLL=3"],
+    "u4": ["-DCDM_PAIR_UNROLL=4", "-DCDM_SHELL_UNROLL=4"],
     "b3": ["-DCDM_MCMC_MIN_BLOCKS=3"],
 }
 

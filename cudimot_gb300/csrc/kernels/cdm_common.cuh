@@ -34,18 +34,18 @@
 
 constexpr int kSseUnroll = CDM_SSE_UNROLL;
 // Unroll of the paired (two-measurement) cost loops: how many pairs' signal
-// loads are in flight per lane. With the per-shell series a pair is short
+// loads are in flight per lane. In the per-shell series a pair is short
 // (one multiply-add per degree) and the loads from L2 become the wait:
-// 4 pairs (NODDI-Watson, grid search + MCMC: 115 ms against 124 ms at 2);
-// 2 otherwise.
+// 4 pairs there (NODDI-Watson, grid search + MCMC: 115 ms against 124 ms at
+// 2); 2 in the per-measurement loop.
 #ifndef CDM_PAIR_UNROLL
-#if CDM_SHELLS
-#define CDM_PAIR_UNROLL 4
-#else
 #define CDM_PAIR_UNROLL 2
 #endif
+#ifndef CDM_SHELL_UNROLL
+#define CDM_SHELL_UNROLL 4
 #endif
 constexpr int kPairUnroll = CDM_PAIR_UNROLL;
+constexpr int kShellUnroll = CDM_SHELL_UNROLL;
 
 // Number type the plugin is evaluated in: fp32 (fp32.h), or double with
 // CDM_EVAL_DOUBLE for plugins whose closed forms need it (CUDIMOT's
@@ -291,7 +291,7 @@ __device__ __forceinline__ double cdm_group_sse_shells(const cdm_voxel_io& io, c
     Shell_Coeffs(P, sproto + (size_t)hdr[4 + 3 * s] * kNCOLS4, FixP, coef);
     const int npairs = hdr[5 + 3 * s];
     const float4* q = reinterpret_cast<const float4*>(io.stab) + (size_t)hdr[6 + 3 * s] * Gw * 2;
-#pragma unroll kPairUnroll
+#pragma unroll kShellUnroll
     for (int j = 0; j < npairs; j++) {
       const float4 c01 = q[0], c2w = q[1];
       const float2 g[3] = {make_float2(c01.x, c01.y), make_float2(c01.z, c01.w),

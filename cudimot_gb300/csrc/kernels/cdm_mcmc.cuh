@@ -79,26 +79,31 @@ __device__ __forceinline__ void cdm_set(Tv* a, int i, Tv x) {
   for (int k = 0; k < kNP; k++) a[k] = (k == i) ? x : a[k];
 }
 
-template <int Gw, bool RICIAN>
-__device__ __forceinline__ double cdm_likelihood(const cdm_voxel_io& io, const float* sproto,
-                                                 cdm_real* P, cdm_real* FixP, float tau, unsigned gmask) {
-  // The energies are written with explicitly rounded operations: whether a
-  // multiply and an add are fused is then fixed by the source, not by the
-  // compiler's view of the surrounding code, so the chain is the same in
-  // every kernel this code is compiled into (model library, multi-model
-  // kernel).
-  if (RICIAN) {
-    const double s = cdm_group_rician<Gw>(io, sproto, P, FixP, tau, gmask);
-    return __fma_rn(-(double)io.nmeas, (double)logf(tau), -s);
-  }
-  // (n/2) log(SSE/2) with SSE kept in FP64: log(m 2^e) = log m + e log 2,
-  // the mantissa's log in FP32 (absolute error ~6e-8 for m in [0.5, 1))
-  // and the rest exact, instead of the FP32 log of a value of ~1e6 (1e-6)
-  const double sse = cdm_group_sse<Gw>(io, sproto, P, FixP, gmask);
-  int ex;
-  const double m = frexp(0.5 * sse, &ex);
-  const double l = __fma_rn((double)ex, 0.69314718055994531, (double)logf((float)m));
-  return __dmul_rn(0.5 * (double)io.nmeas, l);
+// Rician energy of the current state: -n log(tau) - sum log-likelihood
+// terms (FP64 group sum). Written with explicitly rounded operations, so
+// that whether a multiply and an add are fused is fixed by the source, not
+// by the compiler's view of the surrounding code: the chain is the same in
+// every kernel this code is compiled into (model library, multi-model
+// kernel).
+template <int Gw>
+__device__ __forceinline__ double cdm_rician_energy(const cdm_voxel_io& io, const float* sproto,
+                                                    cdm_real* P, cdm_real* FixP, float tau,
+                                                    unsigned gmask) {
+  const double s = cdm_group_rician<Gw>(io, sproto, P, FixP, tau, gmask);
+  return __fma_rn(-(double)io.nmeas, (double)logf(tau), -s);
+}
+
+// Gaussian energy difference of a proposal. The energy is prior +
+// (n/2) log(SSE/2) (MCMC.cu:206-219); the acceptance needs only
+// E_old - E_new = (prior_old - prior_new) + (n/2) log(SSE_old / SSE_new).
+// The SSE sums are FP64 (group sum); their ratio is near 1 and is taken,
+// with its logarithm, in FP32: the difference is then good to about
+// n/2 x 2e-7 (3e-5 for 288 measurements) with no FP64 operation beyond the
+// sum, where the absolute energies (~1e3) would need FP64 logarithms.
+__device__ __forceinline__ float cdm_gauss_delta(double sse_old, double sse_new, float tp_old,
+                                                 float tp_new, float halfn) {
+  const float r = __fdividef((float)sse_old, (float)sse_new);
+  return __fmaf_rn(halfn, logf(r), __fsub_rn(tp_old, tp_new));
 }
 
 // Records sample s of a sample row (element index row0 + s of dst, a row
@@ -181,7 +186,10 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
   // CUDIMOT (MCMC.cu custom_priors); the copy is built by the CTA below
   cdm_real* cf0 = a.cfp_all_off >= 0 ? reinterpret_cast<cdm_real*>(sproto + a.cfp_all_off) : nullptr;
 
-  double energy = 0.0;
+  double energy = 0.0;  // Rician: the current energy
+  double sse_c = 1.0;   // Gaussian: the current SSE and prior total
+  float tp_c = 0.0f;
+  const float halfn = 0.5f * (float)a.nmeas;
   bool stale = false;  // derived values of P out of date (after a rejection)
   for (int phase = 0; phase < 2; phase++) {
     const bool recording = phase == 1;
@@ -232,11 +240,16 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
       tau = (float)((double)io.nmeas / cdm_group_sum<Gw>((double)s2, gm));
       tauSD = tau * 0.5f;
     }
-    energy = __dadd_rn((double)total_prior, cdm_likelihood<Gw, RICIAN>(io, sproto, P, FixP, tau, gm));
+    if constexpr (RICIAN) {
+      energy = __dadd_rn((double)total_prior, cdm_rician_energy<Gw>(io, sproto, P, FixP, tau, gm));
+    } else {
+      sse_c = cdm_group_sse<Gw>(io, sproto, P, FixP, gm);
+      tp_c = total_prior;
+    }
 
     for (int it = 0; it < niters; it++) {
       const uint32_t git = (uint32_t)(recording ? nburn + it : it);
-      if (RICIAN) {
+      if constexpr (RICIAN) {
         const cdm_draw d = cdm_mcmc_draw(a.seed, vid, git, CDM_RNG_SLOT_TAU, a.stream);
         const float old = tau;
         tau = __fmaf_rn(d.normal, tauSD, tau);
@@ -246,7 +259,7 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
           float tp = 0.0f;
 #pragma unroll
           for (int p = 0; p < kNP; p++) tp += prior[p];
-          const double ne = __dadd_rn((double)tp, cdm_likelihood<Gw, RICIAN>(io, sproto, P, FixP, tau, gm));
+          const double ne = __dadd_rn((double)tp, cdm_rician_energy<Gw>(io, sproto, P, FixP, tau, gm));
           if (expf((float)__dsub_rn(energy, ne)) > d.uniform) {
             tacc++;
             energy = ne;
@@ -278,11 +291,21 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
           float tp = 0.0f;
 #pragma unroll
           for (int q = 0; q < kNP; q++) tp += (q == p) ? np_ : prior[q];
-          const double ne = __dadd_rn((double)tp, cdm_likelihood<Gw, RICIAN>(io, sproto, P, FixP, tau, gm));
-          if (expf((float)__dsub_rn(energy, ne)) > d.uniform) {
-            accepted = true;
-            energy = ne;
-            cdm_set(prior, p, np_);
+          if constexpr (RICIAN) {
+            const double ne = __dadd_rn((double)tp, cdm_rician_energy<Gw>(io, sproto, P, FixP, tau, gm));
+            if (expf((float)__dsub_rn(energy, ne)) > d.uniform) {
+              accepted = true;
+              energy = ne;
+              cdm_set(prior, p, np_);
+            }
+          } else {
+            const double sse_n = cdm_group_sse<Gw>(io, sproto, P, FixP, gm);
+            if (expf(cdm_gauss_delta(sse_c, sse_n, tp_c, tp, halfn)) > d.uniform) {
+              accepted = true;
+              sse_c = sse_n;
+              tp_c = tp;
+              cdm_set(prior, p, np_);
+            }
           }
         }
         if (accepted) {
