@@ -205,6 +205,8 @@ struct cdm_voxel_io {
   const float* pairs;  // this lane's first pair-table entry (paired hook only)
   const int* shells;   // shell-table header in shared memory, or null (per-measurement path)
   const float* stab;   // this lane's first shell pair entry
+  const float2* sig2;  // shell order: this lane's first pair of signals (pair-interleaved,
+                       // one 8-byte load per pair; pairs chunk_stride float2 apart)
 };
 
 // Build the pair table (see the layout notes above) after the staged
@@ -285,7 +287,7 @@ __device__ __forceinline__ double cdm_group_sse_shells(const cdm_voxel_io& io, c
   const int* hdr = io.shells;
   const int nshell = hdr[1];
   float2 acc2 = make_float2(0.0f, 0.0f);
-  const float* sig = io.sig;
+  const float2* sig = io.sig2;
   for (int s = 0; s < nshell; s++) {
     float coef[CDM_SHELL_NCOEF];
     Shell_Coeffs(P, sproto + (size_t)hdr[4 + 3 * s] * kNCOLS4, FixP, coef);
@@ -297,11 +299,11 @@ __device__ __forceinline__ double cdm_group_sse_shells(const cdm_voxel_io& io, c
       const float2 g[3] = {make_float2(c01.x, c01.y), make_float2(c01.z, c01.w),
                            make_float2(c2w.x, c2w.y)};
       const float2 s2 = Predicted_Signal_Shell_Pair(P, coef, g);
-      const float2 r = __ffma2_rn(make_float2(c2w.z, c2w.w), s2,
-                                  make_float2(-sig[0], -sig[io.chunk_stride]));
+      const float2 y = *sig;
+      const float2 r = __ffma2_rn(make_float2(c2w.z, c2w.w), s2, make_float2(-y.x, -y.y));
       acc2 = __ffma2_rn(r, r, acc2);
       q += 2 * Gw;
-      sig += 2 * io.chunk_stride;
+      sig += io.chunk_stride;
     }
   }
   return cdm_group_sum<Gw>((double)(acc2.x + acc2.y), gmask);

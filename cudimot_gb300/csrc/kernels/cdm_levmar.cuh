@@ -178,6 +178,7 @@ CDM_KERNEL(CDM_NT) cdm_levmar_kernel(CDM_KARG(cdm_lm_args) a) {
   io.pairs = ptab + (size_t)lane * kNCOLSP * 2;
   io.shells = nullptr;
   io.stab = nullptr;
+  io.sig2 = nullptr;
 
   cdm_real P[kNPS], FixP[kNFIX];
   float Pt[kNP];

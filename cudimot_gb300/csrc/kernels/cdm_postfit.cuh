@@ -299,17 +299,35 @@ CDM_KERNEL0 cdm_prep_shells_kernel(const double* __restrict__ cfp, int nmeas, in
   }
 }
 
-// Signals in the shell order of the table ([npos / Gw][nvox][Gw], 0 on
-// padding), or in measurement order as cdm_pack_signals_kernel when the
-// table is invalid.
+// Signals in the shell order of the table, pair-interleaved
+// ([npos / (2 Gw)][nvox][Gw][2]: a lane's positions of chunks 2k and 2k + 1
+// side by side, 0 on padding), or in measurement order as
+// cdm_pack_signals_kernel ([nchunk][nvox][Gw]) when the table is invalid.
 template <int Gw>
 CDM_KERNEL0 cdm_pack_shell_signals_kernel(const double* __restrict__ meas, int nvox, int nmeas,
                                           int nchunk, const float* __restrict__ table,
                                           const int* __restrict__ perm, float* __restrict__ out) {
   const int* hdr = reinterpret_cast<const int*>(table);
   const bool shells = hdr[0] != 0;
-  const int nc = shells ? hdr[2] / Gw : nchunk;
-  const size_t total = (size_t)nc * nvox * Gw;
+  if (shells) {
+    // pair-interleaved: element (pair k, voxel v, lane j) holds the lane's
+    // positions of chunks 2k and 2k + 1, one 8-byte load for the kernels
+    const int npairs = hdr[2] / (2 * Gw);
+    const size_t total = (size_t)npairs * nvox * Gw;
+    float2* out2 = reinterpret_cast<float2*>(out);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (size_t)gridDim.x * blockDim.x) {
+      const int j = (int)(i % Gw);
+      const size_t rest = i / Gw;
+      const int v = (int)(rest % nvox);
+      const int k = (int)(rest / nvox);
+      const int m0 = perm[(2 * k) * Gw + j], m1 = perm[(2 * k + 1) * Gw + j];
+      const double* row = meas + (size_t)v * nmeas;
+      out2[i] = make_float2(m0 >= 0 ? (float)row[m0] : 0.0f, m1 >= 0 ? (float)row[m1] : 0.0f);
+    }
+    return;
+  }
+  const size_t total = (size_t)nchunk * nvox * Gw;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     const int j = (int)(i % Gw);
@@ -317,8 +335,7 @@ CDM_KERNEL0 cdm_pack_shell_signals_kernel(const double* __restrict__ meas, int n
     const int v = (int)(rest % nvox);
     const int c = (int)(rest / nvox);
     const int p = c * Gw + j;
-    const int m = shells ? perm[p] : (p < nmeas ? p : -1);
-    out[i] = m >= 0 ? (float)meas[(size_t)v * nmeas + m] : 0.0f;
+    out[i] = p < nmeas ? (float)meas[(size_t)v * nmeas + p] : 0.0f;
   }
 }
 #endif
