@@ -444,8 +444,11 @@ cdm_status prep_protocol(cdm_ctx* c, int nmeas, const double* CFP, cudaStream_t 
 constexpr bool kShells = CDM_SHELLS != 0;
 
 size_t shell_sig_floats(int nvox, int nmeas, int Gw) {
-  const int nc = (cdm_shell_max_pos(nmeas, Gw) + Gw - 1) / Gw;
-  return (size_t)std::max(nc, (nmeas + Gw - 1) / Gw) * std::max(nvox, 1) * Gw;
+  // the tile-major shell layout (whole tiles of CDM_NT / Gw voxels), or
+  // the chunk-major layout when the table turns out invalid
+  const size_t tiles = ((size_t)std::max(nvox, 1) + CDM_NT / Gw - 1) / (CDM_NT / Gw);
+  return std::max(tiles * cdm_shell_sig_rows(nmeas, Gw) * 2 * CDM_NT,
+                  (size_t)((nmeas + Gw - 1) / Gw) * std::max(nvox, 1) * Gw);
 }
 
 cdm_status prep_shells_and_pack(cdm_ctx* c, int Gw, int nvox, int nmeas, const double* CFP,

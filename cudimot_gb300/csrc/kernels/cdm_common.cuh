@@ -206,7 +206,7 @@ struct cdm_voxel_io {
   const int* shells;   // shell-table header in shared memory, or null (per-measurement path)
   const float* stab;   // this lane's first shell pair entry
   const float2* sig2;  // shell order: this lane's first pair of signals (pair-interleaved,
-                       // one 8-byte load per pair; pairs chunk_stride float2 apart)
+                       // tile-major: cdm_shell_sig_index; pairs CDM_NT float2 apart)
 };
 
 // Build the pair table (see the layout notes above) after the staged
@@ -303,7 +303,7 @@ __device__ __forceinline__ double cdm_group_sse_shells(const cdm_voxel_io& io, c
       const float2 r = __ffma2_rn(make_float2(c2w.z, c2w.w), s2, make_float2(-y.x, -y.y));
       acc2 = __ffma2_rn(r, r, acc2);
       q += 2 * Gw;
-      sig += io.chunk_stride;
+      sig += CDM_NT;
     }
   }
   return cdm_group_sum<Gw>((double)(acc2.x + acc2.y), gmask);

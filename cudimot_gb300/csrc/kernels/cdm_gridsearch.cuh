@@ -49,7 +49,9 @@ CDM_KERNEL(CDM_NT) cdm_gridsearch_kernel(CDM_KARG(cdm_gs_args) a) {
 
   cdm_voxel_io io;
   io.sig = a.sig + (size_t)v * Gw + lane;
-  io.sig2 = reinterpret_cast<const float2*>(a.sig) + (size_t)v * Gw + lane;
+  io.sig2 = shdr ? reinterpret_cast<const float2*>(a.sig) +
+                       cdm_shell_sig_index(v, 0, lane, shdr[2] / (2 * Gw), Gw)
+                 : nullptr;
   io.chunk_stride = (size_t)a.nvox * Gw;
   io.nchunk = a.nchunk;
   io.nmeas = a.nmeas;

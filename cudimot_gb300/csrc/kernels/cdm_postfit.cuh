@@ -310,8 +310,8 @@ CDM_KERNEL0 cdm_pack_shell_signals_kernel(const double* __restrict__ meas, int n
   const int* hdr = reinterpret_cast<const int*>(table);
   const bool shells = hdr[0] != 0;
   if (shells) {
-    // pair-interleaved: element (pair k, voxel v, lane j) holds the lane's
-    // positions of chunks 2k and 2k + 1, one 8-byte load for the kernels
+    // pair-interleaved, tile-major (cdm_shell_sig_index): element (pair k,
+    // voxel v, lane j) holds the lane's positions of chunks 2k and 2k + 1
     const int npairs = hdr[2] / (2 * Gw);
     const size_t total = (size_t)npairs * nvox * Gw;
     float2* out2 = reinterpret_cast<float2*>(out);
@@ -323,7 +323,7 @@ CDM_KERNEL0 cdm_pack_shell_signals_kernel(const double* __restrict__ meas, int n
       const int k = (int)(rest / nvox);
       const int m0 = perm[(2 * k) * Gw + j], m1 = perm[(2 * k + 1) * Gw + j];
       const double* row = meas + (size_t)v * nmeas;
-      out2[i] = make_float2(m0 >= 0 ? (float)row[m0] : 0.0f, m1 >= 0 ? (float)row[m1] : 0.0f);
+      out2[cdm_shell_sig_index(v, k, j, npairs, Gw)] = make_float2(m0 >= 0 ? (float)row[m0] : 0.0f, m1 >= 0 ? (float)row[m1] : 0.0f);
     }
     return;
   }
