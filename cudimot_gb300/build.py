@@ -207,14 +207,16 @@ def describe(flops_lib, sizes, name, eval_type=None, extra=((), ())):
     return txt
 
 
-def split_device(model_dir, outdir, name=None, eval_type=None, force=False):
+def split_device(model_dir, outdir, name=None, eval_type=None, force=False, lineinfo=True):
     """Device half of a split build: outdir/cdm_module.cubin and
-    outdir/cdm_model_desc.h from the plugin in model_dir."""
+    outdir/cdm_model_desc.h from the plugin in model_dir. lineinfo=False
+    leaves out the source-line tables (a third of the size)."""
     model_dir = os.path.abspath(model_dir)
     outdir = os.path.abspath(outdir)
     name = name or os.path.basename(model_dir.rstrip("/"))
     os.makedirs(outdir, exist_ok=True)
-    flags = ["-O3", "-std=c++17", ARCH, "-lineinfo", "-cubin"] + eval_flags(eval_type)
+    flags = ["-O3", "-std=c++17", ARCH] + (["-lineinfo"] if lineinfo else []) + ["-cubin"] + \
+        eval_flags(eval_type)
     cubin = os.path.join(outdir, "cdm_module.cubin")
     stamp = cubin + ".sha256"
     dig = digest(model_dir, flags + [name])

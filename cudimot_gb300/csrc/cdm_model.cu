@@ -338,6 +338,10 @@ struct cdm_ctx {
   // scratch (owned)
   double* grid_dev = nullptr;
   size_t grid_cap = 0;
+  float* grid32 = nullptr;     // the grid rounded to float, as the kernel evaluates it
+  size_t grid32_cap = 0;
+  uint32_t* grid_ok = nullptr; // bit c: combination c's grid values are within the bounds
+  size_t grid_ok_cap = 0;
   float* proto32 = nullptr;
   size_t proto32_cap = 0;
   double* proto64 = nullptr;
@@ -530,7 +534,9 @@ cdm_status launch_gs(cdm_ctx* c, int Gw, int nvox, int nmeas, double* params, co
   fill_common(c, a, nvox, nmeas, Gw);
   a.params = params;
   a.fixp = FixP;
-  a.grid = c->grid_dev;
+  a.grid = c->grid32;
+  a.grid64 = c->grid_dev;
+  a.grid_ok = c->grid_ok;
   a.ngp = c->cfg.n_grid_params;
   a.combs = c->cfg.grid_combs;
   for (int p = 0; p < kNP; p++) a.gpos[p] = c->gpos[p];
@@ -855,10 +861,31 @@ cdm_status cdm_create(const cdm_model_cfg* cfg, cdm_ctx** out) {
   }
   cdm_status s = ensure_base(c);
   if (s == CDM_OK && !c->grid_host.empty()) {
+    // the grid as the FP32 ranking pass reads it: each value rounded to
+    // float, and per combination whether its grid values pass the bounds
+    // test (the same double-against-float-bound comparisons as the FP64
+    // re-check, so both passes skip the same combinations)
+    const int ngp = cfg->n_grid_params, combs = cfg->grid_combs;
+    std::vector<float> g32(c->grid_host.size());
+    std::vector<uint32_t> ok(((size_t)combs + 31) / 32, 0u);
+    for (size_t i = 0; i < g32.size(); i++) g32[i] = (float)c->grid_host[i];
+    for (int k = 0; k < combs; k++) {
+      bool in = true;
+      for (int p = 0; p < kNP; p++)
+        if (c->gpos[p] >= 0)
+          in = in && cdm_in_bounds1(c->lim, p, c->grid_host[(size_t)k * ngp + c->gpos[p]]);
+      if (in) ok[k / 32] |= 1u << (k % 32);
+    }
     s = dev_alloc(&c->grid_dev, &c->grid_cap, c->grid_host.size());
+    if (s == CDM_OK) s = dev_alloc(&c->grid32, &c->grid32_cap, g32.size());
+    if (s == CDM_OK) s = dev_alloc(&c->grid_ok, &c->grid_ok_cap, ok.size());
     if (s == CDM_OK) {
       e = cudaMemcpy(c->grid_dev, c->grid_host.data(), c->grid_host.size() * sizeof(double),
                      cudaMemcpyHostToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(c->grid32, g32.data(), g32.size() * sizeof(float), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(c->grid_ok, ok.data(), ok.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
       if (e != cudaSuccess) s = cdm_fail(CDM_CUDA_ERROR, cudaGetErrorString(e));
     }
   }
@@ -874,7 +901,7 @@ cdm_status cdm_destroy(cdm_ctx* c) {
   if (!c) return CDM_OK;
   for (cdm_ctx* p : c->piece) cdm_destroy(p);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  void* bufs[] = {c->grid_dev, c->proto32, c->proto64, c->sig, c->gs_flags, c->gs_cand,
+  void* bufs[] = {c->grid_dev, c->grid32, c->grid_ok, c->proto32, c->proto64, c->sig, c->gs_flags, c->gs_cand,
                   c->gs_best, c->shell_perm, c->shell_rank, c->err, c->counters, c->h_meas, c->h_params, c->h_cfp, c->h_fixp,
                   c->h_samples, c->h_tau, c->h_pred, c->h_bic, c->h_aic};
   for (void* b : bufs)

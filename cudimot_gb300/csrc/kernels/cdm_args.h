@@ -102,6 +102,16 @@ struct cdm_limits {
   int fixed[kNP];
 };
 
+// One parameter value against its bounds, in double against the float
+// bounds, as grid search tests a combination (btype: CUDIMOT's enum bound,
+// 0 none, 1 min, 2 max, 3 both).
+__host__ __device__ inline bool cdm_in_bounds1(const cdm_limits& lim, int p, double x) {
+  const int t = lim.btype[p];
+  if ((t == 1 || t == 3) && x < (double)lim.bmin[p]) return false;
+  if ((t == 2 || t == 3) && x > (double)lim.bmax[p]) return false;
+  return true;
+}
+
 struct cdm_gs_args {
   int nvox, nmeas, nmeas_pad, nchunk, fixp_tsize;
   uint32_t proto_bytes;
@@ -109,7 +119,9 @@ struct cdm_gs_args {
   const float* sig;
   double* params;
   const double* fixp;
-  const double* grid;  // [combs][ngp]
+  const float* grid;   // [combs][ngp], rounded to float
+  const double* grid64;  // [combs][ngp], the winner's values are written from here
+  const uint32_t* grid_ok;  // bit c: combination c's grid values pass the bounds test
   int ngp;
   int combs;
   int gpos[kNP];       // column of parameter p in the grid, or -1
@@ -118,8 +130,8 @@ struct cdm_gs_args {
   int* flags;          // [nvox]: 0 decided, 1 recheck candidates, 2 recheck all
   int* cand;           // [nvox][kGsTop]
   int* best;           // [nvox] winning combination (or -1)
-  double* cost_out;    // [nvox] the winner's cost (FP32 terms, FP64 sum), or null
-  int cost_only;       // evaluate the cost at the voxel's own parameters (combs 1, no grid)
+  double* cost_out;    // cost_only: [nvox] the cost (FP32 terms, FP64 sum)
+  int cost_only;       // evaluate the cost at the voxel's own parameters (no grid)
   int* err;
   cdm_limits lim;
 };

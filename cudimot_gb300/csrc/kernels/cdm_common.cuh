@@ -280,10 +280,9 @@ static_assert(CDM_SHELL_MCOLS == 3, "shell pair entries hold three protocol colu
 // protocol row), then the lane's pairs of that shell are evaluated
 // (Predicted_Signal_Shell_Pair); padding positions have weight 0 and
 // signal 0, so r = w S - y vanishes there.
-template <int Gw>
-__device__ __forceinline__ double cdm_group_sse_shells(const cdm_voxel_io& io, const float* sproto,
-                                                       cdm_real* P, cdm_real* FixP,
-                                                       unsigned gmask) {
+template <int Gw, typename Ts>
+__device__ __forceinline__ Ts cdm_group_sse_shells(const cdm_voxel_io& io, const float* sproto,
+                                                   cdm_real* P, cdm_real* FixP, unsigned gmask) {
   const int* hdr = io.shells;
   const int nshell = hdr[1];
   float2 acc2 = make_float2(0.0f, 0.0f);
@@ -306,15 +305,18 @@ __device__ __forceinline__ double cdm_group_sse_shells(const cdm_voxel_io& io, c
       sig += CDM_NT;
     }
   }
-  return cdm_group_sum<Gw>((double)(acc2.x + acc2.y), gmask);
+  return cdm_group_sum<Gw>((Ts)(acc2.x + acc2.y), gmask);
 }
 #endif
 
-template <int Gw>
-__device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const float* sproto,
-                                                cdm_real* P, cdm_real* FixP, unsigned gmask) {
+// The group total is formed in Ts: double for the chain energies and the
+// reported costs, float for the grid search's ranking pass (whose near ties
+// are settled in FP64).
+template <int Gw, typename Ts = double>
+__device__ __forceinline__ Ts cdm_group_sse(const cdm_voxel_io& io, const float* sproto,
+                                            cdm_real* P, cdm_real* FixP, unsigned gmask) {
 #if CDM_SHELLS
-  if (io.shells) return cdm_group_sse_shells<Gw>(io, sproto, P, FixP, gmask);
+  if (io.shells) return cdm_group_sse_shells<Gw, Ts>(io, sproto, P, FixP, gmask);
 #endif
   float acc = 0.0f;
   const int full = io.nmeas / Gw;
@@ -365,7 +367,7 @@ __device__ __forceinline__ double cdm_group_sse(const cdm_voxel_io& io, const fl
     const float r = (float)Predicted_Signal(NPARAMS, P, cf, FixP) - *sig;
     acc = valid ? fmaf(r, r, acc) : acc;
   }
-  return cdm_group_sum<Gw>((double)acc, gmask);
+  return cdm_group_sum<Gw>((Ts)acc, gmask);
 }
 
 // log I0(x) with the polynomial approximations of Abramowitz & Stegun

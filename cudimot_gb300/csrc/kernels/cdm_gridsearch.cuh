@@ -7,8 +7,11 @@
 // :216). Combination order is Model.cu's set_grid order.
 //
 // GB300 structure: costs are evaluated in FP32 (each lane sums its own
-// measurements, the group total in FP64). Each group tracks its four best
-// combinations. If the runner-up lies within `band` (relative) of the best,
+// measurements, the group total too) and ranked in FP32; the grid is read
+// as floats, and which combinations pass the bounds test is decided once
+// per grid on the host (grid_ok), so the loop over combinations runs no FP64
+// instruction (the FP64 pipe is 1/64 of the FP32 rate on this GPU). Each
+// group tracks its four best combinations. If the runner-up lies within `band` (relative) of the best,
 // the FP32 ranking is not trusted: the voxel is flagged and
 // cdm_gs_recheck_kernel re-evaluates the candidates (or, when more than
 // three are within the band, every combination) in FP64 with CUDIMOT's
@@ -21,18 +24,10 @@
 
 
 __device__ __forceinline__ bool cdm_gs_in_bounds(const cdm_limits& lim, const double* x) {
+  bool in = true;
 #pragma unroll
-  for (int p = 0; p < kNP; p++) {
-    if (lim.btype[p] == BMIN) {
-      if (x[p] < (double)lim.bmin[p]) return false;
-    } else if (lim.btype[p] == BMAX) {
-      if (x[p] > (double)lim.bmax[p]) return false;
-    } else if (lim.btype[p] == BMINMAX) {
-      if (x[p] < (double)lim.bmin[p]) return false;
-      if (x[p] > (double)lim.bmax[p]) return false;
-    }
-  }
-  return true;
+  for (int p = 0; p < kNP; p++) in = in && cdm_in_bounds1(lim, p, x[p]);
+  return in;
 }
 
 template <int Gw>
@@ -66,27 +61,38 @@ CDM_KERNEL(CDM_NT) cdm_gridsearch_kernel(CDM_KARG(cdm_gs_args) a) {
   for (int p = 0; p < kNP; p++) base[p] = a.params[(size_t)v * kNP + p];
   cdm_real FixP[kNFIX];
   cdm_load_fixp(a.fixp + (size_t)v * a.fixp_tsize, a.fixp_tsize, FixP);
+  cdm_real P[kNPS];
+#pragma unroll
+  for (int i = 0; i < kNPS; i++) P[i] = cdm_real(0.0f);
+#pragma unroll
+  for (int p = 0; p < kNP; p++) P[p] = cdm_real((float)base[p]);
 
-  double bcost[kGsTop];
+  if (a.cost_only) {  // the cost at the voxel's own parameters, FP64 group sum
+    cdm_update_derived(P, FixP);
+    const double cost = cdm_group_sse<Gw>(io, sproto, P, FixP, gm);
+    if (lane == 0) a.cost_out[v] = cost;
+    return;
+  }
+  // the voxel's own values of the parameters outside the grid are the same
+  // in every combination: tested once
+  bool base_in = true;
+#pragma unroll
+  for (int p = 0; p < kNP; p++) base_in = base_in && (a.gpos[p] >= 0 || cdm_in_bounds1(lim, p, base[p]));
+
+  float bcost[kGsTop];
   int bcomb[kGsTop];
 #pragma unroll
   for (int k = 0; k < kGsTop; k++) {
-    bcost[k] = 9e20;  // CUDIMOT's initial best cost (GridSearch.cu:178)
+    bcost[k] = 9e20f;  // CUDIMOT's initial best cost (GridSearch.cu:178)
     bcomb[k] = -1;
   }
-  for (int c = 0; c < a.combs; c++) {
-    double trial[kNP];
+  for (int c = 0; base_in && c < a.combs; c++) {
+    if (!((__ldg(a.grid_ok + (c >> 5)) >> (c & 31)) & 1u)) continue;
 #pragma unroll
     for (int p = 0; p < kNP; p++)
-      trial[p] = a.gpos[p] >= 0 ? __ldg(a.grid + (size_t)c * a.ngp + a.gpos[p]) : base[p];
-    if (!a.cost_only && !cdm_gs_in_bounds(lim, trial)) continue;
-    cdm_real P[kNPS];
-#pragma unroll
-    for (int i = 0; i < kNPS; i++) P[i] = cdm_real(0.0f);
-#pragma unroll
-    for (int p = 0; p < kNP; p++) P[p] = cdm_real((float)trial[p]);
+      if (a.gpos[p] >= 0) P[p] = cdm_real(__ldg(a.grid + (size_t)c * a.ngp + a.gpos[p]));
     cdm_update_derived(P, FixP);
-    const double cost = cdm_group_sse<Gw>(io, sproto, P, FixP, gm);
+    const float cost = cdm_group_sse<Gw, float>(io, sproto, P, FixP, gm);
     // Sorted insertion with constant indices (register arrays): entries
     // strictly worse than `cost` move down one place, equal costs keep the
     // earlier combination first (CUDIMOT's strict '<').
@@ -104,14 +110,12 @@ CDM_KERNEL(CDM_NT) cdm_gridsearch_kernel(CDM_KARG(cdm_gs_args) a) {
     }
   }
   if (lane != 0) return;
-  if (a.cost_out) a.cost_out[v] = bcost[0];
-  if (a.cost_only) return;
   a.best[v] = bcomb[0];
   if (bcomb[0] < 0) {
     a.flags[v] = 0;
     return;
   }
-  const double band_cost = bcost[0] * (1.0 + (double)a.band);
+  const double band_cost = (double)bcost[0] * (1.0 + (double)a.band);
   int nin = 0;
 #pragma unroll
   for (int k = 0; k < kGsTop; k++) nin += (bcomb[k] >= 0 && bcost[k] <= band_cost) ? 1 : 0;
@@ -120,7 +124,7 @@ CDM_KERNEL(CDM_NT) cdm_gridsearch_kernel(CDM_KARG(cdm_gs_args) a) {
   for (int k = 0; k < kGsTop; k++) a.cand[(size_t)v * kGsTop + k] = bcomb[k];
 #pragma unroll
   for (int p = 0; p < kNP; p++)
-    if (a.gpos[p] >= 0) a.params[(size_t)v * kNP + p] = a.grid[(size_t)bcomb[0] * a.ngp + a.gpos[p]];
+    if (a.gpos[p] >= 0) a.params[(size_t)v * kNP + p] = a.grid64[(size_t)bcomb[0] * a.ngp + a.gpos[p]];
 }
 
 // ----------------------------------------------------------------------------

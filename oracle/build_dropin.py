@@ -55,8 +55,9 @@ def build_all(reference=None, jobs=None):
     if reference:
         def dev(t):
             m, ev = t
+            # no source-line tables: the modules travel with the tests
             return build.split_device(os.path.join(reference, "mymodels", m), outdir(m, ev),
-                                      name=m, eval_type=ev)
+                                      name=m, eval_type=ev, lineinfo=False)
         with cf.ThreadPoolExecutor(jobs) as ex:
             for out, err in ex.map(dev, DROPIN):
                 if err:
