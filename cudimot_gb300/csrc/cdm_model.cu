@@ -448,11 +448,10 @@ cdm_status prep_protocol(cdm_ctx* c, int nmeas, const double* CFP, cudaStream_t 
 constexpr bool kShells = CDM_SHELLS != 0;
 
 size_t shell_sig_floats(int nvox, int nmeas, int Gw) {
-  // the tile-major shell layout (whole tiles of CDM_NT / Gw voxels), or
-  // the chunk-major layout when the table turns out invalid
-  const size_t tiles = ((size_t)std::max(nvox, 1) + CDM_NT / Gw - 1) / (CDM_NT / Gw);
-  return std::max(tiles * cdm_shell_sig_rows(nmeas, Gw) * 2 * CDM_NT,
-                  (size_t)((nmeas + Gw - 1) / Gw) * std::max(nvox, 1) * Gw);
+  // the per-shell layout (float2 pair rows), or the measurement-order
+  // layout when the table turns out invalid
+  return std::max(2 * cdm_tile_elems(nvox, cdm_shell_sig_rows(nmeas, Gw), Gw),
+                  cdm_tile_elems(nvox, (nmeas + Gw - 1) / Gw, Gw));
 }
 
 cdm_status prep_shells_and_pack(cdm_ctx* c, int Gw, int nvox, int nmeas, const double* CFP,
@@ -473,7 +472,7 @@ cdm_status prep_shells_and_pack(cdm_ctx* c, int Gw, int nvox, int nmeas, const d
 cdm_status pack_signals(cdm_ctx* c, int Gw, int nvox, int nmeas, const double* meas, cudaStream_t st) {
   if (cdm_lane_index(Gw) < 0) return cdm_fail(CDM_BAD_ARG, "lanes per voxel must be 1, 2, 4, 8, 16 or 32");
   const int nchunk = (nmeas + Gw - 1) / Gw;
-  CDM_TRY(dev_alloc(&c->sig, &c->sig_cap, (size_t)nchunk * std::max(nvox, 1) * Gw));
+  CDM_TRY(dev_alloc(&c->sig, &c->sig_cap, cdm_tile_elems(nvox, nchunk, Gw)));
   if (nvox == 0) return CDM_OK;
   const size_t total = (size_t)nchunk * nvox * Gw;
   const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)c->num_sms * 32);
@@ -751,7 +750,7 @@ cdm_status fit_sequence(cdm_ctx* c, int nvox, int nmeas, const double* meas, dou
 size_t fit_sig_floats(const cdm_ctx* c, int nvox, int nmeas) {
   size_t sig = 0;
   for (int Gw : {1, 2, 4, 8, 16, 32})
-    sig = std::max(sig, (size_t)((nmeas + Gw - 1) / Gw) * std::max(nvox, 1) * Gw);
+    sig = std::max(sig, cdm_tile_elems(nvox, (nmeas + Gw - 1) / Gw, Gw));
   if (kShells)
     for (int Gw : {pick_lanes(c, c->cfg.lanes_gridsearch, 2, nvox), pick_lanes(c, c->cfg.lanes_mcmc, 2, nvox)})
       sig = std::max(sig, shell_sig_floats(nvox, nmeas, Gw));
@@ -1454,7 +1453,7 @@ cdm_status noalloc_lm_launch(int Gw, const cdm_model_cfg* cfg, unsigned char* sc
   const int pad = round_up(nmeas, 32);
   const int nchunk = (nmeas + Gw - 1) / Gw;
   const size_t pbytes = proto_bytes(pad);
-  const size_t sbytes = (size_t)nchunk * nvox * Gw * sizeof(float);
+  const size_t sbytes = cdm_tile_elems(nvox, nchunk, Gw) * sizeof(float);
   const size_t soff = kNoAllocHeader + (pbytes + 255) / 256 * 256;
   if (soff + sbytes > kNoAllocScratchBytes)
     return cdm_fail(CDM_BAD_ARG,

@@ -70,19 +70,25 @@ constexpr int kShellHeader = 32;  // ints: valid, nshell, npos, then per shell r
 __host__ __device__ constexpr int cdm_shell_max_pos(int nmeas, int Gw) {
   return nmeas + kShellMax * (2 * Gw - 1);
 }
-// Signals of the per-shell path: pair-interleaved (element = the lane's
-// measurements of two consecutive lane chunks, one 8-byte load) and
-// tile-major: the voxels of one CTA (CDM_NT / Gw of them) keep all their
-// pair rows in one contiguous block, [tile][pair row][voxel in tile][lane],
-// so the signals that the resident CTAs re-read on every proposal form one
-// contiguous stretch of memory (with one row per voxel range instead, their
-// L2 misses varied 3x with the buffer's placement). Within a tile the next
-// pair row of a lane is CDM_NT elements on.
+// Packed signals are tile-major: the voxels of one CTA (a tile, CDM_NT / Gw
+// of them) keep all their rows in one contiguous block, [tile][row][voxel in
+// tile][lane], so the signals that the resident CTAs re-read on every pass
+// or proposal form one contiguous stretch of memory (with each row spanning
+// all voxels instead, the rows lay megabytes apart and the MCMC's L2 misses
+// varied 3x with the buffer's placement). A row is one lane chunk (one
+// float per lane) in measurement order, or in the per-shell path one pair of
+// chunks (a float2 per lane, one 8-byte load). Within a tile the next row
+// of a lane is CDM_NT elements on.
+__host__ __device__ constexpr size_t cdm_tile_index(int v, int row, int j, int rows, int Gw) {
+  return (((size_t)(v / (CDM_NT / Gw)) * rows + row) * (CDM_NT / Gw) + v % (CDM_NT / Gw)) * Gw + j;
+}
+// Elements of the packed signals of nvox voxels with `rows` rows (whole tiles).
+__host__ __device__ constexpr size_t cdm_tile_elems(int nvox, int rows, int Gw) {
+  return ((size_t)(nvox > 1 ? nvox : 1) + CDM_NT / Gw - 1) / (CDM_NT / Gw) * rows * CDM_NT;
+}
+// Pair rows the per-shell layout may need.
 __host__ __device__ constexpr int cdm_shell_sig_rows(int nmeas, int Gw) {
   return (cdm_shell_max_pos(nmeas, Gw) + 2 * Gw - 1) / (2 * Gw);
-}
-__host__ __device__ constexpr size_t cdm_shell_sig_index(int v, int k, int j, int rows, int Gw) {
-  return (((size_t)(v / (CDM_NT / Gw)) * rows + k) * (CDM_NT / Gw) + v % (CDM_NT / Gw)) * Gw + j;
 }
 // Floats of the shell table that follows the staged protocol: the header,
 // then 4 floats (gx, gy, gz, weight) per padded position.

@@ -196,8 +196,8 @@ __device__ __forceinline__ void cdm_load_cfp(const float* sproto, int nmeas_pad,
 
 // Per-voxel view handed to the group cost routines.
 struct cdm_voxel_io {
-  const float* sig;  // this lane's first signal value (chunk 0)
-  size_t chunk_stride;
+  const float* sig;  // this lane's first signal value (chunk 0, tile-major: cdm_tile_index)
+  size_t chunk_stride;  // to the lane's next chunk: CDM_NT floats
   int nchunk;
   int nmeas;
   int nmeas_pad;
@@ -206,7 +206,7 @@ struct cdm_voxel_io {
   const int* shells;   // shell-table header in shared memory, or null (per-measurement path)
   const float* stab;   // this lane's first shell pair entry
   const float2* sig2;  // shell order: this lane's first pair of signals (pair-interleaved,
-                       // tile-major: cdm_shell_sig_index; pairs CDM_NT float2 apart)
+                       // tile-major: cdm_tile_index; pairs CDM_NT float2 apart)
 };
 
 // Build the pair table (see the layout notes above) after the staged

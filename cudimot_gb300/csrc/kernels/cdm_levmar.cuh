@@ -169,8 +169,8 @@ CDM_KERNEL(CDM_NT) cdm_levmar_kernel(CDM_KARG(cdm_lm_args) a) {
   const cdm_limits& lim = a.lim;
 
   cdm_voxel_io io;
-  io.sig = a.sig + (size_t)v * Gw + lane;
-  io.chunk_stride = (size_t)a.nvox * Gw;
+  io.sig = a.sig + cdm_tile_index(v, 0, lane, a.nchunk, Gw);
+  io.chunk_stride = CDM_NT;
   io.nchunk = a.nchunk;
   io.nmeas = a.nmeas;
   io.nmeas_pad = a.nmeas_pad;

@@ -158,11 +158,11 @@ CDM_KERNEL(CDM_NT, CDM_MCMC_MIN_BLOCKS) cdm_mcmc_kernel(CDM_KARG(cdm_mcmc_args) 
   const cdm_limits& lim = a.lim;
 
   cdm_voxel_io io;
-  io.sig = a.sig + (size_t)v * Gw + lane;
+  io.sig = a.sig + cdm_tile_index(v, 0, lane, a.nchunk, Gw);
   io.sig2 = shdr ? reinterpret_cast<const float2*>(a.sig) +
-                       cdm_shell_sig_index(v, 0, lane, shdr[2] / (2 * Gw), Gw)
+                       cdm_tile_index(v, 0, lane, shdr[2] / (2 * Gw), Gw)
                  : nullptr;
-  io.chunk_stride = (size_t)a.nvox * Gw;
+  io.chunk_stride = CDM_NT;
   io.nchunk = a.nchunk;
   io.nmeas = a.nmeas;
   io.nmeas_pad = a.nmeas_pad;

@@ -152,8 +152,9 @@ CDM_KERNEL0 cdm_prep_protocol_kernel(const double* __restrict__ cfp, int nmeas, 
   }
 }
 
-// Signals: [nvox][nmeas] double -> [nchunk][nvox][Gw] float, so that the Gw
-// lanes of consecutive groups read one contiguous line per chunk.
+// Signals: [nvox][nmeas] double -> float, tile-major (cdm_tile_index): row
+// c of a tile holds chunk c (measurement c * Gw + lane) of its voxels, so
+// the Gw lanes of consecutive groups read one contiguous line per chunk.
 template <int Gw>
 CDM_KERNEL0 cdm_pack_signals_kernel(const double* __restrict__ meas, int nvox, int nmeas,
                                         int nchunk, float* __restrict__ out) {
@@ -165,7 +166,7 @@ CDM_KERNEL0 cdm_pack_signals_kernel(const double* __restrict__ meas, int nvox, i
     const int v = (int)(rest % nvox);
     const int c = (int)(rest / nvox);
     const int m = c * Gw + j;
-    out[i] = m < nmeas ? (float)meas[(size_t)v * nmeas + m] : 0.0f;
+    out[cdm_tile_index(v, c, j, nchunk, Gw)] = m < nmeas ? (float)meas[(size_t)v * nmeas + m] : 0.0f;
   }
 }
 
@@ -310,7 +311,7 @@ CDM_KERNEL0 cdm_pack_shell_signals_kernel(const double* __restrict__ meas, int n
   const int* hdr = reinterpret_cast<const int*>(table);
   const bool shells = hdr[0] != 0;
   if (shells) {
-    // pair-interleaved, tile-major (cdm_shell_sig_index): element (pair k,
+    // pair-interleaved, tile-major (cdm_tile_index): element (pair k,
     // voxel v, lane j) holds the lane's positions of chunks 2k and 2k + 1
     const int npairs = hdr[2] / (2 * Gw);
     const size_t total = (size_t)npairs * nvox * Gw;
@@ -323,7 +324,7 @@ CDM_KERNEL0 cdm_pack_shell_signals_kernel(const double* __restrict__ meas, int n
       const int k = (int)(rest / nvox);
       const int m0 = perm[(2 * k) * Gw + j], m1 = perm[(2 * k + 1) * Gw + j];
       const double* row = meas + (size_t)v * nmeas;
-      out2[cdm_shell_sig_index(v, k, j, npairs, Gw)] = make_float2(m0 >= 0 ? (float)row[m0] : 0.0f, m1 >= 0 ? (float)row[m1] : 0.0f);
+      out2[cdm_tile_index(v, k, j, npairs, Gw)] = make_float2(m0 >= 0 ? (float)row[m0] : 0.0f, m1 >= 0 ? (float)row[m1] : 0.0f);
     }
     return;
   }
@@ -335,7 +336,7 @@ CDM_KERNEL0 cdm_pack_shell_signals_kernel(const double* __restrict__ meas, int n
     const int v = (int)(rest % nvox);
     const int c = (int)(rest / nvox);
     const int p = c * Gw + j;
-    out[i] = p < nmeas ? (float)meas[(size_t)v * nmeas + p] : 0.0f;
+    out[cdm_tile_index(v, c, j, nchunk, Gw)] = p < nmeas ? (float)meas[(size_t)v * nmeas + p] : 0.0f;
   }
 }
 #endif
