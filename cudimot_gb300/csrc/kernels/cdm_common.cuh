@@ -14,8 +14,11 @@
 // HBM layouts the kernels read (built by cdm_pack_* kernels):
 //   protocol  float [nmeas_pad][NCOLS4]  NCOLS = CFP_Tsize + derived CFP,
 //                                        rows padded to NCOLS4 (16 bytes)
-//   signals   float [nchunk][nvox][Gw]    chunk c holds measurements cG..cG+Gw-1
-// so a warp's signal load is one contiguous 128-byte line.
+//   signals   float [nvox/T][nchunk][T][Gw]  tile-major (cdm_tile_index, T =
+//                                        CDM_NT / Gw voxels per CTA); row c
+//                                        holds measurements cG..cG+Gw-1
+// so a warp's signal load is one contiguous 128-byte line and a CTA's
+// signals are one contiguous block.
 // With the paired signal hook (Predicted_Signal_Pair) the kernels that take
 // the paired cost loop also keep, after the staged protocol in shared
 // memory, a pair table float2 [nchunk/2][Gw][NCOLSP] (NCOLS rounded up to

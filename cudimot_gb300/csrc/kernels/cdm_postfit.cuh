@@ -300,10 +300,10 @@ CDM_KERNEL0 cdm_prep_shells_kernel(const double* __restrict__ cfp, int nmeas, in
   }
 }
 
-// Signals in the shell order of the table, pair-interleaved
-// ([npos / (2 Gw)][nvox][Gw][2]: a lane's positions of chunks 2k and 2k + 1
-// side by side, 0 on padding), or in measurement order as
-// cdm_pack_signals_kernel ([nchunk][nvox][Gw]) when the table is invalid.
+// Signals in the shell order of the table, pair-interleaved and tile-major
+// ([nvox/T][npos / (2 Gw)][T][Gw][2]: a lane's positions of chunks 2k and
+// 2k + 1 side by side, 0 on padding), or in measurement order as
+// cdm_pack_signals_kernel when the table is invalid.
 template <int Gw>
 CDM_KERNEL0 cdm_pack_shell_signals_kernel(const double* __restrict__ meas, int nvox, int nmeas,
                                           int nchunk, const float* __restrict__ table,
